@@ -1,0 +1,211 @@
+/*
+ * tmgpu.h - C ABI of the GB300 (sm_103a) BP+EE energy-and-force library.
+ *
+ * This is the drop-in boundary for TensorMol's energy/force hot path: the
+ * neighbour lists, ANI-1 descriptors, per-element BP energy and charge
+ * networks, DSF/elu Coulomb + C6 vdW between the network charges, forces,
+ * and the integrators that consume them. Plain C types only: host or device
+ * pointers and sizes, int status returns, no exceptions across the ABI.
+ *
+ * Units at the boundary are the reference's: positions in Angstrom, energies
+ * in Hartree, forces in J mol^-1 A^-1 (TFNetworks/TFMolManage.py:1439),
+ * velocities in A/fs and masses in kg/mol (Simulations/SimpleMD.py:14-51).
+ *
+ * Threading: one tm_ctx per host thread; calls on one ctx are not re-entrant.
+ */
+#ifndef TMGPU_H
+#define TMGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (every entry point returns one) ---------------------- */
+#define TM_OK 0
+#define TM_E_ARG 1          /* invalid argument or unsupported shape        */
+#define TM_E_CUDA 2         /* CUDA runtime/driver error                    */
+#define TM_E_CAPACITY 3     /* neighbour capacity exceeded (retry larger)   */
+#define TM_E_NONFINITE 4    /* non-finite positions or outputs              */
+#define TM_E_BUDGET 5       /* allocation would exceed the ctx HBM budget   */
+#define TM_E_TIMEOUT 6      /* a bounded device wait gave up                */
+#define TM_E_STATE 7        /* call out of order (e.g. weights not final)   */
+#define TM_E_UNSUPPORTED 8  /* feature not available in this build          */
+
+/* ---- enums ------------------------------------------------------------- */
+/* Activations of Instance.AssignActivation (TFNetworks/TFInstance.py:108-140) */
+#define TM_ACT_RELU 0
+#define TM_ACT_SIGMOID_WITH_PARAM 1 /* log(1+exp(a x))/a, Util.py:200-201 */
+#define TM_ACT_SOFTPLUS 2
+#define TM_ACT_TANH 3
+#define TM_ACT_ELU 4
+
+/* Arithmetic of the network GEMMs (descriptors, Coulomb and adjoint are FP32) */
+#define TM_PREC_FP32 0   /* 3-pass split TF32 on tcgen05, FP32 accumulate      */
+#define TM_PREC_BF16 1   /* 1-pass BF16 on tcgen05, FP32 accumulate            */
+
+/* tm_energy_force flags */
+#define TM_F_ENERGY_ONLY 1u   /* DoForce=False (samples/test_tensormol01.py:61-69) */
+#define TM_F_DEVICE_IO 2u     /* x/outputs are device pointers on the ctx stream */
+#define TM_F_REUSE_NLIST 4u   /* keep the current lists (caller rebuilt them)    */
+#define TM_F_REFERENCE_PERIODIC_FORCE 8u /* periodic: drop image-side terms as
+                                            the reference's gradient does      */
+
+/* MD integrator kinds (Simulations/SimpleMD.py) */
+#define TM_MD_NVE 0        /* VelocityVerletStep, SimpleMD.py:14-38          */
+#define TM_MD_NOSE 1       /* NoseThermostat.step, SimpleMD.py:104-129       */
+#define TM_MD_NHC 2        /* Nose-Hoover chain, Martyna et al. 1996 (see docs) */
+
+typedef struct tm_ctx tm_ctx;
+typedef struct tm_model tm_model;
+typedef struct tm_system tm_system;
+typedef struct tm_md tm_md;
+
+/*
+ * Model description. Mirrors MolInstance_DirectBP_EE_SymFunction's
+ * constructor and SetANI1Param (TFNetworks/TFBehlerParinelloSymEE.py:660-777)
+ * reading PARAMS (TMParams.py:26-37, 57-79, 140-154).
+ */
+typedef struct tm_model_desc {
+  int n_elements;          /* sorted atomic numbers in elements[]            */
+  int elements[8];
+  int n_hidden;            /* HiddenLayers, e.g. {512, 512, 512}             */
+  int hidden[4];
+  int activation;          /* TM_ACT_*                                       */
+  double sigmoid_alpha;    /* PARAMS["sigmoid_alpha"]                        */
+  double r_rc, a_rc;       /* AN1_r_Rc, AN1_a_Rc                             */
+  double eta, zeta;        /* AN1_eta, AN1_zeta                              */
+  int n_r_rs, n_a_rs, n_a_as; /* AN1_num_r_Rs, AN1_num_a_Rs, AN1_num_a_As    */
+  double ee_cut_on;        /* EECutoffOn (must be 0, as the reference asserts) */
+  double ee_cut_off;       /* EECutoffOff                                    */
+  double elu_width;        /* Elu_Width                                      */
+  double dsf_alpha;        /* DSFAlpha                                       */
+  double poly_width;       /* Poly_Width                                     */
+  int add_ecc;             /* AddEcc                                         */
+  int has_vdw;             /* HasVdw argument of EvalBPDirectEE*             */
+  int precision;           /* TM_PREC_*                                      */
+} tm_model_desc;
+
+/* ---- context ----------------------------------------------------------- */
+/* hbm_budget_bytes = 0 means no limit beyond the device. */
+int tm_ctx_create(int device, size_t hbm_budget_bytes, tm_ctx **out);
+int tm_ctx_destroy(tm_ctx *ctx);
+/* Use a caller-owned cudaStream_t (NULL = the ctx's own stream). */
+int tm_ctx_set_stream(tm_ctx *ctx, void *cuda_stream);
+void *tm_ctx_stream(tm_ctx *ctx);
+/* Last error message (after any non-zero return). */
+int tm_ctx_last_error(tm_ctx *ctx, char *buf, int len);
+size_t tm_ctx_bytes_in_use(tm_ctx *ctx);
+/* Kernels launched by this ctx since creation (a counter kept on the host). */
+int64_t tm_ctx_launch_count(tm_ctx *ctx);
+
+/* ---- model ------------------------------------------------------------- */
+/* Replaces MolInstance_DirectBP_EE_SymFunction.__init__ + EvalPrepare
+ * (TFBehlerParinelloSymEE.py:660-736, 1452-1501). */
+int tm_model_create(tm_ctx *ctx, const tm_model_desc *desc, tm_model **out);
+/*
+ * One dense layer of one element's network: W[fan_in][fan_out] row-major and
+ * b[fan_out] (the reference's tf.matmul(inputs, weights) + biases orientation,
+ * TFBehlerParinelloSymEE.py:914-929 for net 0 = EnergyNet, :975-996 for
+ * net 1 = DipoleNet). layer = 0..n_hidden (the last is the 1-wide output).
+ */
+int tm_model_set_layer(tm_model *m, int net, int element_index, int layer,
+                       const double *W, const double *b, int fan_in, int fan_out);
+int tm_model_finalize(tm_model *m);
+int tm_model_descriptor_width(const tm_model *m);
+int tm_model_destroy(tm_model *m);
+
+/* ---- system (atoms, molecules, cell, device-resident state) ------------ */
+/*
+ * A batch of molecules in CSR order: atoms of molecule m are
+ * mol_offsets[m] .. mol_offsets[m+1]-1. Replaces the padded
+ * [nmol, MaxNAtoms] feed of EvalBPDirectEEUpdateSet (TFMolManage.py:1260-1276).
+ * cell: NULL for open boundaries, else 9 doubles of lattice vectors (rows);
+ * only orthorhombic cells with every edge >= 2 * the largest cutoff are
+ * accepted. Z is host memory.
+ */
+int tm_system_create(tm_model *m, int natoms, int nmol, const int32_t *Z,
+                     const int64_t *mol_offsets, const double *cell, tm_system **out);
+int tm_system_destroy(tm_system *s);
+int tm_system_natoms(const tm_system *s);
+/* Positions [natoms][3] in Angstrom; device pointer if on_device. */
+int tm_system_set_positions(tm_system *s, const double *x, int on_device);
+int tm_system_get_positions(tm_system *s, double *x, int on_device);
+
+/*
+ * Builds the radial (r < AN1_r_Rc, both directions) and angular (r < AN1_a_Rc)
+ * neighbour lists from the current positions with the reference's FP64
+ * membership test. Replaces NeighborListSet.buildPairsAndTriplesWithEleIndex-
+ * Linear/Periodic (ForceModifiers/Neighbors.py:344-470) and MolEmb.Make_NList-
+ * Naive (C_API/MolEmb.cpp:1180-1251).
+ */
+int tm_system_build_nlist(tm_system *s);
+/* counts[0] = radial pairs P, [1] = triples T, [2] = Coulomb pairs (i<j,
+ * r < EECutoffOff; periodic: both directions as the reference lists them),
+ * [3] = max radial neighbours of one atom. */
+int tm_system_nlist_counts(tm_system *s, int64_t counts[4]);
+/*
+ * Exports the lists in the reference's layout and sorted order:
+ * radp[P][4] = (mol, i, j, l), angt[T][5] = (mol, i, j, k, l),
+ * mil_j[P][4], mil_jk[T][4] = (mol, i, l, slot) (Neighbors.py:344-467),
+ * eep[Pee][3] = (mol, i, j) (TFMolManage.py:1430-1431; periodic:
+ * (mol, i, j) with j an index into the 27-image tessellation,
+ * Periodic.py:131-181). Atom indices are molecule-local. Any pointer may be
+ * NULL. Host int64 buffers unless on_device.
+ */
+int tm_system_export_nlist(tm_system *s, int64_t *radp, int64_t *angt, int64_t *mil_j,
+                           int64_t *mil_jk, int on_device);
+int tm_system_export_ee(tm_system *s, int64_t *eep, int64_t cap, int on_device);
+
+/*
+ * Energy and forces: EvalBPDirectEELinearSingle / EvalBPDirectEEUpdateSet /
+ * EvalBPDirectEEUpdateSinglePeriodic (TFMolManage.py:1260-1358, 1410-1439).
+ * x: positions [natoms][3] (NULL = use the resident ones).
+ * E_out[nmol][4] = (Etotal, Ebp, Ecc, Evdw) in Hartree.
+ * F_out[natoms][3] in J/mol/A (ignored with TM_F_ENERGY_ONLY).
+ * q_out[natoms] neutralised charges, dipole_out[nmol][3] (bohr * e), may be NULL.
+ * Eatom_out[natoms] per-atom network energies (Ebp_atom), may be NULL.
+ */
+int tm_energy_force(tm_system *s, const double *x, unsigned flags, double *E_out,
+                    double *F_out, double *q_out, double *dipole_out, double *Eatom_out);
+
+/* ---- molecular dynamics (device-resident FP64 state) ------------------- */
+/*
+ * kind: TM_MD_NVE / TM_MD_NOSE / TM_MD_NHC. dt in fs, T in K, chain = NHC
+ * length. Masses come from Z (PhysicalData.ATOMICMASSES). The first
+ * acceleration is zero, as VelocityVerlet.__init__ sets it (SimpleMD.py:359).
+ */
+int tm_md_create(tm_system *s, int kind, double dt_fs, double T_kelvin, int chain,
+                 tm_md **out);
+int tm_md_destroy(tm_md *md);
+int tm_md_set_velocities(tm_md *md, const double *v, int on_device);
+int tm_md_get_velocities(tm_md *md, double *v, int on_device);
+/*
+ * nsteps integrator steps, each with one energy+force evaluation and a
+ * neighbour-list rebuild when any atom moved more than skin/2 since the last
+ * build (skin = 0: rebuild every step). log[nsteps][4] (host, may be NULL) =
+ * (potential Hartree, kinetic J/mol per atom, conserved J/mol, T_eff K).
+ */
+int tm_md_run(tm_md *md, int nsteps, double skin, double *log);
+
+/* ---- diagnostics (used by the test-suite) ------------------------------ */
+/*
+ * Runs the tensor-core layer kernel alone: C[M][N] = A[M][K] . B[N][K]^T on
+ * host FP32 arrays, in the given precision. M % 128 == 0, N % 256 == 0,
+ * K % 64 == 0. No counterpart in the reference (it has no GPU kernels).
+ */
+int tm_selftest_gemm(tm_ctx *ctx, int precision, int M, int N, int K, const float *A,
+                     const float *B, float *C);
+/*
+ * Descriptor rows of every atom in atom order, FP32 [natoms][D], for the
+ * current positions (lists are built if needed). Replaces reading
+ * TFSymSet_Scattered_Linear_WithEle_Release's SymList (RawSymFunc.py:2267-2309).
+ */
+int tm_system_descriptors(tm_system *s, float *G_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TMGPU_H */

@@ -1,0 +1,770 @@
+// C ABI entry points: context, model, system, energy/force, neighbour export.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "tm_internal.h"
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+int tm_fail(tm_ctx* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+int tm_cuda_check(tm_ctx* ctx, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return TM_OK;
+  return tm_fail(ctx, TM_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int tm_alloc(tm_ctx* ctx, void** p, size_t bytes) {
+  *p = nullptr;
+  if (bytes == 0) bytes = 16;
+  if (ctx->budget && ctx->in_use + bytes > ctx->budget)
+    return tm_fail(ctx, TM_E_BUDGET, "allocation exceeds the HBM budget");
+  cudaError_t e = cudaMallocAsync(p, bytes, ctx->stream);
+  if (e != cudaSuccess) return tm_cuda_check(ctx, e, "cudaMallocAsync");
+  ctx->in_use += bytes;
+  return TM_OK;
+}
+
+void tm_free(tm_ctx* ctx, void* p, size_t bytes) {
+  if (!p) return;
+  if (bytes == 0) bytes = 16;
+  cudaFreeAsync(p, ctx->stream);
+  ctx->in_use -= std::min(ctx->in_use, bytes);
+}
+
+static const char* status_where(int w) {
+  switch (w) {
+    case 1: return "positions";
+    case 2: return "cell grid";
+    case 100: case 101: case 102: return "tensor-core GEMM";
+    default: return "kernel";
+  }
+}
+
+int tm_sync_status(tm_ctx* ctx, const char* what) {
+  int rc = tm_cuda_check(ctx, cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(tm_dev_status),
+                                              cudaMemcpyDeviceToHost, ctx->stream),
+                         what);
+  if (rc) return rc;
+  if ((rc = tm_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), what))) return rc;
+  const tm_dev_status s = *ctx->h_status;
+  if (s.code) {
+    cudaMemsetAsync(ctx->d_status, 0, sizeof(tm_dev_status), ctx->stream);
+    return tm_fail(ctx, s.code, std::string(what) + ": device status " + std::to_string(s.code) +
+                                    " in " + status_where(s.where) + " (detail " +
+                                    std::to_string(s.detail) + ")");
+  }
+  return TM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+extern "C" int tm_ctx_create(int device, size_t budget, tm_ctx** out) {
+  *out = nullptr;
+  tm_ctx* c = new tm_ctx();
+  c->device = device;
+  c->budget = budget;
+  int rc;
+  if ((rc = tm_cuda_check(c, cudaSetDevice(device), "cudaSetDevice"))) { delete c; return rc; }
+  if ((rc = tm_cuda_check(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream"))) {
+    delete c;
+    return rc;
+  }
+  c->own_stream = true;
+  if ((rc = tm_cuda_check(c, cudaMalloc(&c->d_status, sizeof(tm_dev_status)), "status")) ||
+      (rc = tm_cuda_check(c, cudaMallocHost(&c->h_status, sizeof(tm_dev_status)), "status")) ||
+      (rc = tm_cuda_check(c, cudaMemset(c->d_status, 0, sizeof(tm_dev_status)), "status"))) {
+    delete c;
+    return rc;
+  }
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+          cudaSuccess &&
+      q == cudaDriverEntryPointSuccess)
+    c->encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  *out = c;
+  return TM_OK;
+}
+
+extern "C" int tm_ctx_destroy(tm_ctx* c) {
+  if (!c) return TM_OK;
+  cudaStreamSynchronize(c->stream);
+  cudaFree(c->d_status);
+  cudaFreeHost(c->h_status);
+  if (c->own_stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return TM_OK;
+}
+
+extern "C" int tm_ctx_set_stream(tm_ctx* c, void* s) {
+  if (!c) return TM_E_ARG;
+  cudaStreamSynchronize(c->stream);
+  if (s) {
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    c->stream = (cudaStream_t)s;
+    c->own_stream = false;
+  }
+  return TM_OK;
+}
+
+extern "C" void* tm_ctx_stream(tm_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+extern "C" int tm_ctx_last_error(tm_ctx* c, char* buf, int len) {
+  if (!c || !buf || len <= 0) return TM_E_ARG;
+  snprintf(buf, (size_t)len, "%s", c->err.c_str());
+  return TM_OK;
+}
+
+extern "C" size_t tm_ctx_bytes_in_use(tm_ctx* c) { return c ? c->in_use : 0; }
+extern "C" int64_t tm_ctx_launch_count(tm_ctx* c) { return c ? c->launches : 0; }
+
+// ---------------------------------------------------------------------------
+// model
+// ---------------------------------------------------------------------------
+static double dsf_val(double r, double rc, double alpha) {
+  if (r > rc) return 0.0;
+  const double xx = alpha * rc, zz = erfc(xx) / rc, yy = 1.1283791671 * alpha * exp(-xx * xx) / rc;
+  return erfc(alpha * r) / r - zz + (r - rc) * (zz / rc + yy);
+}
+static double dsf_grad(double r, double rc, double alpha) {
+  if (r > rc) return 0.0;
+  const double xx = alpha * rc, zz = erfc(xx) / rc, yy = 1.1283791671 * alpha * exp(-xx * xx) / rc;
+  return -((erfc(alpha * r) / r / r + 1.1283791671 * alpha * exp(-alpha * r * alpha * r) / r) -
+           (zz / rc + yy));
+}
+
+static const double kBohr = 1.889725989;           // PhysicalData.py:30
+static const double kJph = 2625.499638 * 1000.0;   // PhysicalData.py:36-37
+static const double kC6[11] = {0, 0.14, 0.08, 1.16, 1.61, 3.13, 1.75, 1.23, 0.70, 0.75, 0.63};
+static const double kR0[11] = {0, 1.001, 1.012, 0.825, 1.408, 1.485, 1.452, 1.397, 1.342, 1.287, 1.243};
+
+extern "C" int tm_model_create(tm_ctx* ctx, const tm_model_desc* d, tm_model** out) {
+  *out = nullptr;
+  if (!ctx || !d) return TM_E_ARG;
+  if (d->n_elements < 1 || d->n_elements > TM_MAX_ELE)
+    return tm_fail(ctx, TM_E_ARG, "n_elements must be 1..8");
+  for (int e = 0; e < d->n_elements; ++e) {
+    if (d->elements[e] < 1 || d->elements[e] > 10)
+      return tm_fail(ctx, TM_E_UNSUPPORTED, "elements must be Z = 1..10 (vdW tables)");
+    if (e && d->elements[e] <= d->elements[e - 1])
+      return tm_fail(ctx, TM_E_ARG, "elements must be sorted and unique");
+  }
+  if (d->n_hidden < 1 || d->n_hidden > 3)
+    return tm_fail(ctx, TM_E_UNSUPPORTED, "1 to 3 hidden layers are supported");
+  if (d->n_r_rs < 1 || d->n_r_rs > 32 || d->n_a_rs != 8 || d->n_a_as != 8)
+    return tm_fail(ctx, TM_E_UNSUPPORTED, "AN1_num_r_Rs <= 32, AN1_num_a_Rs = AN1_num_a_As = 8");
+  if (d->ee_cut_on != 0.0)
+    return tm_fail(ctx, TM_E_ARG, "EECutoffOn should equal to zero in DSF_elu");
+  if (!(d->a_rc > 0 && d->a_rc <= d->r_rc)) return tm_fail(ctx, TM_E_ARG, "need 0 < AN1_a_Rc <= AN1_r_Rc");
+  if (d->precision != TM_PREC_FP32 && d->precision != TM_PREC_BF16)
+    return tm_fail(ctx, TM_E_ARG, "precision");
+  tm_model* m = new tm_model();
+  m->ctx = ctx;
+  m->desc = *d;
+  tm_consts& k = m->k;
+  memset(&k, 0, sizeof(k));
+  k.nele = d->n_elements;
+  k.nelep = k.nele * (k.nele + 1) / 2;
+  k.nr = d->n_r_rs;
+  k.na_rs = 8;
+  k.na_as = 8;
+  k.D = k.nele * k.nr + k.nelep * 64;
+  k.Dp = ((k.D + TM_BN - 1) / TM_BN) * TM_BN;
+  k.act = d->activation;
+  k.alpha_sig = (float)d->sigmoid_alpha;
+  k.r_rc = (float)d->r_rc;
+  k.a_rc = (float)d->a_rc;
+  k.eta = (float)d->eta;
+  k.zeta = (float)d->zeta;
+  k.zeta_pow2 = d->zeta == 8.0 ? 1 : 0;
+  k.pi_tf = 3.14159265359f;   // RawSymFunc.py:935-936, 1799
+  for (int n = 0; n < k.nr; ++n) k.rs_r[n] = (float)(d->r_rc * n / k.nr);
+  for (int n = 0; n < 8; ++n) {
+    k.rs_a[n] = (float)(d->a_rc * n / 8.0);
+    const double th = 2.0 * M_PI * n / 8.0;
+    k.cos_th[n] = (float)cos(th);
+    k.sin_th[n] = (float)sin(th);
+  }
+  k.two_1mz = (float)pow(2.0, 1.0 - d->zeta);
+  int p = 0;
+  for (int a = 0; a < k.nele; ++a)
+    for (int b = a; b < k.nele; ++b) {
+      k.elepair[a][b] = p;
+      k.elepair[b][a] = p;
+      ++p;
+    }
+  // TFBehlerParinelloSymEE.py:719-729, RawSymFunc.py:1323-1324
+  const double alpha = d->dsf_alpha / kBohr, r_lr = d->ee_cut_off * kBohr, r_sr = d->elu_width * kBohr;
+  k.bohr = (float)kBohr;
+  k.alpha = (float)alpha;
+  k.r_lr = (float)r_lr;
+  k.r_sr = (float)r_sr;
+  k.elu_shift = (float)dsf_val(r_sr, r_lr, alpha);
+  k.elu_a = (float)dsf_grad(r_sr, r_lr, alpha);
+  k.zz = (float)(erfc(alpha * r_lr) / r_lr);
+  k.yy = (float)(1.1283791671 * alpha * exp(-alpha * r_lr * alpha * r_lr) / r_lr);
+  k.vdw_width = (float)(d->poly_width * kBohr);
+  k.vdw_begin = (float)(d->ee_cut_on * kBohr);
+  for (int e = 0; e < k.nele; ++e) {
+    const int z = d->elements[e];
+    k.c6[e] = (float)(kC6[z] * pow(kBohr * 10.0, 6.0) / kJph);
+    k.r0[e] = (float)(kR0[z] * kBohr);
+  }
+  k.r_rc_d = d->r_rc;
+  k.a_rc_d = d->a_rc;
+  k.ree_d = d->ee_cut_off;
+  k.ree = (float)d->ee_cut_off;
+  k.add_ecc = d->add_ecc ? 1 : 0;
+  k.has_vdw = d->has_vdw ? 1 : 0;
+  m->nlayer = d->n_hidden;
+  int hmax = 0;
+  for (int l = 0; l < d->n_hidden; ++l) {
+    if (d->hidden[l] < 1) { delete m; return tm_fail(ctx, TM_E_ARG, "hidden width"); }
+    hmax = std::max(hmax, d->hidden[l]);
+  }
+  m->H = ((hmax + TM_BN - 1) / TM_BN) * TM_BN;
+  m->elem_size = d->precision == TM_PREC_FP32 ? 4 : 2;
+  m->layers.resize((size_t)2 * k.nele * (m->nlayer + 1));
+  *out = m;
+  return TM_OK;
+}
+
+extern "C" int tm_model_descriptor_width(const tm_model* m) { return m ? m->k.D : -1; }
+
+extern "C" int tm_model_set_layer(tm_model* m, int net, int e, int layer, const double* W,
+                                  const double* b, int fan_in, int fan_out) {
+  if (!m || !W || !b || net < 0 || net > 1 || e < 0 || e >= m->k.nele || layer < 0 ||
+      layer > m->nlayer)
+    return tm_fail(m ? m->ctx : nullptr, TM_E_ARG, "set_layer index");
+  const int want_in = layer == 0 ? m->k.D : m->desc.hidden[layer - 1];
+  const int want_out = layer == m->nlayer ? 1 : m->desc.hidden[layer];
+  if (fan_in != want_in || fan_out != want_out)
+    return tm_fail(m->ctx, TM_E_ARG, "layer shape does not match the model description");
+  tm_layer_host& L = m->layers[((size_t)net * m->k.nele + e) * (m->nlayer + 1) + layer];
+  L.W.assign(W, W + (size_t)fan_in * fan_out);
+  L.b.assign(b, b + fan_out);
+  L.fan_in = fan_in;
+  L.fan_out = fan_out;
+  L.set = true;
+  m->final_ = false;
+  return TM_OK;
+}
+
+// pack one matrix into hi/lo (tf32) or bf16 device layout
+static int upload_split(tm_model* m, const std::vector<float>& host, void* out[2]) {
+  tm_ctx* ctx = m->ctx;
+  const size_t n = host.size();
+  int rc;
+  if (m->desc.precision == TM_PREC_FP32) {
+    std::vector<float> hi(n), lo(n);
+    for (size_t q = 0; q < n; ++q) {
+      uint32_t u;
+      memcpy(&u, &host[q], 4);
+      u &= 0xffffe000u;
+      memcpy(&hi[q], &u, 4);
+      lo[q] = host[q] - hi[q];
+    }
+    if ((rc = tm_alloc(ctx, &out[0], n * 4)) || (rc = tm_alloc(ctx, &out[1], n * 4))) return rc;
+    cudaMemcpyAsync(out[0], hi.data(), n * 4, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(out[1], lo.data(), n * 4, cudaMemcpyHostToDevice, ctx->stream);
+    return tm_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "upload");
+  }
+  std::vector<__nv_bfloat16> b(n);
+  for (size_t q = 0; q < n; ++q) b[q] = __float2bfloat16_rn(host[q]);
+  if ((rc = tm_alloc(ctx, &out[0], n * 2))) return rc;
+  out[1] = out[0];
+  cudaMemcpyAsync(out[0], b.data(), n * 2, cudaMemcpyHostToDevice, ctx->stream);
+  return tm_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "upload");
+}
+
+extern "C" int tm_model_finalize(tm_model* m) {
+  if (!m) return TM_E_ARG;
+  tm_ctx* ctx = m->ctx;
+  for (auto& L : m->layers)
+    if (!L.set) return tm_fail(ctx, TM_E_STATE, "every layer of both networks must be set");
+  const int nele = m->k.nele, L = m->nlayer, H = m->H, Dp = m->k.Dp;
+  auto layer = [&](int net, int e, int l) -> tm_layer_host& {
+    return m->layers[((size_t)net * nele + e) * (L + 1) + l];
+  };
+  int rc;
+  for (int l = 0; l < L; ++l) {
+    const int Kin = l == 0 ? Dp : H;
+    std::vector<float> fwd((size_t)2 * nele * H * Kin, 0.f), bwd((size_t)2 * nele * Kin * H, 0.f);
+    std::vector<float> bias((size_t)2 * nele * H, 0.f);
+    for (int net = 0; net < 2; ++net)
+      for (int e = 0; e < nele; ++e) {
+        const tm_layer_host& Lh = layer(net, e, l);
+        const size_t blk = (size_t)net * nele + e;
+        for (int i = 0; i < Lh.fan_in; ++i)
+          for (int o = 0; o < Lh.fan_out; ++o) {
+            const float w = (float)Lh.W[(size_t)i * Lh.fan_out + o];
+            fwd[(blk * H + o) * Kin + i] = w;     // W^T: [Nout][Kin]
+            bwd[(blk * Kin + i) * H + o] = w;     // W:   [Kin][Nout]
+          }
+        for (int o = 0; o < Lh.fan_out; ++o) bias[blk * H + o] = (float)Lh.b[o];
+      }
+    if ((rc = upload_split(m, fwd, m->w_fwd[l])) || (rc = upload_split(m, bwd, m->w_bwd[l]))) return rc;
+    if ((rc = tm_alloc(ctx, (void**)&m->bias[l], bias.size() * 4))) return rc;
+    cudaMemcpyAsync(m->bias[l], bias.data(), bias.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
+    const int eb = (int)m->elem_size;
+    if ((rc = tm_make_tmap(ctx, &m->tm_wf[l][0], m->w_fwd[l][0], eb, (uint64_t)2 * nele * H, Kin, TM_BN)) ||
+        (rc = tm_make_tmap(ctx, &m->tm_wf[l][1], m->w_fwd[l][1], eb, (uint64_t)2 * nele * H, Kin, TM_BN)) ||
+        (rc = tm_make_tmap(ctx, &m->tm_wb[l][0], m->w_bwd[l][0], eb, (uint64_t)2 * nele * Kin, H, TM_BN)) ||
+        (rc = tm_make_tmap(ctx, &m->tm_wb[l][1], m->w_bwd[l][1], eb, (uint64_t)2 * nele * Kin, H, TM_BN)))
+      return rc;
+  }
+  std::vector<float> wout((size_t)2 * nele * H, 0.f);
+  std::vector<double> bout((size_t)2 * nele, 0.0);
+  for (int net = 0; net < 2; ++net)
+    for (int e = 0; e < nele; ++e) {
+      const tm_layer_host& Lh = layer(net, e, L);
+      const size_t blk = (size_t)net * nele + e;
+      for (int i = 0; i < Lh.fan_in; ++i) wout[blk * H + i] = (float)Lh.W[i];
+      bout[blk] = Lh.b[0];
+    }
+  if ((rc = tm_alloc(ctx, (void**)&m->wout, wout.size() * 4)) ||
+      (rc = tm_alloc(ctx, (void**)&m->bout, bout.size() * 8)))
+    return rc;
+  cudaMemcpyAsync(m->wout, wout.data(), wout.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
+  cudaMemcpyAsync(m->bout, bout.data(), bout.size() * 8, cudaMemcpyHostToDevice, ctx->stream);
+  if ((rc = tm_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "finalize"))) return rc;
+  m->final_ = true;
+  return TM_OK;
+}
+
+extern "C" int tm_model_destroy(tm_model* m) {
+  if (!m) return TM_OK;
+  tm_ctx* ctx = m->ctx;
+  const int nele = m->k.nele, H = m->H, Dp = m->k.Dp;
+  for (int l = 0; l < m->nlayer; ++l) {
+    const int Kin = l == 0 ? Dp : H;
+    const size_t n = (size_t)2 * nele * H * Kin * m->elem_size;
+    for (int s = 0; s < 2; ++s) {
+      if (m->desc.precision == TM_PREC_BF16 && s == 1) continue;
+      tm_free(ctx, m->w_fwd[l][s], n);
+      tm_free(ctx, m->w_bwd[l][s], n);
+    }
+    tm_free(ctx, m->bias[l], (size_t)2 * nele * H * 4);
+  }
+  tm_free(ctx, m->wout, (size_t)2 * nele * H * 4);
+  tm_free(ctx, m->bout, (size_t)2 * nele * 8);
+  cudaStreamSynchronize(ctx->stream);
+  delete m;
+  return TM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// system
+// ---------------------------------------------------------------------------
+struct AllocList {
+  tm_system* s;
+  int rc = 0;
+  template <typename T>
+  void get(T** p, size_t bytes) {
+    if (rc) return;
+    rc = tm_alloc(s->ctx, (void**)p, bytes);
+    if (!rc) s->bytes += bytes;
+  }
+};
+
+static void system_free(tm_system* s);
+
+extern "C" int tm_system_create(tm_model* m, int N, int nmol, const int32_t* Z,
+                                const int64_t* off, const double* cell, tm_system** out) {
+  *out = nullptr;
+  if (!m || !Z || !off || N <= 0 || nmol <= 0) return tm_fail(m ? m->ctx : nullptr, TM_E_ARG, "system args");
+  tm_ctx* ctx = m->ctx;
+  if (!m->final_) return tm_fail(ctx, TM_E_STATE, "model weights are not finalized");
+  if (off[0] != 0 || off[nmol] != N) return tm_fail(ctx, TM_E_ARG, "mol_offsets must span 0..natoms");
+  for (int q = 0; q < nmol; ++q)
+    if (off[q + 1] <= off[q]) return tm_fail(ctx, TM_E_ARG, "empty or unsorted molecule");
+  if (N >= (1 << 27)) return tm_fail(ctx, TM_E_ARG, "too many atoms");
+  tm_system* s = new tm_system();
+  s->model = m;
+  s->ctx = ctx;
+  s->N = N;
+  s->nmol = nmol;
+  s->Z.assign(Z, Z + N);
+  s->off.assign(off, off + nmol + 1);
+  const tm_consts& k = m->k;
+  if (cell) {
+    for (int q = 0; q < 9; ++q) s->lat[q] = cell[q];
+    if (cell[1] != 0 || cell[2] != 0 || cell[3] != 0 || cell[5] != 0 || cell[6] != 0 || cell[7] != 0) {
+      delete s;
+      return tm_fail(ctx, TM_E_UNSUPPORTED, "only orthorhombic cells are supported");
+    }
+    if (nmol != 1) { delete s; return tm_fail(ctx, TM_E_ARG, "a periodic system is one molecule"); }
+    const double Lmin = std::min(cell[0], std::min(cell[4], cell[8]));
+    const double rmax = std::max(k.r_rc_d, k.ree_d);
+    if (Lmin < 2.0 * rmax) {
+      delete s;
+      return tm_fail(ctx, TM_E_ARG, "cell edges must be at least twice the largest cutoff");
+    }
+    for (int d = 0; d < 3; ++d) {
+      const double L = cell[4 * d];
+      const int n = (int)floor(L / k.r_rc_d);
+      const int R = (int)ceil(k.ree_d / (L / n));
+      if (n < 3 || 2 * R + 1 > n) {
+        delete s;
+        return tm_fail(ctx, TM_E_ARG, "cell too small for the minimum-image cell search");
+      }
+    }
+    s->periodic = true;
+  }
+  // elements and element-sorted rows
+  s->elem_h.resize(N);
+  std::vector<int> count(k.nele, 0);
+  for (int i = 0; i < N; ++i) {
+    int e = -1;
+    for (int q = 0; q < k.nele; ++q)
+      if (m->desc.elements[q] == Z[i]) e = q;
+    if (e < 0) { delete s; return tm_fail(ctx, TM_E_ARG, "atom element not in the model"); }
+    s->elem_h[i] = e;
+    count[e]++;
+  }
+  std::vector<int> row_off(k.nele + 1, 0);
+  for (int e = 0; e < k.nele; ++e) row_off[e + 1] = row_off[e] + ((count[e] + TM_BM - 1) / TM_BM) * TM_BM;
+  s->Mpad = row_off[k.nele];
+  s->ntiles = s->Mpad / TM_BM;
+  s->row_of_atom_h.resize(N);
+  std::vector<int> fill(k.nele, 0);
+  std::vector<int32_t> atom_of_row(s->Mpad, -1);
+  for (int i = 0; i < N; ++i) {
+    const int e = s->elem_h[i];
+    const int r = row_off[e] + fill[e]++;
+    s->row_of_atom_h[i] = r;
+    atom_of_row[r] = i;
+  }
+  s->tile_elem_h.resize(s->ntiles);
+  for (int e = 0; e < k.nele; ++e)
+    for (int r = row_off[e]; r < row_off[e + 1]; r += TM_BM) s->tile_elem_h[r / TM_BM] = e;
+  std::vector<int32_t> mol(N);
+  for (int q = 0; q < nmol; ++q)
+    for (int64_t i = off[q]; i < off[q + 1]; ++i) mol[i] = q;
+  std::vector<int32_t> off32(nmol + 1);
+  for (int q = 0; q <= nmol; ++q) off32[q] = (int32_t)off[q];
+  s->ncell_cap = s->periodic ? 0 : 2 * N + 64 * nmol;
+  if (s->periodic) {
+    long nc = 1;
+    for (int d = 0; d < 3; ++d) nc *= (long)floor(s->lat[4 * d] / k.r_rc_d);
+    s->ncell_cap = (int)nc;
+  }
+  const int H = m->H, Dp = k.Dp;
+  const size_t es = m->elem_size;
+  const size_t Mp = s->Mpad;
+  AllocList A{s};
+  A.get(&s->row_of_atom, sizeof(int32_t) * N);
+  A.get(&s->atom_of_row, sizeof(int32_t) * Mp);
+  A.get(&s->tile_elem, sizeof(int32_t) * s->ntiles);
+  A.get(&s->d_Z, sizeof(int32_t) * N);
+  A.get(&s->d_elem, sizeof(int32_t) * N);
+  A.get(&s->d_mol, sizeof(int32_t) * N);
+  A.get(&s->d_off, sizeof(int32_t) * (nmol + 1));
+  A.get(&s->d_x, sizeof(double) * 3 * N);
+  A.get(&s->d_xhi, sizeof(float4) * N);
+  A.get(&s->d_xlo, sizeof(float4) * N);
+  A.get(&s->d_x_at_build, sizeof(double) * 3 * N);
+  A.get(&s->d_grid, sizeof(tm_grid) * nmol);
+  A.get(&s->d_ncell, sizeof(int32_t));
+  A.get(&s->d_ncell_m, sizeof(int32_t) * nmol);
+  A.get(&s->d_need, sizeof(int32_t) * 2);
+  A.get(&s->d_cell_cnt, sizeof(int32_t) * (s->ncell_cap + 1));
+  A.get(&s->d_cell_start, sizeof(int32_t) * (s->ncell_cap + 1));
+  A.get(&s->d_cell_atoms, sizeof(int32_t) * N);
+  A.get(&s->d_cell_of_atom, sizeof(int32_t) * N);
+  A.get(&s->d_cnt_r, sizeof(int32_t) * N);
+  A.get(&s->d_cnt_a, sizeof(int32_t) * N);
+  A.get(&s->d_nbr_r, sizeof(uint32_t) * (size_t)N * s->KR);
+  A.get(&s->d_nbr_a, sizeof(uint32_t) * (size_t)N * s->KA);
+  A.get(&s->d_rev_r, sizeof(int32_t) * (size_t)N * s->KR);
+  A.get(&s->d_rev_a, sizeof(int32_t) * (size_t)N * s->KA);
+  A.get(&s->d_sr, sizeof(float) * (size_t)N * s->KR);
+  A.get(&s->d_va, sizeof(float4) * (size_t)N * s->KA);
+  for (int h = 0; h < 2; ++h) {
+    if (m->desc.precision == TM_PREC_BF16 && h == 1) {
+      s->G[1] = s->G[0]; s->H1[1] = s->H1[0]; s->H2[1] = s->H2[0]; s->G3[1] = s->G3[0];
+      continue;
+    }
+    A.get(&s->G[h], Mp * Dp * es);
+    A.get(&s->H1[h], 2 * Mp * H * es);
+    A.get(&s->H2[h], 2 * Mp * H * es);
+    A.get(&s->G3[h], 2 * Mp * H * es);
+  }
+  A.get(&s->dEdG, sizeof(float) * 2 * Mp * Dp);
+  A.get(&s->epart, sizeof(float) * 2 * Mp * (H / TM_BN));
+  A.get(&s->d_Eatom, sizeof(double) * N);
+  A.get(&s->d_qraw, sizeof(float) * N);
+  A.get(&s->d_q, sizeof(float) * N);
+  A.get(&s->d_dEdq, sizeof(float) * N);
+  A.get(&s->d_fself, sizeof(float4) * N);
+  A.get(&s->d_fcv, sizeof(float4) * N);
+  A.get(&s->d_ecv, sizeof(double) * 2 * N);
+  A.get(&s->d_F, sizeof(double) * 3 * N);
+  A.get(&s->d_mol_E, sizeof(double) * 4 * nmol);
+  A.get(&s->d_mol_aux, sizeof(double) * 8 * nmol);
+  if (A.rc) {
+    system_free(s);
+    return A.rc;
+  }
+  cudaStream_t st = ctx->stream;
+  cudaMemcpyAsync(s->row_of_atom, s->row_of_atom_h.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s->atom_of_row, atom_of_row.data(), sizeof(int32_t) * Mp, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s->tile_elem, s->tile_elem_h.data(), sizeof(int32_t) * s->ntiles, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s->d_Z, Z, sizeof(int32_t) * N, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s->d_elem, s->elem_h.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s->d_mol, mol.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s->d_off, off32.data(), sizeof(int32_t) * (nmol + 1), cudaMemcpyHostToDevice, st);
+  for (int h = 0; h < 2; ++h) {
+    if (m->desc.precision == TM_PREC_BF16 && h == 1) break;
+    cudaMemsetAsync(s->G[h], 0, Mp * Dp * es, st);
+  }
+  cudaMemsetAsync(s->d_x, 0, sizeof(double) * 3 * N, st);
+  int rc;
+  if ((rc = tm_cuda_check(ctx, cudaStreamSynchronize(st), "system upload"))) {
+    system_free(s);
+    return rc;
+  }
+  const int eb = (int)es;
+  for (int h = 0; h < 2; ++h) {
+    if ((rc = tm_make_tmap(ctx, &s->tm_G[h], s->G[h], eb, Mp, Dp, TM_BM)) ||
+        (rc = tm_make_tmap(ctx, &s->tm_H1[h], s->H1[h], eb, 2 * Mp, H, TM_BM)) ||
+        (rc = tm_make_tmap(ctx, &s->tm_H2[h], s->H2[h], eb, 2 * Mp, H, TM_BM)) ||
+        (rc = tm_make_tmap(ctx, &s->tm_G3[h], s->G3[h], eb, 2 * Mp, H, TM_BM))) {
+      system_free(s);
+      return rc;
+    }
+  }
+  *out = s;
+  return TM_OK;
+}
+
+static void system_free(tm_system* s) {
+  tm_ctx* ctx = s->ctx;
+  // sizes are not needed by cudaFreeAsync; budget accounting uses s->bytes
+  void* ptrs[] = {s->row_of_atom, s->atom_of_row, s->tile_elem, s->d_Z, s->d_elem, s->d_mol,
+                  s->d_off, s->d_x, s->d_xhi, s->d_xlo, s->d_x_at_build, s->d_grid, s->d_ncell, s->d_ncell_m, s->d_need,
+                  s->d_cell_cnt, s->d_cell_start, s->d_cell_atoms, s->d_cell_of_atom, s->d_cnt_r,
+                  s->d_cnt_a, s->d_nbr_r, s->d_nbr_a, s->d_rev_r, s->d_rev_a, s->d_sr, s->d_va,
+                  s->dEdG, s->epart, s->d_Eatom, s->d_qraw, s->d_q, s->d_dEdq, s->d_fself,
+                  s->d_fcv, s->d_ecv, s->d_F, s->d_mol_E, s->d_mol_aux};
+  for (void* p : ptrs)
+    if (p) cudaFreeAsync(p, ctx->stream);
+  for (int h = 0; h < 2; ++h) {
+    if (h == 1 && s->G[1] == s->G[0]) break;
+    void* q[] = {s->G[h], s->H1[h], s->H2[h], s->G3[h]};
+    for (void* p : q)
+      if (p) cudaFreeAsync(p, ctx->stream);
+  }
+  ctx->in_use -= std::min(ctx->in_use, s->bytes);
+  cudaStreamSynchronize(ctx->stream);
+  delete s;
+}
+
+extern "C" int tm_system_destroy(tm_system* s) {
+  if (s) system_free(s);
+  return TM_OK;
+}
+
+extern "C" int tm_system_natoms(const tm_system* s) { return s ? s->N : -1; }
+
+extern "C" int tm_system_set_positions(tm_system* s, const double* x, int on_device) {
+  if (!s || !x) return TM_E_ARG;
+  tm_ctx* ctx = s->ctx;
+  s->nlist_valid = false;
+  return tm_cuda_check(ctx, cudaMemcpyAsync(s->d_x, x, sizeof(double) * 3 * s->N,
+                                            on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                            ctx->stream),
+                       "positions");
+}
+
+extern "C" int tm_system_get_positions(tm_system* s, double* x, int on_device) {
+  if (!s || !x) return TM_E_ARG;
+  tm_ctx* ctx = s->ctx;
+  int rc = tm_cuda_check(ctx, cudaMemcpyAsync(x, s->d_x, sizeof(double) * 3 * s->N,
+                                              on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                              ctx->stream),
+                         "positions");
+  if (rc) return rc;
+  return tm_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "positions");
+}
+
+extern "C" int tm_system_build_nlist(tm_system* s) {
+  if (!s) return TM_E_ARG;
+  for (int attempt = 0; attempt < 3; ++attempt) {
+    int rc = tm_launch_nlist(s);
+    if (rc) return rc;
+    bool grew = false;
+    if ((rc = tm_nlist_grow(s, &grew))) return rc;
+    if (!grew) return tm_sync_status(s->ctx, "build_nlist");
+  }
+  return tm_fail(s->ctx, TM_E_CAPACITY, "neighbour rows could not be grown");
+}
+
+extern "C" int tm_system_nlist_counts(tm_system* s, int64_t counts[4]) {
+  if (!s || !counts) return TM_E_ARG;
+  if (!s->nlist_valid) return tm_fail(s->ctx, TM_E_STATE, "neighbour lists not built");
+  return tm_count_nlist(s, counts);
+}
+
+extern "C" int tm_system_export_nlist(tm_system* s, int64_t* radp, int64_t* angt, int64_t* mil_j,
+                                      int64_t* mil_jk, int on_device) {
+  if (!s) return TM_E_ARG;
+  tm_ctx* ctx = s->ctx;
+  if (!s->nlist_valid) return tm_fail(ctx, TM_E_STATE, "neighbour lists not built");
+  int64_t c[4];
+  int rc = tm_count_nlist(s, c);
+  if (rc) return rc;
+  const int64_t P = c[0], T = c[1];
+  int64_t* dst[4] = {radp, angt, mil_j, mil_jk};
+  const int64_t sz[4] = {P * 4, T * 5, P * 4, T * 4};
+  int64_t* dev[4] = {nullptr, nullptr, nullptr, nullptr};
+  for (int q = 0; q < 4; ++q) {
+    if (!dst[q]) continue;
+    if (on_device) { dev[q] = dst[q]; continue; }
+    if ((rc = tm_alloc(ctx, (void**)&dev[q], sizeof(int64_t) * (size_t)std::max<int64_t>(sz[q], 1))))
+      return rc;
+  }
+  rc = tm_launch_export_nlist(s, dev[0], dev[1], dev[2], dev[3], P, T);
+  for (int q = 0; q < 4; ++q) {
+    if (!dst[q] || on_device) continue;
+    if (!rc && sz[q] > 0)
+      rc = tm_cuda_check(ctx, cudaMemcpyAsync(dst[q], dev[q], sizeof(int64_t) * sz[q], cudaMemcpyDeviceToHost, ctx->stream), "export");
+    tm_free(ctx, dev[q], sizeof(int64_t) * (size_t)std::max<int64_t>(sz[q], 1));
+  }
+  if (!rc) rc = tm_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "export");
+  return rc;
+}
+
+extern "C" int tm_system_export_ee(tm_system* s, int64_t* eep, int64_t cap, int on_device) {
+  if (!s || !eep) return TM_E_ARG;
+  tm_ctx* ctx = s->ctx;
+  if (!s->nlist_valid) return tm_fail(ctx, TM_E_STATE, "neighbour lists not built");
+  if (on_device) return tm_launch_export_ee(s, eep, cap);
+  int64_t* dev = nullptr;
+  int rc = tm_alloc(ctx, (void**)&dev, sizeof(int64_t) * 3 * (size_t)std::max<int64_t>(cap, 1));
+  if (rc) return rc;
+  rc = tm_launch_export_ee(s, dev, cap);
+  if (!rc) {
+    int64_t n = 0;
+    rc = tm_count_ee(s, &n);
+    if (!rc && n > 0)
+      rc = tm_cuda_check(ctx, cudaMemcpyAsync(eep, dev, sizeof(int64_t) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream), "ee");
+    if (!rc) rc = tm_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "ee");
+  }
+  tm_free(ctx, dev, sizeof(int64_t) * 3 * (size_t)std::max<int64_t>(cap, 1));
+  return rc;
+}
+
+// Device-side pipeline of one energy(+force) evaluation; no host sync unless
+// the neighbour lists have to be (re)built.
+int tm_energy_force_device(tm_system* s, unsigned flags) {
+  int rc;
+  if (!(flags & TM_F_REUSE_NLIST) || !s->nlist_valid) {
+    if ((rc = tm_launch_nlist(s))) return rc;
+  } else {
+    if ((rc = tm_launch_positions(s))) return rc;
+  }
+  const bool force = !(flags & TM_F_ENERGY_ONLY);
+  if ((rc = tm_launch_descriptors(s))) return rc;
+  if ((rc = tm_launch_mlp(s, force))) return rc;
+  if ((rc = tm_launch_mlp_finish(s))) return rc;
+  if ((rc = tm_launch_coulomb(s, flags))) return rc;
+  if (force && (rc = tm_launch_adjoint(s, flags))) return rc;
+  return TM_OK;
+}
+
+extern "C" int tm_energy_force(tm_system* s, const double* x, unsigned flags, double* E_out,
+                               double* F_out, double* q_out, double* dipole_out, double* Eatom_out) {
+  if (!s) return TM_E_ARG;
+  tm_ctx* ctx = s->ctx;
+  const bool dev = flags & TM_F_DEVICE_IO;
+  int rc;
+  if (x) {
+    if ((rc = tm_cuda_check(ctx, cudaMemcpyAsync(s->d_x, x, sizeof(double) * 3 * s->N,
+                                                 dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                                 ctx->stream),
+                            "x")))
+      return rc;
+    if (!(flags & TM_F_REUSE_NLIST)) s->nlist_valid = false;
+  }
+  for (int attempt = 0;; ++attempt) {
+    if ((rc = tm_energy_force_device(s, flags))) return rc;
+    bool grew = false;
+    if ((rc = tm_nlist_grow(s, &grew))) return rc;
+    if (!grew) break;
+    if (attempt == 2) return tm_fail(ctx, TM_E_CAPACITY, "neighbour rows could not be grown");
+  }
+  const cudaMemcpyKind kind = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  cudaStream_t st = ctx->stream;
+  if (E_out) cudaMemcpyAsync(E_out, s->d_mol_E, sizeof(double) * 4 * s->nmol, kind, st);
+  if (F_out && !(flags & TM_F_ENERGY_ONLY)) cudaMemcpyAsync(F_out, s->d_F, sizeof(double) * 3 * s->N, kind, st);
+  if (Eatom_out) cudaMemcpyAsync(Eatom_out, s->d_Eatom, sizeof(double) * s->N, kind, st);
+  if (q_out || dipole_out) {
+    // q (float) and dipole (aux[2..4]) are converted on the host side
+    std::vector<float> qf(s->N);
+    std::vector<double> aux((size_t)8 * s->nmol);
+    cudaMemcpyAsync(qf.data(), s->d_q, sizeof(float) * s->N, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(aux.data(), s->d_mol_aux, sizeof(double) * 8 * s->nmol, cudaMemcpyDeviceToHost, st);
+    if ((rc = tm_sync_status(ctx, "energy_force"))) return rc;
+    std::vector<double> qd(s->N), dip((size_t)3 * s->nmol);
+    for (int i = 0; i < s->N; ++i) qd[i] = qf[i];
+    for (int m = 0; m < s->nmol; ++m)
+      for (int d = 0; d < 3; ++d) dip[3 * m + d] = aux[8 * m + 2 + d];
+    if (q_out) cudaMemcpy(q_out, qd.data(), sizeof(double) * s->N, dev ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost);
+    if (dipole_out) cudaMemcpy(dipole_out, dip.data(), sizeof(double) * 3 * s->nmol, dev ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost);
+  }
+  return tm_sync_status(ctx, "energy_force");
+}
+
+// ---------------------------------------------------------------------------
+// diagnostics
+// ---------------------------------------------------------------------------
+extern "C" int tm_selftest_gemm(tm_ctx* ctx, int prec, int M, int N, int K, const float* A,
+                                const float* B, float* C) {
+  if (!ctx || !A || !B || !C) return TM_E_ARG;
+  if (prec != TM_PREC_FP32 && prec != TM_PREC_BF16) return tm_fail(ctx, TM_E_ARG, "precision");
+  return tm_gemm_selftest(ctx, prec, M, N, K, A, B, C);
+}
+
+int tm_launch_descriptors_f32(tm_system* s, float* out);
+
+extern "C" int tm_system_descriptors(tm_system* s, float* G_out) {
+  if (!s || !G_out) return TM_E_ARG;
+  tm_ctx* ctx = s->ctx;
+  int rc;
+  for (int attempt = 0; attempt < 3; ++attempt) {
+    if (!s->nlist_valid) {
+      if ((rc = tm_launch_nlist(s))) return rc;
+      bool grew = false;
+      if ((rc = tm_nlist_grow(s, &grew))) return rc;
+      if (grew) continue;
+    }
+    break;
+  }
+  const int Dp = s->model->k.Dp, D = s->model->k.D;
+  float* dev = nullptr;
+  if ((rc = tm_alloc(ctx, (void**)&dev, sizeof(float) * (size_t)s->Mpad * Dp))) return rc;
+  cudaMemsetAsync(dev, 0, sizeof(float) * (size_t)s->Mpad * Dp, ctx->stream);
+  if (!(rc = tm_launch_descriptors_f32(s, dev))) {
+    std::vector<float> rows((size_t)s->Mpad * Dp);
+    rc = tm_cuda_check(ctx, cudaMemcpyAsync(rows.data(), dev, rows.size() * 4, cudaMemcpyDeviceToHost, ctx->stream), "G");
+    if (!rc) rc = tm_sync_status(ctx, "descriptors");
+    if (!rc)
+      for (int i = 0; i < s->N; ++i)
+        memcpy(G_out + (size_t)i * D, rows.data() + (size_t)s->row_of_atom_h[i] * Dp, sizeof(float) * D);
+  }
+  tm_free(ctx, dev, sizeof(float) * (size_t)s->Mpad * Dp);
+  return rc;
+}

@@ -1,0 +1,563 @@
+// ANI-1 symmetry functions (forward) and their Jacobian-transpose (adjoint).
+//
+// Forward follows TFSymRSet_Linear_WithEle_Release (TFDescriptors/RawSymFunc.py:
+// 1757-1810) and TFSymASet_Linear_WithEle (RawSymFunc.py:868-963), assembled as
+// in TFSymSet_Scattered_Linear_WithEle_Release (RawSymFunc.py:2267-2309):
+//   row = [ radial: element-major, AN1_num_r_Rs shifts
+//         | angular: element-pair-major, theta-major (8), then Rs (8) ]
+//   radial  G[l(j), n]   += exp(-eta (r_ij - Rs_n)^2) fc_r(r_ij)
+//   angular G[p(j,k),m,n] += 2^(1-zeta) (1 + cos(theta_ijk - theta_m))^zeta
+//                            exp(-eta ((r_ij + r_ik)/2 - Rs_n)^2) fc_a(r_ij) fc_a(r_ik)
+//   fc(r) = 0.5 (cos(3.14159265359 r / Rc) + 1)
+// cos(theta - theta_m) is formed as c cos(theta_m) + s sin(theta_m) with
+// c = u_ij . u_ik and s = sqrt(1 - c^2) >= 0, which is cos(acos(c) - theta_m)
+// without the acos; the reference's clamp of c to +-(1 - 1e-16) only protects
+// its acos and is a no-op in FP32.
+//
+// The adjoint takes dE/dG per atom (energy net + dE/dq * charge net), recomputes
+// the pair/triple geometry from the positions, and produces
+//   * the centre's own dE/dx_i,
+//   * one scalar per radial edge and one vector per angular edge for the
+//     neighbour side, gathered per atom through the reverse-edge index
+//     (no atomics on global memory: forces are deterministic).
+#include <cuda_runtime.h>
+
+#include "tm_internal.h"
+
+namespace {
+
+struct DescArgs {
+  const float4* xhi;
+  const float4* xlo;
+  const uint32_t* nbr_r;
+  const uint32_t* nbr_a;
+  const int32_t* cnt_r;
+  const int32_t* cnt_a;
+  const int32_t* rev_r;
+  const int32_t* rev_a;
+  const int32_t* row_of_atom;
+  int N, KR, KA, Mpad;
+  int prec;             // TM_PREC_FP32: hi/lo fp32 out; TM_PREC_BF16: bf16 out
+  void* out0;
+  void* out1;
+  float* out_f32;       // optional plain fp32 rows [Mpad][Dp]
+  // adjoint
+  const float* dEdG;    // [2*Mpad][Dp]
+  const float* dEdq;    // [N]
+  float4* fself;        // [N]
+  float* sr;            // [N*KR]
+  float4* va;           // [N*KA]
+  float sh_hi[27][3];
+  float sh_lo[27][3];
+};
+
+__device__ __forceinline__ void nbr_vec(const DescArgs& a, float4 hi, float4 lo, uint32_t e,
+                                        float& dx, float& dy, float& dz, int& el) {
+  const int j = (int)tm_atom(e);
+  const int r = tm_img(e);
+  const float4 hj = a.xhi[j], lj = a.xlo[j];
+  dx = ds_sub_shift(hi.x, lo.x, hj.x, lj.x, a.sh_hi[r][0], a.sh_lo[r][0]);
+  dy = ds_sub_shift(hi.y, lo.y, hj.y, lj.y, a.sh_hi[r][1], a.sh_lo[r][1]);
+  dz = ds_sub_shift(hi.z, lo.z, hj.z, lj.z, a.sh_hi[r][2], a.sh_lo[r][2]);
+  el = __float_as_int(hj.w);
+}
+
+__device__ __forceinline__ float fcut(float r, float pi_tf, float rc) {
+  return 0.5f * (cosf(pi_tf * r / rc) + 1.0f);
+}
+__device__ __forceinline__ float fcut_d(float r, float pi_tf, float rc) {
+  return -0.5f * sinf(pi_tf * r / rc) * (pi_tf / rc);
+}
+
+// x^zeta for x >= 0 and its derivative factor zeta*x^(zeta-1)
+__device__ __forceinline__ void powz(float x, const tm_consts& k, float& p, float& dp) {
+  if (k.zeta_pow2) {  // zeta == 8
+    const float x2 = x * x, x4 = x2 * x2, x7 = x4 * x2 * x;
+    p = x7 * x;
+    dp = 8.0f * x7;
+  } else {
+    p = powf(x, k.zeta);
+    dp = k.zeta * powf(x, k.zeta - 1.0f);
+  }
+}
+
+// Per-warp shared memory layout
+struct WarpSmem {
+  float* row;     // [Dp]
+  float* ux;      // [KA]
+  float* uy;
+  float* uz;
+  float* r;
+  float* fc;
+  float* fcd;
+  float* vx;      // adjoint accumulators [KA]
+  float* vy;
+  float* vz;
+};
+
+__device__ __forceinline__ WarpSmem warp_smem(float* base, int Dp, int KA) {
+  WarpSmem w;
+  w.row = base;
+  w.ux = base + Dp;
+  w.uy = w.ux + KA;
+  w.uz = w.uy + KA;
+  w.r = w.uz + KA;
+  w.fc = w.r + KA;
+  w.fcd = w.fc + KA;
+  w.vx = w.fcd + KA;
+  w.vy = w.vx + KA;
+  w.vz = w.vy + KA;
+  return w;
+}
+
+__host__ __device__ __forceinline__ int smem_floats(int Dp, int KA) { return Dp + 9 * KA; }
+
+// angular neighbour geometry + element segments; returns segment starts in seg[]
+__device__ __forceinline__ void load_angular(const DescArgs& a, const tm_consts& k, int i,
+                                             float4 hi, float4 lo, int ca, WarpSmem& w,
+                                             int* seg, int lane) {
+  for (int s = lane; s < ca; s += 32) {
+    float dx, dy, dz;
+    int el;
+    nbr_vec(a, hi, lo, a.nbr_a[(size_t)i * a.KA + s], dx, dy, dz, el);
+    const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+    const float inv = 1.0f / r;
+    w.ux[s] = dx * inv;
+    w.uy[s] = dy * inv;
+    w.uz[s] = dz * inv;
+    w.r[s] = r;
+    w.fc[s] = fcut(r, k.pi_tf, k.a_rc);
+    w.fcd[s] = fcut_d(r, k.pi_tf, k.a_rc);
+  }
+  for (int e = 0; e < k.nele; ++e) {
+    int c = 0;
+    for (int s = lane; s < ca; s += 32) {
+      const uint32_t ent = a.nbr_a[(size_t)i * a.KA + s];
+      c += __float_as_int(a.xhi[tm_atom(ent)].w) == e;
+    }
+    seg[e] = __reduce_add_sync(TM_FULL, c);
+  }
+  int acc = 0;
+  for (int e = 0; e < k.nele; ++e) { int c = seg[e]; seg[e] = acc; acc += c; }
+  seg[k.nele] = acc;
+  __syncwarp();
+}
+
+// advance the (pa, pb) pair index by 4 in the enumeration order used for the
+// element pair (b outer, a inner; a < b when both atoms share an element)
+__device__ __forceinline__ void pair_advance(int& pa, int& pb, int na_, bool tri) {
+  pa += 4;
+  if (tri) {
+    while (pa >= pb && pb > 0) { pa -= pb; ++pb; }
+  } else {
+    while (pa >= na_ && na_ > 0) { pa -= na_; ++pb; }
+  }
+}
+__device__ __forceinline__ void pair_start(int t, int& pa, int& pb, int na_, bool tri) {
+  if (tri) {
+    int b = 1, acc = 0;
+    while (acc + b <= t) { acc += b; ++b; }
+    pb = b;
+    pa = t - acc;
+  } else {
+    pb = na_ > 0 ? t / na_ : 0;
+    pa = na_ > 0 ? t % na_ : 0;
+  }
+}
+
+__global__ void __launch_bounds__(128) k_desc_fwd(const DescArgs a, const tm_consts k) {
+  extern __shared__ float sh[];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * (blockDim.x >> 5) + wib;
+  if (i >= a.N) return;
+  WarpSmem w = warp_smem(sh + (size_t)wib * smem_floats(k.Dp, a.KA), k.Dp, a.KA);
+  for (int c = lane; c < k.Dp; c += 32) w.row[c] = 0.f;
+  __syncwarp();
+  const float4 hi = a.xhi[i], lo = a.xlo[i];
+  // ---- radial ----
+  const int cr = a.cnt_r[i];
+  for (int base = 0; base < cr; base += 32) {
+    const int s = base + lane;
+    float r = 0.f, f = 0.f;
+    int el = 0;
+    if (s < cr) {
+      float dx, dy, dz;
+      nbr_vec(a, hi, lo, a.nbr_r[(size_t)i * a.KR + s], dx, dy, dz, el);
+      r = sqrtf(dx * dx + dy * dy + dz * dz);
+      f = fcut(r, k.pi_tf, k.r_rc);
+    }
+    const int n = min(32, cr - base);
+    for (int q = 0; q < n; ++q) {
+      const float rq = __shfl_sync(TM_FULL, r, q);
+      const float fq = __shfl_sync(TM_FULL, f, q);
+      const int lq = __shfl_sync(TM_FULL, el, q);
+      if (lane < k.nr) {
+        const float t = rq - k.rs_r[lane];
+        w.row[lq * k.nr + lane] += expf(-k.eta * t * t) * fq;
+      }
+    }
+  }
+  // ---- angular ----
+  const int ca = a.cnt_a[i];
+  int seg[TM_MAX_ELE + 1];
+  load_angular(a, k, i, hi, lo, ca, w, seg, lane);
+  const int grp = lane >> 3, q = lane & 7;
+  const float cth = k.cos_th[q], sth = k.sin_th[q], rsq = k.rs_a[q];
+  for (int ea = 0; ea < k.nele; ++ea) {
+    for (int eb = ea; eb < k.nele; ++eb) {
+      const int na_ = seg[ea + 1] - seg[ea], nb_ = seg[eb + 1] - seg[eb];
+      const bool tri = (ea == eb);
+      const int npair = tri ? na_ * (na_ - 1) / 2 : na_ * nb_;
+      if (npair == 0) continue;
+      const int l = k.elepair[ea][eb];
+      float acc[8];
+#pragma unroll
+      for (int n = 0; n < 8; ++n) acc[n] = 0.f;
+      int pa, pb;
+      pair_start(grp, pa, pb, na_, tri);
+      for (int tb = 0; tb < npair; tb += 4) {
+        const bool act = tb + grp < npair;
+        float AF = 0.f, B = 0.f;
+        if (act) {
+          const int sa = seg[ea] + pa, sb = seg[eb] + pb;
+          const float c = w.ux[sa] * w.ux[sb] + w.uy[sa] * w.uy[sb] + w.uz[sa] * w.uz[sb];
+          const float sn = sqrtf(fmaxf(0.f, 1.f - c * c));
+          const float T = c * cth + sn * sth;
+          float p, dp;
+          powz(fmaxf(0.f, 1.f + T), k, p, dp);
+          AF = k.two_1mz * p * w.fc[sa] * w.fc[sb];
+          const float u = 0.5f * (w.r[sa] + w.r[sb]) - rsq;
+          B = expf(-k.eta * u * u);
+        }
+#pragma unroll
+        for (int n = 0; n < 8; ++n) {
+          const float Bn = __shfl_sync(TM_FULL, B, (lane & ~7) | n);
+          acc[n] += AF * Bn;
+        }
+        pair_advance(pa, pb, na_, tri);
+      }
+#pragma unroll
+      for (int n = 0; n < 8; ++n) {
+        acc[n] += __shfl_xor_sync(TM_FULL, acc[n], 8);
+        acc[n] += __shfl_xor_sync(TM_FULL, acc[n], 16);
+      }
+      if (grp == 0) {
+        float* dst = w.row + k.nele * k.nr + l * 64 + q * 8;
+#pragma unroll
+        for (int n = 0; n < 8; ++n) dst[n] = acc[n];
+      }
+    }
+  }
+  __syncwarp();
+  // ---- write the row (element-sorted order) ----
+  const int row = a.row_of_atom[i];
+  if (a.prec == TM_PREC_FP32) {
+    float4* o0 = reinterpret_cast<float4*>(static_cast<float*>(a.out0) + (size_t)row * k.Dp);
+    float4* o1 = reinterpret_cast<float4*>(static_cast<float*>(a.out1) + (size_t)row * k.Dp);
+    for (int c = lane; c < k.Dp / 4; c += 32) {
+      float4 v = reinterpret_cast<const float4*>(w.row)[c];
+      float4 h;
+      h.x = __uint_as_float(__float_as_uint(v.x) & 0xffffe000u);
+      h.y = __uint_as_float(__float_as_uint(v.y) & 0xffffe000u);
+      h.z = __uint_as_float(__float_as_uint(v.z) & 0xffffe000u);
+      h.w = __uint_as_float(__float_as_uint(v.w) & 0xffffe000u);
+      o0[c] = h;
+      o1[c] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+    }
+  } else {
+    uint2* o0 = reinterpret_cast<uint2*>(static_cast<uint16_t*>(a.out0) + (size_t)row * k.Dp);
+    for (int c = lane; c < k.Dp / 4; c += 32) {
+      float4 v = reinterpret_cast<const float4*>(w.row)[c];
+      __nv_bfloat162 p0 = __floats2bfloat162_rn(v.x, v.y);
+      __nv_bfloat162 p1 = __floats2bfloat162_rn(v.z, v.w);
+      o0[c] = make_uint2(*reinterpret_cast<uint32_t*>(&p0), *reinterpret_cast<uint32_t*>(&p1));
+    }
+  }
+  if (a.out_f32) {
+    float4* o = reinterpret_cast<float4*>(a.out_f32 + (size_t)row * k.Dp);
+    for (int c = lane; c < k.Dp / 4; c += 32) o[c] = reinterpret_cast<const float4*>(w.row)[c];
+  }
+}
+
+__global__ void __launch_bounds__(128) k_desc_adj(const DescArgs a, const tm_consts k) {
+  extern __shared__ float sh[];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * (blockDim.x >> 5) + wib;
+  if (i >= a.N) return;
+  WarpSmem w = warp_smem(sh + (size_t)wib * smem_floats(k.Dp, a.KA), k.Dp, a.KA);
+  // upstream dE/dG for this centre: energy net + dE/dq * charge net
+  const int row = a.row_of_atom[i];
+  const float dq = a.dEdq[i];
+  const float* gE = a.dEdG + (size_t)row * k.Dp;
+  const float* gQ = a.dEdG + ((size_t)a.Mpad + row) * k.Dp;
+  for (int c = lane; c < k.Dp; c += 32) w.row[c] = gE[c] + dq * gQ[c];
+  __syncwarp();
+  const float4 hi = a.xhi[i], lo = a.xlo[i];
+  float fx = 0.f, fy = 0.f, fz = 0.f;   // dE/dx_i, per-lane partials
+  // ---- radial ----
+  const int cr = a.cnt_r[i];
+  for (int base = 0; base < cr; base += 32) {
+    const int s = base + lane;
+    float r = 1.f, f = 0.f, fd = 0.f, dx = 0.f, dy = 0.f, dz = 0.f;
+    int el = 0;
+    if (s < cr) {
+      nbr_vec(a, hi, lo, a.nbr_r[(size_t)i * a.KR + s], dx, dy, dz, el);
+      r = sqrtf(dx * dx + dy * dy + dz * dz);
+      f = fcut(r, k.pi_tf, k.r_rc);
+      fd = fcut_d(r, k.pi_tf, k.r_rc);
+    }
+    float myS = 0.f;
+    const int n = min(32, cr - base);
+    for (int q = 0; q < n; ++q) {
+      const float rq = __shfl_sync(TM_FULL, r, q);
+      const float fq = __shfl_sync(TM_FULL, f, q);
+      const float fdq = __shfl_sync(TM_FULL, fd, q);
+      const int lq = __shfl_sync(TM_FULL, el, q);
+      float part = 0.f;
+      if (lane < k.nr) {
+        const float t = rq - k.rs_r[lane];
+        const float g = expf(-k.eta * t * t);
+        part = w.row[lq * k.nr + lane] * g * (-2.f * k.eta * t * fq + fdq);
+      }
+      const float S = warp_sum(part);
+      if (lane == q) myS = S;
+    }
+    if (s < cr) {
+      a.sr[(size_t)i * a.KR + s] = myS;
+      const float inv = 1.f / r;
+      fx += myS * dx * inv;
+      fy += myS * dy * inv;
+      fz += myS * dz * inv;
+    }
+  }
+  // ---- angular ----
+  const int ca = a.cnt_a[i];
+  int seg[TM_MAX_ELE + 1];
+  load_angular(a, k, i, hi, lo, ca, w, seg, lane);
+  for (int s = lane; s < ca; s += 32) { w.vx[s] = 0.f; w.vy[s] = 0.f; w.vz[s] = 0.f; }
+  __syncwarp();
+  const int grp = lane >> 3, q = lane & 7;
+  const float cth = k.cos_th[q], sth = k.sin_th[q], rsq = k.rs_a[q];
+  for (int ea = 0; ea < k.nele; ++ea) {
+    for (int eb = ea; eb < k.nele; ++eb) {
+      const int na_ = seg[ea + 1] - seg[ea], nb_ = seg[eb + 1] - seg[eb];
+      const bool tri = (ea == eb);
+      const int npair = tri ? na_ * (na_ - 1) / 2 : na_ * nb_;
+      if (npair == 0) continue;
+      const int l = k.elepair[ea][eb];
+      float wl[8];
+      const float* src = w.row + k.nele * k.nr + l * 64 + q * 8;
+#pragma unroll
+      for (int n = 0; n < 8; ++n) wl[n] = src[n];
+      int pa, pb;
+      pair_start(grp, pa, pb, na_, tri);
+      for (int tb = 0; tb < npair; tb += 4) {
+        const bool act = tb + grp < npair;
+        int sa = 0, sb = 0;
+        float c = 0.f, sn = 0.f, A = 0.f, dA = 0.f, B = 0.f, Bd = 0.f;
+        if (act) {
+          sa = seg[ea] + pa;
+          sb = seg[eb] + pb;
+          c = w.ux[sa] * w.ux[sb] + w.uy[sa] * w.uy[sb] + w.uz[sa] * w.uz[sb];
+          sn = sqrtf(fmaxf(0.f, 1.f - c * c));
+          const float T = c * cth + sn * sth;
+          const float dT = -(sn * cth - c * sth);   // d cos(theta - theta_m) / d theta
+          float p, dp;
+          powz(fmaxf(0.f, 1.f + T), k, p, dp);
+          A = k.two_1mz * p;
+          dA = k.two_1mz * dp * dT;
+          const float u = 0.5f * (w.r[sa] + w.r[sb]) - rsq;
+          B = expf(-k.eta * u * u);
+          Bd = B * (-2.f * k.eta * u);
+        }
+        float P = 0.f, Q = 0.f;
+#pragma unroll
+        for (int n = 0; n < 8; ++n) {
+          const int src_lane = (lane & ~7) | n;
+          P += wl[n] * __shfl_sync(TM_FULL, B, src_lane);
+          Q += wl[n] * __shfl_sync(TM_FULL, Bd, src_lane);
+        }
+        float S1 = A * P, S2 = A * Q, S3 = dA * P;
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) {
+          S1 += __shfl_xor_sync(TM_FULL, S1, o);
+          S2 += __shfl_xor_sync(TM_FULL, S2, o);
+          S3 += __shfl_xor_sync(TM_FULL, S3, o);
+        }
+        if (act && q == 0) {
+          const float fa = w.fc[sa], fb = w.fc[sb];
+          const float fcc = fa * fb;
+          const float dra = 0.5f * S2 * fcc + S1 * w.fcd[sa] * fb;
+          const float drb = 0.5f * S2 * fcc + S1 * fa * w.fcd[sb];
+          const float dth = S3 * fcc;
+          const float kc = -dth / fmaxf(sn, 1e-6f);   // dE/dc
+          const float ra = w.r[sa], rb = w.r[sb];
+          const float uax = w.ux[sa], uay = w.uy[sa], uaz = w.uz[sa];
+          const float ubx = w.ux[sb], uby = w.uy[sb], ubz = w.uz[sb];
+          const float ka = kc / ra, kb = kc / rb;
+          const float gax = dra * uax + ka * (ubx - c * uax);
+          const float gay = dra * uay + ka * (uby - c * uay);
+          const float gaz = dra * uaz + ka * (ubz - c * uaz);
+          const float gbx = drb * ubx + kb * (uax - c * ubx);
+          const float gby = drb * uby + kb * (uay - c * uby);
+          const float gbz = drb * ubz + kb * (uaz - c * ubz);
+          fx += gax + gbx;
+          fy += gay + gby;
+          fz += gaz + gbz;
+          atomicAdd(&w.vx[sa], -gax); atomicAdd(&w.vy[sa], -gay); atomicAdd(&w.vz[sa], -gaz);
+          atomicAdd(&w.vx[sb], -gbx); atomicAdd(&w.vy[sb], -gby); atomicAdd(&w.vz[sb], -gbz);
+        }
+        pair_advance(pa, pb, na_, tri);
+      }
+    }
+  }
+  __syncwarp();
+  for (int s = lane; s < ca; s += 32)
+    a.va[(size_t)i * a.KA + s] = make_float4(w.vx[s], w.vy[s], w.vz[s], 0.f);
+  fx = warp_sum(fx);
+  fy = warp_sum(fy);
+  fz = warp_sum(fz);
+  if (lane == 0) a.fself[i] = make_float4(fx, fy, fz, 0.f);
+}
+
+}  // namespace
+
+// shared helpers used by tm_api.cu
+void tm_fill_shifts(const tm_system* s, float hi[27][3], float lo[27][3]) {
+  for (int r = 0; r < 27; ++r) {
+    const int sx = r / 9 - 1, sy = (r / 3) % 3 - 1, sz = r % 3 - 1;
+    for (int d = 0; d < 3; ++d) {
+      double v = 0.0;
+      if (s->periodic) v = sx * s->lat[0 + d] + sy * s->lat[3 + d] + sz * s->lat[6 + d];
+      const float h = (float)v;
+      hi[r][d] = h;
+      lo[r][d] = (float)(v - (double)h);
+    }
+  }
+}
+
+static DescArgs make_desc_args(tm_system* s) {
+  DescArgs a;
+  a.xhi = s->d_xhi; a.xlo = s->d_xlo; a.nbr_r = s->d_nbr_r; a.nbr_a = s->d_nbr_a;
+  a.cnt_r = s->d_cnt_r; a.cnt_a = s->d_cnt_a; a.rev_r = s->d_rev_r; a.rev_a = s->d_rev_a;
+  a.row_of_atom = s->row_of_atom; a.N = s->N; a.KR = s->KR; a.KA = s->KA; a.Mpad = s->Mpad;
+  a.prec = s->model->desc.precision;
+  a.out0 = s->G[0]; a.out1 = s->G[1]; a.out_f32 = nullptr;
+  a.dEdG = s->dEdG; a.dEdq = s->d_dEdq; a.fself = s->d_fself; a.sr = s->d_sr; a.va = s->d_va;
+  tm_fill_shifts(s, a.sh_hi, a.sh_lo);
+  return a;
+}
+
+int tm_launch_descriptors(tm_system* s) {
+  tm_ctx* ctx = s->ctx;
+  DescArgs a = make_desc_args(s);
+  const tm_consts& k = s->model->k;
+  const size_t shm = (size_t)4 * smem_floats(k.Dp, s->KA) * sizeof(float);
+  if (shm > 48 * 1024)
+    cudaFuncSetAttribute(k_desc_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  k_desc_fwd<<<tm_div_up(s->N, 4), 128, shm, ctx->stream>>>(a, k);
+  ctx->launches++;
+  return tm_cuda_check(ctx, cudaGetLastError(), "descriptors");
+}
+
+int tm_launch_descriptors_f32(tm_system* s, float* out) {
+  tm_ctx* ctx = s->ctx;
+  DescArgs a = make_desc_args(s);
+  a.out_f32 = out;
+  const tm_consts& k = s->model->k;
+  const size_t shm = (size_t)4 * smem_floats(k.Dp, s->KA) * sizeof(float);
+  if (shm > 48 * 1024)
+    cudaFuncSetAttribute(k_desc_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  k_desc_fwd<<<tm_div_up(s->N, 4), 128, shm, ctx->stream>>>(a, k);
+  ctx->launches++;
+  return tm_cuda_check(ctx, cudaGetLastError(), "descriptors");
+}
+
+namespace {
+struct GatherArgs {
+  const float4* xhi;
+  const float4* xlo;
+  const uint32_t* nbr_r;
+  const uint32_t* nbr_a;
+  const int32_t* cnt_r;
+  const int32_t* cnt_a;
+  const int32_t* rev_r;
+  const int32_t* rev_a;
+  const float4* fself;
+  const float* sr;
+  const float4* va;
+  const float4* fcv;
+  double* F;
+  int N, KR, KA;
+  int ref_periodic;   // drop neighbour-side terms that reach an atom through an image
+  double scale;       // -JOULEPERHARTREE
+  float sh_hi[27][3];
+  float sh_lo[27][3];
+};
+
+__global__ void __launch_bounds__(128) k_force_gather(const GatherArgs a) {
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * (blockDim.x >> 5) + wib;
+  if (i >= a.N) return;
+  const float4 hi = a.xhi[i], lo = a.xlo[i];
+  float gx = 0.f, gy = 0.f, gz = 0.f;
+  const int cr = a.cnt_r[i];
+  for (int s = lane; s < cr; s += 32) {
+    const uint32_t e = a.nbr_r[(size_t)i * a.KR + s];
+    const int rv = a.rev_r[(size_t)i * a.KR + s];
+    if (rv < 0) continue;
+    if (a.ref_periodic && tm_img(e) != TM_IMG_SELF) continue;
+    const int j = (int)tm_atom(e), r = tm_img(e);
+    const float4 hj = a.xhi[j], lj = a.xlo[j];
+    const float dx = ds_sub_shift(hi.x, lo.x, hj.x, lj.x, a.sh_hi[r][0], a.sh_lo[r][0]);
+    const float dy = ds_sub_shift(hi.y, lo.y, hj.y, lj.y, a.sh_hi[r][1], a.sh_lo[r][1]);
+    const float dz = ds_sub_shift(hi.z, lo.z, hj.z, lj.z, a.sh_hi[r][2], a.sh_lo[r][2]);
+    const float S = a.sr[rv] / sqrtf(dx * dx + dy * dy + dz * dz);
+    gx += S * dx;
+    gy += S * dy;
+    gz += S * dz;
+  }
+  const int ca = a.cnt_a[i];
+  for (int s = lane; s < ca; s += 32) {
+    const uint32_t e = a.nbr_a[(size_t)i * a.KA + s];
+    const int rv = a.rev_a[(size_t)i * a.KA + s];
+    if (rv < 0) continue;
+    if (a.ref_periodic && tm_img(e) != TM_IMG_SELF) continue;
+    const float4 v = a.va[rv];
+    gx += v.x;
+    gy += v.y;
+    gz += v.z;
+  }
+  gx = warp_sum(gx);
+  gy = warp_sum(gy);
+  gz = warp_sum(gz);
+  if (lane == 0) {
+    const float4 f0 = a.fself[i];
+    const float4 fc = a.fcv[i];
+    a.F[3 * i + 0] = a.scale * ((double)f0.x + (double)gx + (double)fc.x);
+    a.F[3 * i + 1] = a.scale * ((double)f0.y + (double)gy + (double)fc.y);
+    a.F[3 * i + 2] = a.scale * ((double)f0.z + (double)gz + (double)fc.z);
+  }
+}
+}  // namespace
+
+int tm_launch_adjoint(tm_system* s, unsigned flags) {
+  tm_ctx* ctx = s->ctx;
+  DescArgs a = make_desc_args(s);
+  const tm_consts& k = s->model->k;
+  const size_t shm = (size_t)4 * smem_floats(k.Dp, s->KA) * sizeof(float);
+  if (shm > 48 * 1024)
+    cudaFuncSetAttribute(k_desc_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  k_desc_adj<<<tm_div_up(s->N, 4), 128, shm, ctx->stream>>>(a, k);
+  GatherArgs g;
+  g.xhi = s->d_xhi; g.xlo = s->d_xlo; g.nbr_r = s->d_nbr_r; g.nbr_a = s->d_nbr_a;
+  g.cnt_r = s->d_cnt_r; g.cnt_a = s->d_cnt_a; g.rev_r = s->d_rev_r; g.rev_a = s->d_rev_a;
+  g.fself = s->d_fself; g.sr = s->d_sr; g.va = s->d_va; g.fcv = s->d_fcv; g.F = s->d_F;
+  g.N = s->N; g.KR = s->KR; g.KA = s->KA;
+  g.ref_periodic = (s->periodic && (flags & TM_F_REFERENCE_PERIODIC_FORCE)) ? 1 : 0;
+  g.scale = -2625.499638 * 1000.0;   // -JOULEPERHARTREE (PhysicalData.py:36-37)
+  tm_fill_shifts(s, g.sh_hi, g.sh_lo);
+  k_force_gather<<<tm_div_up(s->N, 4), 128, 0, ctx->stream>>>(g);
+  ctx->launches += 2;
+  return tm_cuda_check(ctx, cudaGetLastError(), "adjoint");
+}

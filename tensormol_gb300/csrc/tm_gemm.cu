@@ -1,0 +1,597 @@
+// Per-element BP network layers as tcgen05 tensor-core GEMMs (sm_103a).
+//
+// One launch computes one layer for every element and both networks
+// (grid.z = 0: EnergyNet, 1: DipoleNet; TFBehlerParinelloSymEE.py:884-944,
+// 946-1015): C[128 x 256 tile] = A[rows of one element, K] . W^T, with the
+// element of each 128-row tile taken from a table (rows of each element are
+// padded to 128, so no tile mixes elements).
+//
+// Pipeline per CTA (192 threads):
+//   warp 4       TMA producer: K-slices of A and B into a ring of 128-byte-
+//                swizzled shared-memory stages (cp.async.bulk.tensor, mbarriers)
+//   warp 5       MMA issuer: one elected thread issues tcgen05.mma into a
+//                128 x 256 FP32 accumulator in tensor memory
+//   warps 0..3   epilogue: tcgen05.ld 32 columns at a time, fused bias +
+//                activation (forward) or activation-derivative product
+//                (backward), stores to global.
+// Precision modes:
+//   TM_PREC_FP32  kind::tf32 with operands split as x = hi + lo (hi = x with
+//                 the 13 low mantissa bits cleared); D += Ahi Bhi + Ahi Blo +
+//                 Alo Bhi, FP32 accumulate. Measured on CPU emulation to give
+//                 FP32-level energy/force error.
+//   TM_PREC_BF16  kind::f16 with BF16 operands, one pass, FP32 accumulate.
+// All waits on mbarriers are bounded (about 2 s); a timeout sets the device
+// status word to TM_E_TIMEOUT and the CTA still frees its tensor memory.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "tm_internal.h"
+
+namespace {
+
+constexpr int BM = TM_BM, BN = TM_BN;
+constexpr int EPI_FWD = 0, EPI_FWD_LAST = 1, EPI_BWD = 2, EPI_OUT = 3;
+
+struct GemmArgs {
+  CUtensorMap a0, a1, b0, b1;
+  int K;             // reduction length
+  int N;             // output width of one (net, element) block
+  int a_net_rows;    // row offset of net 1 in A (0 when both nets read the same A)
+  int nele;
+  const int32_t* tile_elem;
+  int Mpad;
+  int act;
+  float alpha;
+  const float* bias;   // [2][nele][N]
+  const float* wout;   // [2][nele][N]
+  float* epart;        // [2][Mpad][N/BN]
+  void* out0;
+  void* out1;
+  int ldo;
+  const void* hprev0;
+  const void* hprev1;
+  tm_dev_status* st;
+};
+
+// ---- PTX wrappers ---------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t cnt) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(cnt) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: false after about 2^32 SM cycles.
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(b, parity)) {
+    if (clock64() - t0 > (1LL << 32)) return false;
+  }
+  return true;
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void umma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                          uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void umma_f16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+        "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (stride byte offset), version 1 (bits 46-47).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)(16 >> 4) << 16;     // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset
+  d |= (uint64_t)1 << 46;             // descriptor version
+  d |= (uint64_t)2 << 61;             // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor: D = F32, A/B format (BF16 = 1, TF32 = 2), K-major
+// A and B, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t make_idesc(int ab_format, int M, int N) {
+  return (1u << 4) | ((uint32_t)ab_format << 7) | ((uint32_t)ab_format << 10) |
+         ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// ---- activations ----------------------------------------------------------
+__device__ __forceinline__ float act_f(float z, int act, float a) {
+  switch (act) {
+    case TM_ACT_RELU: return fmaxf(z, 0.f);
+    case TM_ACT_SIGMOID_WITH_PARAM: {
+      const float t = a * z;
+      return (fmaxf(t, 0.f) + log1pf(expf(-fabsf(t)))) / a;
+    }
+    case TM_ACT_SOFTPLUS: return fmaxf(z, 0.f) + log1pf(expf(-fabsf(z)));
+    case TM_ACT_TANH: return tanhf(z);
+    default: return z > 0.f ? z : expm1f(z);   // elu
+  }
+}
+__device__ __forceinline__ float actd_z(float z, int act, float a) {
+  switch (act) {
+    case TM_ACT_RELU: return z > 0.f ? 1.f : 0.f;
+    case TM_ACT_SIGMOID_WITH_PARAM: return 1.f / (1.f + expf(-a * z));
+    case TM_ACT_SOFTPLUS: return 1.f / (1.f + expf(-z));
+    case TM_ACT_TANH: { const float t = tanhf(z); return 1.f - t * t; }
+    default: return z > 0.f ? 1.f : expf(z);
+  }
+}
+// derivative expressed through the activation's output h = act(z)
+__device__ __forceinline__ float actd_h(float h, int act, float a) {
+  switch (act) {
+    case TM_ACT_RELU: return h > 0.f ? 1.f : 0.f;
+    case TM_ACT_SIGMOID_WITH_PARAM: return -expm1f(-a * h);
+    case TM_ACT_SOFTPLUS: return -expm1f(-h);
+    case TM_ACT_TANH: return 1.f - h * h;
+    default: return h > 0.f ? 1.f : h + 1.f;
+  }
+}
+
+__device__ __forceinline__ float tf32_hi(float v) {
+  return __uint_as_float(__float_as_uint(v) & 0xffffe000u);
+}
+
+template <int PREC>
+__device__ __forceinline__ void store32(void* o0, void* o1, size_t idx, const float (&v)[32]) {
+  if (PREC == TM_PREC_FP32) {
+    float4* p0 = reinterpret_cast<float4*>(static_cast<float*>(o0) + idx);
+    float4* p1 = reinterpret_cast<float4*>(static_cast<float*>(o1) + idx);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      float4 h = make_float4(tf32_hi(v[4 * q]), tf32_hi(v[4 * q + 1]), tf32_hi(v[4 * q + 2]),
+                             tf32_hi(v[4 * q + 3]));
+      p0[q] = h;
+      p1[q] = make_float4(v[4 * q] - h.x, v[4 * q + 1] - h.y, v[4 * q + 2] - h.z,
+                          v[4 * q + 3] - h.w);
+    }
+  } else {
+    uint4* p0 = reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(o0) + idx);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      __nv_bfloat162 b0 = __floats2bfloat162_rn(v[8 * q + 0], v[8 * q + 1]);
+      __nv_bfloat162 b1 = __floats2bfloat162_rn(v[8 * q + 2], v[8 * q + 3]);
+      __nv_bfloat162 b2 = __floats2bfloat162_rn(v[8 * q + 4], v[8 * q + 5]);
+      __nv_bfloat162 b3 = __floats2bfloat162_rn(v[8 * q + 6], v[8 * q + 7]);
+      p0[q] = make_uint4(*reinterpret_cast<uint32_t*>(&b0), *reinterpret_cast<uint32_t*>(&b1),
+                         *reinterpret_cast<uint32_t*>(&b2), *reinterpret_cast<uint32_t*>(&b3));
+    }
+  }
+}
+
+template <int PREC>
+__device__ __forceinline__ void load32(const void* h0, const void* h1, size_t idx, float (&v)[32]) {
+  if (PREC == TM_PREC_FP32) {
+    const float4* p0 = reinterpret_cast<const float4*>(static_cast<const float*>(h0) + idx);
+    const float4* p1 = reinterpret_cast<const float4*>(static_cast<const float*>(h1) + idx);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const float4 a = p0[q], b = p1[q];
+      v[4 * q] = a.x + b.x;
+      v[4 * q + 1] = a.y + b.y;
+      v[4 * q + 2] = a.z + b.z;
+      v[4 * q + 3] = a.w + b.w;
+    }
+  } else {
+    const uint4* p0 = reinterpret_cast<const uint4*>(static_cast<const __nv_bfloat16*>(h0) + idx);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      uint4 u = p0[q];
+      uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        __nv_bfloat162 b = *reinterpret_cast<__nv_bfloat162*>(&w[t]);
+        float2 f = __bfloat1622float2(b);
+        v[8 * q + 2 * t] = f.x;
+        v[8 * q + 2 * t + 1] = f.y;
+      }
+    }
+  }
+}
+
+template <int PREC>
+struct Cfg {
+  static constexpr int ELEM = PREC == TM_PREC_FP32 ? 4 : 2;
+  static constexpr int BK = 128 / ELEM;               // one 128-byte swizzle row
+  static constexpr int NSPLIT = PREC == TM_PREC_FP32 ? 2 : 1;
+  static constexpr int A_TILE = BM * 128;             // 16 KB
+  static constexpr int B_TILE = BN * 128;             // 32 KB
+  static constexpr int STAGE = NSPLIT * (A_TILE + B_TILE);
+  static constexpr int NSTAGE = PREC == TM_PREC_FP32 ? 2 : 4;
+  static constexpr int SMEM = NSTAGE * STAGE + 1024 + 256;
+  static constexpr uint32_t IDESC = make_idesc(PREC == TM_PREC_FP32 ? 2 : 1, BM, BN);
+};
+
+template <int PREC, int EPI>
+__global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArgs g) {
+  using C = Cfg<PREC>;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~static_cast<uintptr_t>(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + C::NSTAGE * C::STAGE);
+  uint64_t* empty = full + C::NSTAGE;
+  uint64_t* accf = empty + C::NSTAGE;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accf + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m_tile = blockIdx.x, n_tile = blockIdx.y, net = blockIdx.z;
+  const int nk = g.K / C::BK;
+  const int elem = g.tile_elem[m_tile];
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < C::NSTAGE; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(accf, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(BN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 4) {
+    if (lane == 0) {
+      const int a_row = net * g.a_net_rows + m_tile * BM;
+      const int b_row = (net * g.nele + elem) * g.N + n_tile * BN;
+      for (int kb = 0; kb < nk; ++kb) {
+        const int s = kb % C::NSTAGE;
+        if (kb >= C::NSTAGE) {
+          if (!mbar_wait(&empty[s], ((kb / C::NSTAGE) - 1) & 1)) {
+            tm_flag(g.st, TM_E_TIMEOUT, kb, 100);
+            break;
+          }
+        }
+        uint8_t* st = smem + s * C::STAGE;
+        mbar_expect_tx(&full[s], C::STAGE);
+        const int x = kb * C::BK;
+        tma_load_2d(st, &g.a0, x, a_row, &full[s]);
+        tma_load_2d(st + C::NSPLIT * C::A_TILE, &g.b0, x, b_row, &full[s]);
+        if (C::NSPLIT == 2) {
+          tma_load_2d(st + C::A_TILE, &g.a1, x, a_row, &full[s]);
+          tma_load_2d(st + 2 * C::A_TILE + C::B_TILE, &g.b1, x, b_row, &full[s]);
+        }
+      }
+    }
+  } else if (warp == 5) {
+    if (lane == 0) {
+      bool ok = true;
+      for (int kb = 0; kb < nk; ++kb) {
+        const int s = kb % C::NSTAGE;
+        if (!mbar_wait(&full[s], (kb / C::NSTAGE) & 1)) {
+          tm_flag(g.st, TM_E_TIMEOUT, kb, 101);
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t base = smem_u32(smem + s * C::STAGE);
+        const uint32_t a0 = base;
+        const uint32_t a1 = base + C::A_TILE;
+        const uint32_t b0 = base + C::NSPLIT * C::A_TILE;
+        const uint32_t b1 = b0 + C::B_TILE;
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+          const uint64_t ad0 = sw128_desc(a0 + kk * 32), bd0 = sw128_desc(b0 + kk * 32);
+          const uint32_t acc = (kb | kk) ? 1u : 0u;
+          if (PREC == TM_PREC_FP32) {
+            const uint64_t ad1 = sw128_desc(a1 + kk * 32), bd1 = sw128_desc(b1 + kk * 32);
+            umma_tf32(tmem, ad0, bd0, C::IDESC, acc);
+            umma_tf32(tmem, ad0, bd1, C::IDESC, 1u);
+            umma_tf32(tmem, ad1, bd0, C::IDESC, 1u);
+          } else {
+            umma_f16(tmem, ad0, bd0, C::IDESC, acc);
+          }
+        }
+        umma_commit(&empty[s]);
+      }
+      if (ok) umma_commit(accf);
+    }
+  } else {
+    // ---- epilogue: warps 0..3, thread = accumulator row ----
+    const bool ready = mbar_wait(accf, 0);
+    if (!ready) tm_flag(g.st, TM_E_TIMEOUT, m_tile, 102);
+    tc_fence_after();
+    if (ready) {
+      const int row = m_tile * BM + warp * 32 + lane;          // row in this net
+      const size_t orow = (size_t)net * g.Mpad + row;
+      const int pblk = (net * g.nele + elem) * g.N;
+      float esum = 0.f;
+      for (int c = 0; c < BN; c += 32) {
+        uint32_t r[32];
+        tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, r);
+        const int col = n_tile * BN + c;
+        float v[32];
+        if (EPI == EPI_FWD || EPI == EPI_FWD_LAST) {
+          const float* bias = g.bias + pblk + col;
+#pragma unroll
+          for (int q = 0; q < 32; ++q) {
+            const float z = __uint_as_float(r[q]) + __ldg(bias + q);
+            if (EPI == EPI_FWD) {
+              v[q] = act_f(z, g.act, g.alpha);
+            } else {
+              const float w = __ldg(g.wout + pblk + col + q);
+              esum += act_f(z, g.act, g.alpha) * w;
+              v[q] = w * actd_z(z, g.act, g.alpha);
+            }
+          }
+          store32<PREC>(g.out0, g.out1, orow * g.ldo + col, v);
+        } else if (EPI == EPI_BWD) {
+          float h[32];
+          load32<PREC>(g.hprev0, g.hprev1, orow * g.ldo + col, h);
+#pragma unroll
+          for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]) * actd_h(h[q], g.act, g.alpha);
+          store32<PREC>(g.out0, g.out1, orow * g.ldo + col, v);
+        } else {
+          float4* o = reinterpret_cast<float4*>(static_cast<float*>(g.out0) + orow * g.ldo + col);
+#pragma unroll
+          for (int q = 0; q < 8; ++q)
+            o[q] = make_float4(__uint_as_float(r[4 * q]), __uint_as_float(r[4 * q + 1]),
+                               __uint_as_float(r[4 * q + 2]), __uint_as_float(r[4 * q + 3]));
+        }
+      }
+      if (EPI == EPI_FWD_LAST) g.epart[orow * (g.N / BN) + n_tile] = esum;
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN)
+                 : "memory");
+  }
+}
+
+template <int PREC, int EPI>
+int launch_gemm(tm_ctx* ctx, const GemmArgs& g, int mtiles, int ntiles) {
+  using C = Cfg<PREC>;
+  cudaError_t e = cudaFuncSetAttribute(k_gemm<PREC, EPI>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
+  if (e != cudaSuccess) return tm_cuda_check(ctx, e, "gemm attr");
+  dim3 grid(mtiles, ntiles, 2);
+  k_gemm<PREC, EPI><<<grid, 192, C::SMEM, ctx->stream>>>(g);
+  ctx->launches++;
+  return tm_cuda_check(ctx, cudaGetLastError(), "gemm");
+}
+
+template <int PREC>
+int run_gemm(tm_ctx* ctx, int epi, const GemmArgs& g, int mtiles, int ntiles) {
+  switch (epi) {
+    case EPI_FWD: return launch_gemm<PREC, EPI_FWD>(ctx, g, mtiles, ntiles);
+    case EPI_FWD_LAST: return launch_gemm<PREC, EPI_FWD_LAST>(ctx, g, mtiles, ntiles);
+    case EPI_BWD: return launch_gemm<PREC, EPI_BWD>(ctx, g, mtiles, ntiles);
+    default: return launch_gemm<PREC, EPI_OUT>(ctx, g, mtiles, ntiles);
+  }
+}
+
+int dispatch(tm_ctx* ctx, int prec, int epi, const GemmArgs& g, int mtiles, int ntiles) {
+  return prec == TM_PREC_FP32 ? run_gemm<TM_PREC_FP32>(ctx, epi, g, mtiles, ntiles)
+                              : run_gemm<TM_PREC_BF16>(ctx, epi, g, mtiles, ntiles);
+}
+
+}  // namespace
+
+int tm_make_tmap(tm_ctx* ctx, CUtensorMap* map, void* base, int elem_bytes, uint64_t rows,
+                 uint64_t cols, uint32_t box_rows) {
+  if (!ctx->encode) return tm_fail(ctx, TM_E_CUDA, "cuTensorMapEncodeTiled unavailable");
+  const CUtensorMapDataType dt =
+      elem_bytes == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+  cuuint64_t dims[2] = {cols, rows};
+  cuuint64_t strides[1] = {cols * (cuuint64_t)elem_bytes};
+  cuuint32_t box[2] = {(cuuint32_t)(128 / elem_bytes), box_rows};
+  cuuint32_t es[2] = {1, 1};
+  if ((reinterpret_cast<uintptr_t>(base) & 15) || (strides[0] & 15))
+    return tm_fail(ctx, TM_E_ARG, "tensor map alignment");
+  CUresult r = ctx->encode(map, dt, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                           CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return tm_fail(ctx, TM_E_CUDA, "cuTensorMapEncodeTiled failed");
+  return TM_OK;
+}
+
+// Six launches per energy+force (both networks per launch):
+//   fwd 0..L-1 (last one: energy dot product + g_L = w_out * act'(z_L)),
+//   bwd L-1..1 (g_{l-1} = (g_l W_l^T) * act'(z_{l-1}), in place over h_{l-1}),
+//   bwd 0 (dE/dG = g_1 W_1^T, FP32).
+int tm_launch_mlp(tm_system* s, bool backward) {
+  tm_model* m = s->model;
+  tm_ctx* ctx = s->ctx;
+  const int L = m->nlayer;
+  const int H = m->H, Dp = m->k.Dp;
+  const int mt = s->ntiles;
+  const int prec = m->desc.precision;
+  int rc;
+  // activation buffers: level 0 = G (shared), levels 1..L-1 = H_l, level L = g_L
+  const CUtensorMap* lv0[2] = {&s->tm_G[0], &s->tm_G[1]};
+  const CUtensorMap* lvH[TM_MAX_HIDDEN][2] = {{&s->tm_H1[0], &s->tm_H1[1]},
+                                              {&s->tm_H2[0], &s->tm_H2[1]}};
+  void* bufH[TM_MAX_HIDDEN][2] = {{s->H1[0], s->H1[1]}, {s->H2[0], s->H2[1]}};
+  GemmArgs g;
+  memset(&g, 0, sizeof(g));
+  g.nele = m->k.nele;
+  g.tile_elem = s->tile_elem;
+  g.Mpad = s->Mpad;
+  g.act = m->k.act;
+  g.alpha = m->k.alpha_sig;
+  g.st = ctx->d_status;
+  for (int l = 0; l < L; ++l) {
+    const bool last = (l == L - 1);
+    const CUtensorMap* const* A = l == 0 ? lv0 : lvH[l - 1];
+    g.a0 = *A[0];
+    g.a1 = *A[1];
+    g.b0 = m->tm_wf[l][0];
+    g.b1 = m->tm_wf[l][1];
+    g.K = l == 0 ? Dp : H;
+    g.N = H;
+    g.a_net_rows = l == 0 ? 0 : s->Mpad;
+    g.bias = m->bias[l];
+    g.wout = m->wout;
+    g.epart = s->epart;
+    g.ldo = H;
+    g.out0 = last ? s->G3[0] : bufH[l][0];
+    g.out1 = last ? s->G3[1] : bufH[l][1];
+    if ((rc = dispatch(ctx, prec, last ? EPI_FWD_LAST : EPI_FWD, g, mt, H / BN))) return rc;
+  }
+  if (!backward) return TM_OK;
+  for (int l = L - 1; l >= 0; --l) {
+    // A = g_{l+1} (level l+1 buffer), B = W_l as [Kin x Nout] rows
+    const CUtensorMap* gA[2];
+    if (l == L - 1) { gA[0] = &s->tm_G3[0]; gA[1] = &s->tm_G3[1]; }
+    else { gA[0] = lvH[l][0]; gA[1] = lvH[l][1]; }
+    g.a0 = *gA[0];
+    g.a1 = *gA[1];
+    g.b0 = m->tm_wb[l][0];
+    g.b1 = m->tm_wb[l][1];
+    g.K = H;
+    g.a_net_rows = s->Mpad;
+    if (l > 0) {
+      g.N = H;
+      g.ldo = H;
+      g.hprev0 = bufH[l - 1][0];
+      g.hprev1 = bufH[l - 1][1];
+      g.out0 = bufH[l - 1][0];
+      g.out1 = bufH[l - 1][1];
+      if ((rc = dispatch(ctx, prec, EPI_BWD, g, mt, H / BN))) return rc;
+    } else {
+      g.N = Dp;
+      g.ldo = Dp;
+      g.out0 = s->dEdG;
+      g.out1 = nullptr;
+      if ((rc = dispatch(ctx, prec, EPI_OUT, g, mt, Dp / BN))) return rc;
+    }
+  }
+  return TM_OK;
+}
+
+// Stand-alone check of the tensor-core path: C[M,N] = A[M,K] B[N,K]^T with a
+// single element and net 0 (host fp32 in/out). Used by the GPU tests.
+int tm_gemm_selftest(tm_ctx* ctx, int prec, int M, int N, int K, const float* A, const float* B,
+                     float* Cout) {
+  if (M % BM || N % BN || K % 64) return tm_fail(ctx, TM_E_ARG, "selftest shape");
+  const int eb = prec == TM_PREC_FP32 ? 4 : 2;
+  const size_t nA = (size_t)M * K, nB = (size_t)N * K, nC = (size_t)M * N;
+  std::vector<uint8_t> ha0(nA * eb), ha1(nA * eb), hb0(nB * eb), hb1(nB * eb);
+  auto split = [&](const float* src, size_t n, uint8_t* d0, uint8_t* d1) {
+    for (size_t q = 0; q < n; ++q) {
+      if (prec == TM_PREC_FP32) {
+        uint32_t u;
+        memcpy(&u, &src[q], 4);
+        u &= 0xffffe000u;
+        float h;
+        memcpy(&h, &u, 4);
+        float lo = src[q] - h;
+        memcpy(d0 + 4 * q, &h, 4);
+        memcpy(d1 + 4 * q, &lo, 4);
+      } else {
+        __nv_bfloat16 b = __float2bfloat16_rn(src[q]);
+        memcpy(d0 + 2 * q, &b, 2);
+      }
+    }
+  };
+  split(A, nA, ha0.data(), ha1.data());
+  split(B, nB, hb0.data(), hb1.data());
+  // stack two copies of B rows so that net 1 (unused output) stays in bounds
+  void *da0, *da1, *db0, *db1, *dc, *dc1, *dbias, *dw;
+  int32_t* dte;
+  tm_dev_status* st = ctx->d_status;
+  int rc = 0;
+  if ((rc = tm_alloc(ctx, &da0, nA * eb * 2)) || (rc = tm_alloc(ctx, &da1, nA * eb * 2)) ||
+      (rc = tm_alloc(ctx, &db0, nB * eb * 2)) || (rc = tm_alloc(ctx, &db1, nB * eb * 2)) ||
+      (rc = tm_alloc(ctx, &dc, nC * 4 * 2)) || (rc = tm_alloc(ctx, &dc1, nC * 4 * 2)) ||
+      (rc = tm_alloc(ctx, &dbias, (size_t)N * 4 * 2)) || (rc = tm_alloc(ctx, &dw, (size_t)N * 4 * 2)) ||
+      (rc = tm_alloc(ctx, (void**)&dte, sizeof(int32_t) * (M / BM))))
+    return rc;
+  cudaStream_t sm = ctx->stream;
+  for (int c = 0; c < 2; ++c) {
+    cudaMemcpyAsync((uint8_t*)da0 + c * nA * eb, ha0.data(), nA * eb, cudaMemcpyHostToDevice, sm);
+    cudaMemcpyAsync((uint8_t*)da1 + c * nA * eb, ha1.data(), nA * eb, cudaMemcpyHostToDevice, sm);
+    cudaMemcpyAsync((uint8_t*)db0 + c * nB * eb, hb0.data(), nB * eb, cudaMemcpyHostToDevice, sm);
+    cudaMemcpyAsync((uint8_t*)db1 + c * nB * eb, hb1.data(), nB * eb, cudaMemcpyHostToDevice, sm);
+  }
+  cudaMemsetAsync(dte, 0, sizeof(int32_t) * (M / BM), sm);
+  GemmArgs g;
+  memset(&g, 0, sizeof(g));
+  if ((rc = tm_make_tmap(ctx, &g.a0, da0, eb, 2 * (uint64_t)M, K, BM)) ||
+      (rc = tm_make_tmap(ctx, &g.a1, prec == TM_PREC_FP32 ? da1 : da0, eb, 2 * (uint64_t)M, K, BM)) ||
+      (rc = tm_make_tmap(ctx, &g.b0, db0, eb, 2 * (uint64_t)N, K, BN)) ||
+      (rc = tm_make_tmap(ctx, &g.b1, prec == TM_PREC_FP32 ? db1 : db0, eb, 2 * (uint64_t)N, K, BN)))
+    return rc;
+  g.K = K; g.N = N; g.a_net_rows = M; g.nele = 1; g.tile_elem = dte; g.Mpad = M;
+  g.out0 = dc; g.out1 = dc1; g.ldo = N; g.st = st;
+  rc = dispatch(ctx, prec, EPI_OUT, g, M / BM, N / BN);
+  if (!rc) rc = tm_cuda_check(ctx, cudaMemcpyAsync(Cout, dc, nC * 4, cudaMemcpyDeviceToHost, sm), "selftest d2h");
+  if (!rc) rc = tm_sync_status(ctx, "gemm selftest");
+  tm_free(ctx, da0, nA * eb * 2); tm_free(ctx, da1, nA * eb * 2);
+  tm_free(ctx, db0, nB * eb * 2); tm_free(ctx, db1, nB * eb * 2);
+  tm_free(ctx, dc, nC * 8); tm_free(ctx, dc1, nC * 8);
+  tm_free(ctx, dbias, (size_t)N * 8); tm_free(ctx, dw, (size_t)N * 8);
+  tm_free(ctx, dte, sizeof(int32_t) * (M / BM));
+  return rc;
+}

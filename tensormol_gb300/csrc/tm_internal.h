@@ -1,0 +1,188 @@
+// Internal host/device structures of libtmgpu (not part of the ABI).
+#pragma once
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/tmgpu.h"
+#include "tm_common.cuh"
+
+#define TM_MAX_ELE 8
+#define TM_MAX_HIDDEN 4
+#define TM_BN 256          // GEMM N tile
+#define TM_BM 128          // GEMM M tile (rows per element are padded to this)
+
+// Constants of the model read by the device kernels (passed by value).
+struct tm_consts {
+  int nele, nelep, nr, na_rs, na_as, D, Dp;
+  int act;
+  float alpha_sig;
+  float r_rc, a_rc, eta, zeta, zeta_pow2;  // zeta_pow2: 1 when zeta == 8
+  float pi_tf;                              // 3.14159265359 as in RawSymFunc.py
+  float rs_r[32], rs_a[8], cos_th[8], sin_th[8];
+  float two_1mz;                            // 2^(1 - zeta)
+  int elepair[TM_MAX_ELE][TM_MAX_ELE];      // unordered element pair -> index
+  // Coulomb / vdW (atomic units, see params.coulomb_constants)
+  float bohr, alpha, r_lr, r_sr, elu_shift, elu_a, zz, yy;
+  float vdw_width, vdw_begin;
+  float c6[TM_MAX_ELE], r0[TM_MAX_ELE];
+  double r_rc_d, a_rc_d, ree_d;             // membership radii (FP64 test)
+  float ree;
+  int add_ecc, has_vdw;
+};
+
+// Per-molecule cell grid.
+struct tm_grid {
+  double ox, oy, oz;      // origin
+  double cx, cy, cz;      // cell edge per dimension
+  int nx, ny, nz;
+  int cell_off;           // first global cell index
+  int periodic;
+  int atom_off, natom;    // atoms of the molecule
+  int pad;
+};
+
+struct tm_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  size_t budget = 0, in_use = 0;
+  int64_t launches = 0;
+  tm_dev_status* d_status = nullptr;
+  tm_dev_status* h_status = nullptr;   // pinned
+  std::string err;
+  PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+};
+
+struct tm_layer_host {
+  std::vector<double> W, b;
+  int fan_in = 0, fan_out = 0;
+  bool set = false;
+};
+
+struct tm_model {
+  tm_ctx* ctx = nullptr;
+  tm_model_desc desc;
+  tm_consts k;
+  int H = 0;         // padded hidden width (multiple of TM_BN), all layers equal
+  int nlayer = 0;    // hidden layers
+  bool final_ = false;
+  // host copies: [net][ele][layer]
+  std::vector<tm_layer_host> layers;  // index (net*nele + e)*(nlayer+1) + l
+  // device weights (row-major, stacked over net, element):
+  //   fwd[l]: W^T [2*nele*Nout_l][Kin_l] (hi, lo), bwd[l]: W [2*nele*Kin_l][Nout_l]
+  void* w_fwd[TM_MAX_HIDDEN][2] = {};
+  void* w_bwd[TM_MAX_HIDDEN][2] = {};
+  float* bias[TM_MAX_HIDDEN] = {};     // [2][nele][H]
+  float* wout = nullptr;               // [2][nele][H]  last layer weight vector
+  double* bout = nullptr;              // [2][nele]
+  CUtensorMap tm_wf[TM_MAX_HIDDEN][2];
+  CUtensorMap tm_wb[TM_MAX_HIDDEN][2];
+  size_t elem_size = 4;                // 4 (tf32 split) or 2 (bf16)
+};
+
+struct tm_system {
+  tm_model* model = nullptr;
+  tm_ctx* ctx = nullptr;
+  int N = 0, nmol = 0;
+  bool periodic = false;
+  double lat[9] = {0};
+  std::vector<int32_t> Z;              // host
+  std::vector<int64_t> off;            // host
+  std::vector<int32_t> elem_h;         // element index per atom
+  // element-sorted MLP rows
+  int Mpad = 0, ntiles = 0;
+  std::vector<int32_t> row_of_atom_h, tile_elem_h;
+  int32_t* row_of_atom = nullptr;
+  int32_t* atom_of_row = nullptr;      // -1 for padding rows
+  int32_t* tile_elem = nullptr;
+  // atoms
+  int32_t* d_Z = nullptr;
+  int32_t* d_elem = nullptr;
+  int32_t* d_mol = nullptr;            // molecule of atom
+  int32_t* d_off = nullptr;            // [nmol+1]
+  double* d_x = nullptr;               // [N][3]
+  float4* d_xhi = nullptr;             // hi parts (w = element index)
+  float4* d_xlo = nullptr;
+  double* d_x_at_build = nullptr;      // positions at the last list build
+  // cell grid
+  tm_grid* d_grid = nullptr;           // [nmol]
+  int ncell_cap = 0;
+  int32_t* d_ncell = nullptr;          // total cells (device scalar)
+  int32_t* d_ncell_m = nullptr;        // [nmol] cells per molecule
+  int32_t* d_need = nullptr;           // [2] largest radial / angular count seen
+  int32_t* d_cell_cnt = nullptr;       // [ncell_cap+1]
+  int32_t* d_cell_start = nullptr;     // [ncell_cap+1]
+  int32_t* d_cell_atoms = nullptr;     // [N]
+  int32_t* d_cell_of_atom = nullptr;   // [N]
+  // neighbour lists (ELL, per centre sorted by (element, reference index))
+  int KR = 64, KA = 48;
+  int32_t* d_cnt_r = nullptr;
+  int32_t* d_cnt_a = nullptr;
+  uint32_t* d_nbr_r = nullptr;         // [N*KR] packed (img << 27 | atom)
+  uint32_t* d_nbr_a = nullptr;         // [N*KA]
+  int32_t* d_rev_r = nullptr;          // [N*KR] j*KR + position of i in j's list
+  int32_t* d_rev_a = nullptr;
+  bool nlist_valid = false;
+  // descriptors + networks
+  void* G[2] = {};                     // [Mpad][Dp] hi/lo (tf32) or bf16 (G[0])
+  void* H1[2] = {};                    // [2*Mpad][H] per net stacked
+  void* H2[2] = {};
+  void* G3[2] = {};
+  float* dEdG = nullptr;               // [2*Mpad][Dp]
+  float* epart = nullptr;              // [2][Mpad][H/TM_BN]
+  CUtensorMap tm_G[2], tm_H1[2], tm_H2[2], tm_G3[2];
+  // per atom
+  double* d_Eatom = nullptr;           // [N]
+  float* d_qraw = nullptr;             // [N]
+  float* d_q = nullptr;                // neutralised [N]
+  float* d_dEdq = nullptr;             // [N]
+  float4* d_fself = nullptr;           // [N] centre-side dE/dx from descriptors
+  float* d_sr = nullptr;               // [N*KR] radial edge scalars
+  float4* d_va = nullptr;              // [N*KA] angular edge vectors
+  float4* d_fcv = nullptr;             // [N] Coulomb+vdW dE/dx (xyz), w unused
+  double* d_ecv = nullptr;             // [N][2] per-atom half pair energies (cc, vdw)
+  double* d_F = nullptr;               // [N][3] force (J/mol/A)
+  double* d_mol_E = nullptr;           // [nmol][4]
+  double* d_mol_aux = nullptr;         // [nmol][8]: sum q, sum dEdq~, dipole xyz
+  // export scratch
+  int64_t* d_exp_off = nullptr;        // [N+1]
+  size_t bytes = 0;
+};
+
+// ---- helpers (tm_api.cu) ----
+int tm_fail(tm_ctx* ctx, int code, const std::string& msg);
+int tm_cuda_check(tm_ctx* ctx, cudaError_t e, const char* what);
+int tm_alloc(tm_ctx* ctx, void** p, size_t bytes);
+void tm_free(tm_ctx* ctx, void* p, size_t bytes);
+int tm_sync_status(tm_ctx* ctx, const char* what);
+
+// ---- launchers ----
+// tm_nlist.cu
+int tm_launch_positions(tm_system* s);
+int tm_launch_nlist(tm_system* s);
+int tm_nlist_grow(tm_system* s, bool* grew);
+int tm_launch_export_nlist(tm_system* s, int64_t* radp, int64_t* angt, int64_t* mil_j,
+                           int64_t* mil_jk, int64_t P, int64_t T);
+int tm_count_ee(tm_system* s, int64_t* npairs);
+int tm_launch_export_ee(tm_system* s, int64_t* eep, int64_t cap);
+int tm_count_nlist(tm_system* s, int64_t counts[4]);
+// tm_desc.cu
+int tm_launch_descriptors(tm_system* s);
+int tm_launch_adjoint(tm_system* s, unsigned flags);
+// tm_gemm.cu
+int tm_make_tmap(tm_ctx* ctx, CUtensorMap* map, void* base, int elem_bytes, uint64_t rows,
+                 uint64_t cols, uint32_t box_rows);
+int tm_launch_mlp(tm_system* s, bool backward);
+int tm_gemm_selftest(tm_ctx* ctx, int prec, int M, int N, int K, const float* A,
+                     const float* B, float* C);
+// tm_coulomb.cu
+int tm_launch_mlp_finish(tm_system* s);
+int tm_launch_coulomb(tm_system* s, unsigned flags);
+int tm_launch_finish(tm_system* s, unsigned flags);
+
+static inline int tm_div_up(int a, int b) { return (a + b - 1) / b; }

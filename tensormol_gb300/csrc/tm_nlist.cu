@@ -1,0 +1,891 @@
+// Cell-list neighbour build, bit-exact with the reference's pair and triple sets.
+//
+// Reference: MolEmb.Make_NListNaive (C_API/MolEmb.cpp:1180-1251) decides
+// membership with sqrt(dx^2+dy^2+dz^2) + 1e-13 < rc in FP64; the Python layer
+// (ForceModifiers/Neighbors.py:117-201, 344-470) flattens, builds j<k triples,
+// tags elements, lexsorts and numbers slots. Here:
+//   * atoms are binned per molecule into cells of edge >= AN1_r_Rc;
+//   * one warp per centre atom screens the 27 neighbouring cells with an FP32
+//     double-single distance and settles every candidate within 1e-5 (relative,
+//     on d^2) of a cutoff with the reference's exact FP64 expression;
+//   * accepted neighbours are sorted per centre by (element, reference index),
+//     which is the reference's (mol, i, l, j) lexsort order, and stored in
+//     fixed-capacity rows (ELL) for the descriptor kernels;
+//   * periodic cells use minimum-image search over wrapped cells; each entry
+//     carries the image shift whose raster index reproduces the reference's
+//     27-image tessellation numbering (ForceModifiers/Periodic.py:131-181).
+#include <cuda_runtime.h>
+
+#include "tm_internal.h"
+
+namespace {
+
+constexpr float kBand = 1e-5f;   // relative band on d^2 settled in FP64
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// ---------------------------------------------------------------------------
+// positions: FP64 -> double-single, finiteness check
+// ---------------------------------------------------------------------------
+__global__ void k_positions(const double* __restrict__ x, const int32_t* __restrict__ elem,
+                            float4* __restrict__ xhi, float4* __restrict__ xlo, int N,
+                            tm_dev_status* st) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  double a = x[3 * i], b = x[3 * i + 1], c = x[3 * i + 2];
+  if (!isfinite(a) || !isfinite(b) || !isfinite(c)) tm_flag(st, TM_E_NONFINITE, i, 1);
+  float ah = (float)a, bh = (float)b, ch = (float)c;
+  xhi[i] = make_float4(ah, bh, ch, __int_as_float(elem[i]));
+  xlo[i] = make_float4((float)(a - (double)ah), (float)(b - (double)bh), (float)(c - (double)ch), 0.f);
+}
+
+// ---------------------------------------------------------------------------
+// per-molecule grid set-up (block per molecule)
+// ---------------------------------------------------------------------------
+__global__ void k_grid_setup(const double* __restrict__ x, const int32_t* __restrict__ off,
+                             tm_grid* __restrict__ grid, int32_t* __restrict__ ncell_m,
+                             double rc, int periodic, double Lx, double Ly, double Lz) {
+  const int m = blockIdx.x;
+  const int a0 = off[m], a1 = off[m + 1];
+  __shared__ double smin[3][32], smax[3][32];
+  double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+  for (int a = a0 + threadIdx.x; a < a1; a += blockDim.x) {
+    for (int d = 0; d < 3; ++d) {
+      double v = x[3 * a + d];
+      mn[d] = fmin(mn[d], v);
+      mx[d] = fmax(mx[d], v);
+    }
+  }
+  for (int d = 0; d < 3; ++d) {
+    for (int o = 16; o > 0; o >>= 1) {
+      mn[d] = fmin(mn[d], __shfl_xor_sync(TM_FULL, mn[d], o));
+      mx[d] = fmax(mx[d], __shfl_xor_sync(TM_FULL, mx[d], o));
+    }
+  }
+  const int w = threadIdx.x / 32, l = threadIdx.x % 32, nw = blockDim.x / 32;
+  if (l == 0)
+    for (int d = 0; d < 3; ++d) { smin[d][w] = mn[d]; smax[d][w] = mx[d]; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int d = 0; d < 3; ++d) {
+      for (int q = 1; q < nw; ++q) { mn[d] = fmin(mn[d], smin[d][q]); mx[d] = fmax(mx[d], smax[d][q]); }
+    }
+    tm_grid g;
+    g.atom_off = a0;
+    g.natom = a1 - a0;
+    g.periodic = periodic;
+    g.pad = 0;
+    if (periodic) {
+      g.ox = g.oy = g.oz = 0.0;
+      g.nx = max(1, (int)floor(Lx / rc));
+      g.ny = max(1, (int)floor(Ly / rc));
+      g.nz = max(1, (int)floor(Lz / rc));
+      g.cx = Lx / g.nx; g.cy = Ly / g.ny; g.cz = Lz / g.nz;
+    } else {
+      if (a1 <= a0) { mn[0] = mn[1] = mn[2] = 0.0; mx[0] = mx[1] = mx[2] = 0.0; }
+      // non-finite or absurd extents collapse to a single cell (the positions
+      // kernel has already flagged them); counts never exceed the cap
+      double ext[3];
+      for (int d = 0; d < 3; ++d) {
+        ext[d] = mx[d] - mn[d];
+        if (!(ext[d] >= 0.0 && ext[d] < 1e7)) { ext[d] = 0.0; mn[d] = 0.0; }
+      }
+      g.ox = mn[0]; g.oy = mn[1]; g.oz = mn[2];
+      const double cap = 2.0 * (a1 - a0) + 64.0;
+      double cs = rc;
+      for (int it = 0; it < 200; ++it) {
+        const double p = (floor(ext[0] / cs) + 1.0) * (floor(ext[1] / cs) + 1.0) * (floor(ext[2] / cs) + 1.0);
+        if (p <= cap) break;
+        cs *= 1.25;
+      }
+      g.cx = g.cy = g.cz = cs;
+      g.nx = (int)floor(ext[0] / cs) + 1;
+      g.ny = (int)floor(ext[1] / cs) + 1;
+      g.nz = (int)floor(ext[2] / cs) + 1;
+      if ((double)g.nx * g.ny * g.nz > cap) g.nx = g.ny = g.nz = 1;
+    }
+    g.cell_off = 0;
+    grid[m] = g;
+    ncell_m[m] = g.nx * g.ny * g.nz;
+  }
+}
+
+__device__ __forceinline__ int cell_coord(double v, double o, double c, int n) {
+  int q = (int)floor((v - o) / c);
+  return q < 0 ? 0 : (q >= n ? n - 1 : q);
+}
+
+__global__ void k_cell_count(const double* __restrict__ x, const int32_t* __restrict__ mol,
+                             const tm_grid* __restrict__ grid, int32_t* __restrict__ cnt,
+                             int32_t* __restrict__ cell_of, int N, int cap, tm_dev_status* st) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const tm_grid g = grid[mol[i]];
+  int ix = cell_coord(x[3 * i], g.ox, g.cx, g.nx);
+  int iy = cell_coord(x[3 * i + 1], g.oy, g.cy, g.ny);
+  int iz = cell_coord(x[3 * i + 2], g.oz, g.cz, g.nz);
+  int c = g.cell_off + (ix * g.ny + iy) * g.nz + iz;
+  if (c < 0 || c >= cap) {   // cannot happen for a valid grid; never index out of range
+    tm_flag(st, TM_E_CAPACITY, i, 2);
+    c = 0;
+  }
+  cell_of[i] = c;
+  atomicAdd(&cnt[c], 1);
+}
+
+__global__ void k_cell_fill(const int32_t* __restrict__ cell_of, const int32_t* __restrict__ start,
+                            int32_t* __restrict__ cursor, int32_t* __restrict__ atoms, int N) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  int c = cell_of[i];
+  atoms[start[c] + atomicAdd(&cursor[c], 1)] = i;
+}
+
+// Atom order inside a cell is made deterministic (ascending index).
+__global__ void k_cell_sort(const int32_t* __restrict__ start, int32_t* __restrict__ atoms,
+                            const int32_t* __restrict__ ncell, int cap) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cap || c >= *ncell) return;
+  int a = start[c], b = start[c + 1];
+  for (int p = a + 1; p < b; ++p) {
+    int v = atoms[p];
+    int q = p - 1;
+    while (q >= a && atoms[q] > v) { atoms[q + 1] = atoms[q]; --q; }
+    atoms[q + 1] = v;
+  }
+}
+
+__global__ void k_grid_offsets(tm_grid* __restrict__ grid, const int32_t* __restrict__ ncell_m,
+                               int nmol, int32_t* __restrict__ total, int cap, tm_dev_status* st) {
+  // single thread: nmol is at most a few thousand; this runs once per build
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int acc = 0;
+  for (int m = 0; m < nmol; ++m) {
+    grid[m].cell_off = acc;
+    acc += ncell_m[m];
+  }
+  *total = acc;
+  if (acc > cap) tm_flag(st, TM_E_CAPACITY, acc, 2);
+}
+
+// ---------------------------------------------------------------------------
+// exclusive scan (int32 / int64), three passes
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_scan_blocks(const T* __restrict__ in, T* __restrict__ out, T* __restrict__ bsum,
+                              int64_t n) {
+  __shared__ T s[1024];
+  const int64_t base = (int64_t)blockIdx.x * 4096;
+  T v[4];
+  T tsum = 0;
+  for (int q = 0; q < 4; ++q) {
+    int64_t idx = base + threadIdx.x * 4 + q;
+    v[q] = idx < n ? in[idx] : (T)0;
+    tsum += v[q];
+  }
+  s[threadIdx.x] = tsum;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    T t = threadIdx.x >= o ? s[threadIdx.x - o] : (T)0;
+    __syncthreads();
+    s[threadIdx.x] += t;
+    __syncthreads();
+  }
+  T run = s[threadIdx.x] - tsum;
+  for (int q = 0; q < 4; ++q) {
+    int64_t idx = base + threadIdx.x * 4 + q;
+    if (idx < n) out[idx] = run;
+    run += v[q];
+  }
+  if (threadIdx.x == 1023) bsum[blockIdx.x] = s[1023];
+}
+
+template <typename T>
+__global__ void k_scan_top(T* __restrict__ bsum, int nb, T* __restrict__ total) {
+  __shared__ T s[1024];
+  // nb <= 1024 * 4
+  T v[4];
+  T tsum = 0;
+  for (int q = 0; q < 4; ++q) {
+    int idx = threadIdx.x * 4 + q;
+    v[q] = idx < nb ? bsum[idx] : (T)0;
+    tsum += v[q];
+  }
+  s[threadIdx.x] = tsum;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    T t = threadIdx.x >= o ? s[threadIdx.x - o] : (T)0;
+    __syncthreads();
+    s[threadIdx.x] += t;
+    __syncthreads();
+  }
+  T run = s[threadIdx.x] - tsum;
+  for (int q = 0; q < 4; ++q) {
+    int idx = threadIdx.x * 4 + q;
+    if (idx < nb) bsum[idx] = run;
+    run += v[q];
+  }
+  if (threadIdx.x == 1023 && total) *total = s[1023];
+}
+
+template <typename T>
+__global__ void k_scan_add(T* __restrict__ out, const T* __restrict__ bsum, int64_t n) {
+  int64_t idx = (int64_t)blockIdx.x * 4096 + threadIdx.x;
+  T add = bsum[blockIdx.x];
+  for (int q = 0; q < 4; ++q, idx += 1024)
+    if (idx < n) out[idx] += add;
+}
+
+// ---------------------------------------------------------------------------
+// neighbour build: one warp per centre atom
+// ---------------------------------------------------------------------------
+struct NbrArgs {
+  const double* x;
+  const float4* xhi;
+  const float4* xlo;
+  const int32_t* mol;
+  const int32_t* elem;
+  const tm_grid* grid;
+  const int32_t* cell_of;
+  const int32_t* cell_start;
+  const int32_t* cell_atoms;
+  int32_t* cnt_r;
+  int32_t* cnt_a;
+  uint32_t* nbr_r;
+  uint32_t* nbr_a;
+  int32_t* need;      // [2] max counts seen (radial, angular)
+  int N, KR, KA;
+  double rr, ra;      // radial / angular cutoffs (FP64, exact test)
+  float rr2_lo, rr2_hi, ra2_lo, ra2_hi;
+  double lat[9];
+};
+
+__device__ __forceinline__ uint64_t nbr_key(int elem, int r, int local) {
+  return ((uint64_t)elem << 37) | ((uint64_t)tm_ref_image_index(r) << 32) | (uint32_t)local;
+}
+__device__ __forceinline__ int ref_to_raster(int ref) {
+  return ref == 0 ? TM_IMG_SELF : (ref <= TM_IMG_SELF ? ref - 1 : ref);
+}
+
+template <bool PERIODIC>
+__global__ void __launch_bounds__(128) k_nbr_build(const NbrArgs a) {
+  extern __shared__ uint64_t sh_keys[];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * (blockDim.x >> 5) + wib;
+  uint64_t* kr = sh_keys + (size_t)wib * (a.KR + a.KA);
+  uint64_t* ka = kr + a.KR;
+  if (i >= a.N) return;
+  const int m = a.mol[i];
+  const tm_grid g = a.grid[m];
+  const float4 hi = a.xhi[i], lo = a.xlo[i];
+  const double xi = a.x[3 * i], yi = a.x[3 * i + 1], zi = a.x[3 * i + 2];
+  const int lc = a.cell_of[i] - g.cell_off;
+  const int iz = lc % g.nz, iy = (lc / g.nz) % g.ny, ix = lc / (g.nz * g.ny);
+  int nr = 0, na = 0;
+  for (int ox = -1; ox <= 1; ++ox) {
+    for (int oy = -1; oy <= 1; ++oy) {
+      for (int oz = -1; oz <= 1; ++oz) {
+        int jx = ix + ox, jy = iy + oy, jz = iz + oz, sx = 0, sy = 0, sz = 0;
+        if (PERIODIC) {
+          if (jx < 0) { jx += g.nx; sx = -1; } else if (jx >= g.nx) { jx -= g.nx; sx = 1; }
+          if (jy < 0) { jy += g.ny; sy = -1; } else if (jy >= g.ny) { jy -= g.ny; sy = 1; }
+          if (jz < 0) { jz += g.nz; sz = -1; } else if (jz >= g.nz) { jz -= g.nz; sz = 1; }
+        } else {
+          if (jx < 0 || jx >= g.nx || jy < 0 || jy >= g.ny || jz < 0 || jz >= g.nz) continue;
+        }
+        const int c = g.cell_off + (jx * g.ny + jy) * g.nz + jz;
+        const int r = 9 * (sx + 1) + 3 * (sy + 1) + (sz + 1);
+        // shift added to the neighbour: s = sx*a0 + sy*a1 + sz*a2
+        double shx = 0, shy = 0, shz = 0;
+        float shx_h = 0, shy_h = 0, shz_h = 0, shx_l = 0, shy_l = 0, shz_l = 0;
+        if (PERIODIC) {
+          shx = sx * a.lat[0] + sy * a.lat[3] + sz * a.lat[6];
+          shy = sx * a.lat[1] + sy * a.lat[4] + sz * a.lat[7];
+          shz = sx * a.lat[2] + sy * a.lat[5] + sz * a.lat[8];
+          shx_h = (float)shx; shy_h = (float)shy; shz_h = (float)shz;
+          shx_l = (float)(shx - shx_h); shy_l = (float)(shy - shy_h); shz_l = (float)(shz - shz_h);
+        }
+        const int t0 = a.cell_start[c], t1 = a.cell_start[c + 1];
+        for (int tb = t0; tb < t1; tb += 32) {
+          const int t = tb + lane;
+          bool in_r = false, in_a = false;
+          uint64_t key = 0;
+          if (t < t1) {
+            const int j = a.cell_atoms[t];
+            if (!(j == i && r == TM_IMG_SELF)) {
+              const float4 hj = a.xhi[j], lj = a.xlo[j];
+              float dx, dy, dz;
+              if (PERIODIC) {
+                dx = ds_sub_shift(hi.x, lo.x, hj.x, lj.x, shx_h, shx_l);
+                dy = ds_sub_shift(hi.y, lo.y, hj.y, lj.y, shy_h, shy_l);
+                dz = ds_sub_shift(hi.z, lo.z, hj.z, lj.z, shz_h, shz_l);
+              } else {
+                dx = ds_sub(hi.x, lo.x, hj.x, lj.x);
+                dy = ds_sub(hi.y, lo.y, hj.y, lj.y);
+                dz = ds_sub(hi.z, lo.z, hj.z, lj.z);
+              }
+              const float d2 = dx * dx + dy * dy + dz * dz;
+              if (d2 <= a.rr2_hi) {
+                double xj = a.x[3 * j], yj = a.x[3 * j + 1], zj = a.x[3 * j + 2];
+                if (PERIODIC) {
+                  xj = tm_image_coord(xj, sx, sy, sz, a.lat[0], a.lat[3], a.lat[6]);
+                  yj = tm_image_coord(yj, sx, sy, sz, a.lat[1], a.lat[4], a.lat[7]);
+                  zj = tm_image_coord(zj, sx, sy, sz, a.lat[2], a.lat[5], a.lat[8]);
+                }
+                in_r = d2 < a.rr2_lo ? true : tm_exact_within(xi, yi, zi, xj, yj, zj, a.rr);
+                if (in_r) in_a = d2 < a.ra2_lo ? true
+                                 : (d2 <= a.ra2_hi ? tm_exact_within(xi, yi, zi, xj, yj, zj, a.ra)
+                                                   : false);
+                key = nbr_key(__float_as_int(hj.w), r, j - g.atom_off);
+              }
+            }
+          }
+          const unsigned mr = __ballot_sync(TM_FULL, in_r);
+          const unsigned ma = __ballot_sync(TM_FULL, in_a);
+          if (in_r) {
+            int p = nr + __popc(mr & lanemask_lt());
+            if (p < a.KR) kr[p] = key;
+          }
+          if (in_a) {
+            int p = na + __popc(ma & lanemask_lt());
+            if (p < a.KA) ka[p] = key;
+          }
+          nr += __popc(mr);
+          na += __popc(ma);
+        }
+      }
+    }
+  }
+  __syncwarp();
+  if (nr > a.KR || na > a.KA) {
+    if (lane == 0) {
+      atomicMax(&a.need[0], nr);
+      atomicMax(&a.need[1], na);
+    }
+  }
+  const int cr = min(nr, a.KR), ca = min(na, a.KA);
+  // rank sort (keys are unique) and write packed entries
+  for (int p = lane; p < cr; p += 32) {
+    const uint64_t kp = kr[p];
+    int rank = 0;
+    for (int q = 0; q < cr; ++q) rank += kr[q] < kp;
+    const int r = ref_to_raster((int)((kp >> 32) & 31));
+    a.nbr_r[(size_t)i * a.KR + rank] = tm_pack((uint32_t)(g.atom_off + (int)(kp & 0xffffffffu)), r);
+  }
+  for (int p = lane; p < ca; p += 32) {
+    const uint64_t kp = ka[p];
+    int rank = 0;
+    for (int q = 0; q < ca; ++q) rank += ka[q] < kp;
+    const int r = ref_to_raster((int)((kp >> 32) & 31));
+    a.nbr_a[(size_t)i * a.KA + rank] = tm_pack((uint32_t)(g.atom_off + (int)(kp & 0xffffffffu)), r);
+  }
+  if (lane == 0) {
+    a.cnt_r[i] = cr;
+    a.cnt_a[i] = ca;
+  }
+}
+
+// Reverse edge index: for entry s of centre i (neighbour j at image r),
+// the position of i (at image 26 - r) in j's list.
+__global__ void k_nbr_reverse(const uint32_t* __restrict__ nbr, const int32_t* __restrict__ cnt,
+                              int32_t* __restrict__ rev, const int32_t* __restrict__ elem,
+                              const int32_t* __restrict__ mol, const int32_t* __restrict__ off,
+                              int N, int K) {
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * (blockDim.x >> 5) + wib;
+  if (i >= N) return;
+  const int ci = cnt[i];
+  const int ei = elem[i];
+  const int li = i - off[mol[i]];
+  for (int s = lane; s < ci; s += 32) {
+    const uint32_t e = nbr[(size_t)i * K + s];
+    const int j = (int)tm_atom(e);
+    const int rj = TM_IMG_SELF * 2 - tm_img(e);
+    const uint64_t want = nbr_key(ei, rj, li);
+    const int cj = cnt[j];
+    const int jo = off[mol[j]];
+    int lo = 0, hi = cj - 1, found = -1;
+    while (lo <= hi) {
+      const int mid = (lo + hi) >> 1;
+      const uint32_t q = nbr[(size_t)j * K + mid];
+      const int qa = (int)tm_atom(q);
+      const uint64_t kq = nbr_key(elem[qa], tm_img(q), qa - jo);
+      if (kq == want) { found = mid; break; }
+      if (kq < want) lo = mid + 1; else hi = mid - 1;
+    }
+    rev[(size_t)i * K + s] = found < 0 ? -1 : j * K + found;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// export in the reference's layout
+// ---------------------------------------------------------------------------
+__global__ void k_export_sizes(const int32_t* __restrict__ cnt_r, const int32_t* __restrict__ cnt_a,
+                               int64_t* __restrict__ pr, int64_t* __restrict__ pt, int N) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  pr[i] = cnt_r[i];
+  const int64_t c = cnt_a[i];
+  pt[i] = c * (c - 1) / 2;
+}
+
+struct ExportArgs {
+  const uint32_t* nbr_r;
+  const uint32_t* nbr_a;
+  const int32_t* cnt_r;
+  const int32_t* cnt_a;
+  const int32_t* elem;
+  const int32_t* mol;
+  const int32_t* off;
+  const int64_t* pr;   // exclusive offsets
+  const int64_t* pt;
+  int64_t* radp;       // [P][4]
+  int64_t* milj;       // [P][4]
+  int64_t* angt;       // [T][5]
+  int64_t* miljk;      // [T][4]
+  int N, KR, KA, nele, nreal_stride;
+  int elepair[TM_MAX_ELE][TM_MAX_ELE];
+};
+
+__device__ __forceinline__ int64_t ref_index(uint32_t e, int jo, int nreal) {
+  return (int64_t)tm_ref_image_index(tm_img(e)) * nreal + ((int)tm_atom(e) - jo);
+}
+
+__global__ void k_export_lists(const ExportArgs a) {
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * (blockDim.x >> 5) + wib;
+  if (i >= a.N) return;
+  const int m = a.mol[i];
+  const int jo = a.off[m];
+  const int li = i - jo;
+  const int nreal = a.nreal_stride > 0 ? a.nreal_stride : (a.off[m + 1] - jo);
+  // radial: segment starts per element
+  const int cr = a.cnt_r[i];
+  int seg[TM_MAX_ELE + 1];
+  for (int e = 0; e < a.nele; ++e) {
+    int c = 0;
+    for (int s = lane; s < cr; s += 32) c += a.elem[tm_atom(a.nbr_r[(size_t)i * a.KR + s])] == e;
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(TM_FULL, c, o);
+    seg[e] = c;
+  }
+  {
+    int acc = 0;
+    for (int e = 0; e < a.nele; ++e) { int c = seg[e]; seg[e] = acc; acc += c; }
+    seg[a.nele] = acc;
+  }
+  if (a.radp || a.milj) {
+    const int64_t base = a.pr[i];
+    for (int s = lane; s < cr; s += 32) {
+      const uint32_t e = a.nbr_r[(size_t)i * a.KR + s];
+      const int l = a.elem[tm_atom(e)];
+      const int64_t row = base + s;
+      if (a.radp) {
+        a.radp[row * 4 + 0] = m; a.radp[row * 4 + 1] = li;
+        a.radp[row * 4 + 2] = ref_index(e, jo, nreal); a.radp[row * 4 + 3] = l;
+      }
+      if (a.milj) {
+        a.milj[row * 4 + 0] = m; a.milj[row * 4 + 1] = li;
+        a.milj[row * 4 + 2] = l; a.milj[row * 4 + 3] = s - seg[l];
+      }
+    }
+  }
+  if (!(a.angt || a.miljk)) return;
+  // angular: element segments of the angular list
+  const int ca = a.cnt_a[i];
+  for (int e = 0; e < a.nele; ++e) {
+    int c = 0;
+    for (int s = lane; s < ca; s += 32) c += a.elem[tm_atom(a.nbr_a[(size_t)i * a.KA + s])] == e;
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(TM_FULL, c, o);
+    seg[e] = c;
+  }
+  {
+    int acc = 0;
+    for (int e = 0; e < a.nele; ++e) { int c = seg[e]; seg[e] = acc; acc += c; }
+    seg[a.nele] = acc;
+  }
+  int64_t row0 = a.pt[i];
+  for (int ea = 0; ea < a.nele; ++ea) {
+    for (int eb = ea; eb < a.nele; ++eb) {
+      const int na_ = seg[ea + 1] - seg[ea], nb_ = seg[eb + 1] - seg[eb];
+      const int64_t npair = ea < eb ? (int64_t)na_ * nb_ : (int64_t)na_ * (na_ - 1) / 2;
+      const int l = a.elepair[ea][eb];
+      for (int64_t t = lane; t < npair; t += 32) {
+        int pa, pb;
+        if (ea < eb) {
+          pb = (int)(t / na_);
+          pa = (int)(t % na_);
+        } else {
+          // t = b(b-1)/2 + a with 0 <= a < b
+          int b = (int)((1.0 + sqrt(1.0 + 8.0 * (double)t)) * 0.5);
+          while ((int64_t)b * (b - 1) / 2 > t) --b;
+          while ((int64_t)(b + 1) * b / 2 <= t) ++b;
+          pb = b;
+          pa = (int)(t - (int64_t)b * (b - 1) / 2);
+        }
+        const uint32_t ej = a.nbr_a[(size_t)i * a.KA + seg[ea] + pa];
+        const uint32_t ek = a.nbr_a[(size_t)i * a.KA + seg[eb] + pb];
+        const int64_t row = row0 + t;
+        if (a.angt) {
+          a.angt[row * 5 + 0] = m; a.angt[row * 5 + 1] = li;
+          a.angt[row * 5 + 2] = ref_index(ej, jo, nreal);
+          a.angt[row * 5 + 3] = ref_index(ek, jo, nreal);
+          a.angt[row * 5 + 4] = l;
+        }
+        if (a.miljk) {
+          a.miljk[row * 4 + 0] = m; a.miljk[row * 4 + 1] = li;
+          a.miljk[row * 4 + 2] = l; a.miljk[row * 4 + 3] = t;
+        }
+      }
+      row0 += npair;
+    }
+  }
+}
+
+// Coulomb pair list (materialised only for export / the plain path).
+struct EEArgs {
+  const double* x;
+  const float4* xhi;
+  const float4* xlo;
+  const int32_t* mol;
+  const tm_grid* grid;
+  const int32_t* cell_of;
+  const int32_t* cell_start;
+  const int32_t* cell_atoms;
+  const int64_t* offs;    // fill pass: exclusive offsets per centre
+  int64_t* count;         // count pass: per centre
+  int64_t* out;           // [Pee][3]
+  int N;
+  double ree;
+  float ree2_lo, ree2_hi;
+  double lat[9];
+  int periodic;
+};
+
+template <bool FILL>
+__global__ void __launch_bounds__(128) k_ee_pairs(const EEArgs a) {
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * (blockDim.x >> 5) + wib;
+  if (i >= a.N) return;
+  const int m = a.mol[i];
+  const tm_grid g = a.grid[m];
+  const float4 hi = a.xhi[i], lo = a.xlo[i];
+  const double xi = a.x[3 * i], yi = a.x[3 * i + 1], zi = a.x[3 * i + 2];
+  const int lc = a.cell_of[i] - g.cell_off;
+  const int iz = lc % g.nz, iy = (lc / g.nz) % g.ny, ix = lc / (g.nz * g.ny);
+  const int Rx = (int)ceil(a.ree / g.cx), Ry = (int)ceil(a.ree / g.cy), Rz = (int)ceil(a.ree / g.cz);
+  const int nreal = g.natom;
+  int64_t n = 0;
+  int64_t base = FILL ? a.offs[i] : 0;
+  for (int ox = -Rx; ox <= Rx; ++ox) {
+    for (int oy = -Ry; oy <= Ry; ++oy) {
+      for (int oz = -Rz; oz <= Rz; ++oz) {
+        int jx = ix + ox, jy = iy + oy, jz = iz + oz, sx = 0, sy = 0, sz = 0;
+        if (a.periodic) {
+          if (jx < 0) { jx += g.nx; sx = -1; } else if (jx >= g.nx) { jx -= g.nx; sx = 1; }
+          if (jy < 0) { jy += g.ny; sy = -1; } else if (jy >= g.ny) { jy -= g.ny; sy = 1; }
+          if (jz < 0) { jz += g.nz; sz = -1; } else if (jz >= g.nz) { jz -= g.nz; sz = 1; }
+        } else if (jx < 0 || jx >= g.nx || jy < 0 || jy >= g.ny || jz < 0 || jz >= g.nz) {
+          continue;
+        }
+        const int c = g.cell_off + (jx * g.ny + jy) * g.nz + jz;
+        const int r = 9 * (sx + 1) + 3 * (sy + 1) + (sz + 1);
+        double shx = 0, shy = 0, shz = 0;
+        if (a.periodic) {
+          shx = sx * a.lat[0] + sy * a.lat[3] + sz * a.lat[6];
+          shy = sx * a.lat[1] + sy * a.lat[4] + sz * a.lat[7];
+          shz = sx * a.lat[2] + sy * a.lat[5] + sz * a.lat[8];
+        }
+        const float shx_h = (float)shx, shy_h = (float)shy, shz_h = (float)shz;
+        const float shx_l = (float)(shx - shx_h), shy_l = (float)(shy - shy_h), shz_l = (float)(shz - shz_h);
+        const int t0 = a.cell_start[c], t1 = a.cell_start[c + 1];
+        for (int tb = t0; tb < t1; tb += 32) {
+          const int t = tb + lane;
+          bool ok = false;
+          int j = 0;
+          if (t < t1) {
+            j = a.cell_atoms[t];
+            // open: i < j only (DoPerms = 0); periodic: every other atom/image
+            const bool cand = a.periodic ? !(j == i && r == TM_IMG_SELF) : (j > i);
+            if (cand) {
+              const float4 hj = a.xhi[j], lj = a.xlo[j];
+              const float dx = ds_sub_shift(hi.x, lo.x, hj.x, lj.x, shx_h, shx_l);
+              const float dy = ds_sub_shift(hi.y, lo.y, hj.y, lj.y, shy_h, shy_l);
+              const float dz = ds_sub_shift(hi.z, lo.z, hj.z, lj.z, shz_h, shz_l);
+              const float d2 = dx * dx + dy * dy + dz * dz;
+              if (d2 < a.ree2_lo) ok = true;
+              else if (d2 <= a.ree2_hi) {
+                double xj = a.x[3 * j], yj = a.x[3 * j + 1], zj = a.x[3 * j + 2];
+                if (a.periodic) {
+                  xj = tm_image_coord(xj, sx, sy, sz, a.lat[0], a.lat[3], a.lat[6]);
+                  yj = tm_image_coord(yj, sx, sy, sz, a.lat[1], a.lat[4], a.lat[7]);
+                  zj = tm_image_coord(zj, sx, sy, sz, a.lat[2], a.lat[5], a.lat[8]);
+                }
+                ok = tm_exact_within(xi, yi, zi, xj, yj, zj, a.ree);
+              }
+            }
+          }
+          const unsigned mk = __ballot_sync(TM_FULL, ok);
+          if (FILL && ok) {
+            const int64_t row = base + n + __popc(mk & lanemask_lt());
+            a.out[row * 3 + 0] = m;
+            a.out[row * 3 + 1] = i - g.atom_off;
+            a.out[row * 3 + 2] = (int64_t)tm_ref_image_index(r) * nreal + (j - g.atom_off);
+          }
+          n += __popc(mk);
+        }
+      }
+    }
+  }
+  if (!FILL && lane == 0) a.count[i] = n;
+}
+
+template <typename T>
+int scan_exclusive(tm_ctx* ctx, const T* in, T* out, int64_t n, T* total_dev) {
+  const int64_t nb = (n + 4095) / 4096;
+  if (nb > 4096) return tm_fail(ctx, TM_E_ARG, "scan too large");
+  T* bsum = nullptr;
+  if (tm_alloc(ctx, (void**)&bsum, sizeof(T) * (size_t)(nb > 0 ? nb : 1))) return TM_E_CUDA;
+  if (n > 0) {
+    k_scan_blocks<T><<<(unsigned)nb, 1024, 0, ctx->stream>>>(in, out, bsum, n);
+    k_scan_top<T><<<1, 1024, 0, ctx->stream>>>(bsum, (int)nb, total_dev);
+    k_scan_add<T><<<(unsigned)nb, 1024, 0, ctx->stream>>>(out, bsum, n);
+    ctx->launches += 3;
+  }
+  int rc = tm_cuda_check(ctx, cudaGetLastError(), "scan");
+  tm_free(ctx, bsum, sizeof(T) * (size_t)(nb > 0 ? nb : 1));
+  return rc;
+}
+
+NbrArgs make_nbr_args(tm_system* s, int32_t* need) {
+  const tm_consts& k = s->model->k;
+  NbrArgs a;
+  a.x = s->d_x; a.xhi = s->d_xhi; a.xlo = s->d_xlo; a.mol = s->d_mol; a.elem = s->d_elem;
+  a.grid = s->d_grid; a.cell_of = s->d_cell_of_atom; a.cell_start = s->d_cell_start;
+  a.cell_atoms = s->d_cell_atoms; a.cnt_r = s->d_cnt_r; a.cnt_a = s->d_cnt_a;
+  a.nbr_r = s->d_nbr_r; a.nbr_a = s->d_nbr_a; a.need = need;
+  a.N = s->N; a.KR = s->KR; a.KA = s->KA;
+  a.rr = k.r_rc_d; a.ra = k.a_rc_d;
+  a.rr2_lo = (float)(k.r_rc_d * k.r_rc_d) * (1.f - kBand);
+  a.rr2_hi = (float)(k.r_rc_d * k.r_rc_d) * (1.f + kBand);
+  a.ra2_lo = (float)(k.a_rc_d * k.a_rc_d) * (1.f - kBand);
+  a.ra2_hi = (float)(k.a_rc_d * k.a_rc_d) * (1.f + kBand);
+  for (int q = 0; q < 9; ++q) a.lat[q] = s->lat[q];
+  return a;
+}
+
+}  // namespace
+
+int tm_launch_positions(tm_system* s) {
+  tm_ctx* ctx = s->ctx;
+  k_positions<<<tm_div_up(s->N, 256), 256, 0, ctx->stream>>>(s->d_x, s->d_elem, s->d_xhi, s->d_xlo,
+                                                             s->N, ctx->d_status);
+  ctx->launches++;
+  return tm_cuda_check(ctx, cudaGetLastError(), "positions");
+}
+
+// Bins atoms and builds both neighbour lists on the ctx stream without any
+// host synchronisation. A centre with more neighbours than its row capacity
+// records the count it needed in s->d_need; tm_nlist_grow() checks that after
+// the caller's own sync point and enlarges the rows so the call can be redone.
+int tm_launch_nlist(tm_system* s) {
+  tm_ctx* ctx = s->ctx;
+  cudaStream_t st = ctx->stream;
+  const tm_consts& k = s->model->k;
+  int rc;
+  if ((rc = tm_launch_positions(s))) return rc;
+  k_grid_setup<<<s->nmol, 256, 0, st>>>(s->d_x, s->d_off, s->d_grid, s->d_ncell_m, k.r_rc_d,
+                                          s->periodic ? 1 : 0, s->lat[0], s->lat[4], s->lat[8]);
+  k_grid_offsets<<<1, 32, 0, st>>>(s->d_grid, s->d_ncell_m, s->nmol, s->d_ncell, s->ncell_cap,
+                                   ctx->d_status);
+  ctx->launches += 2;
+  cudaMemsetAsync(s->d_cell_cnt, 0, sizeof(int32_t) * (s->ncell_cap + 1), st);
+  k_cell_count<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_x, s->d_mol, s->d_grid, s->d_cell_cnt,
+                                                      s->d_cell_of_atom, s->N, s->ncell_cap,
+                                                      ctx->d_status);
+  ctx->launches++;
+  if ((rc = scan_exclusive<int32_t>(ctx, s->d_cell_cnt, s->d_cell_start, s->ncell_cap + 1,
+                                    nullptr)))
+    return rc;
+  cudaMemsetAsync(s->d_cell_cnt, 0, sizeof(int32_t) * (s->ncell_cap + 1), st);
+  k_cell_fill<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_cell_of_atom, s->d_cell_start,
+                                                     s->d_cell_cnt, s->d_cell_atoms, s->N);
+  k_cell_sort<<<tm_div_up(s->ncell_cap, 128), 128, 0, st>>>(s->d_cell_start, s->d_cell_atoms,
+                                                             s->d_ncell, s->ncell_cap);
+  ctx->launches += 2;
+  cudaMemsetAsync(s->d_need, 0, sizeof(int32_t) * 2, st);
+  NbrArgs a = make_nbr_args(s, s->d_need);
+  const size_t shm = (size_t)4 * (s->KR + s->KA) * sizeof(uint64_t);
+  if (shm > 48 * 1024) {
+    cudaFuncSetAttribute(k_nbr_build<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+    cudaFuncSetAttribute(k_nbr_build<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  }
+  if (s->periodic)
+    k_nbr_build<true><<<tm_div_up(s->N, 4), 128, shm, st>>>(a);
+  else
+    k_nbr_build<false><<<tm_div_up(s->N, 4), 128, shm, st>>>(a);
+  k_nbr_reverse<<<tm_div_up(s->N, 4), 128, 0, st>>>(s->d_nbr_r, s->d_cnt_r, s->d_rev_r, s->d_elem,
+                                                    s->d_mol, s->d_off, s->N, s->KR);
+  k_nbr_reverse<<<tm_div_up(s->N, 4), 128, 0, st>>>(s->d_nbr_a, s->d_cnt_a, s->d_rev_a, s->d_elem,
+                                                    s->d_mol, s->d_off, s->N, s->KA);
+  ctx->launches += 3;
+  cudaMemcpyAsync(s->d_x_at_build, s->d_x, sizeof(double) * 3 * s->N, cudaMemcpyDeviceToDevice, st);
+  s->nlist_valid = true;
+  return tm_cuda_check(ctx, cudaGetLastError(), "nlist");
+}
+
+// After a stream sync: if the last build overflowed a row, enlarge the rows
+// (to the next multiple of 32 above what was needed) and report it.
+int tm_nlist_grow(tm_system* s, bool* grew) {
+  tm_ctx* ctx = s->ctx;
+  *grew = false;
+  int32_t h_need[2] = {0, 0};
+  int rc;
+  if ((rc = tm_cuda_check(ctx, cudaMemcpyAsync(h_need, s->d_need, sizeof(h_need), cudaMemcpyDeviceToHost, ctx->stream), "need")) ||
+      (rc = tm_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "need")))
+    return rc;
+  if (h_need[0] <= s->KR && h_need[1] <= s->KA) return TM_OK;
+  const int KR = h_need[0] > s->KR ? ((h_need[0] + 31) / 32) * 32 : s->KR;
+  const int KA = h_need[1] > s->KA ? ((h_need[1] + 31) / 32) * 32 : s->KA;
+  tm_free(ctx, s->d_nbr_r, sizeof(uint32_t) * (size_t)s->N * s->KR);
+  tm_free(ctx, s->d_rev_r, sizeof(int32_t) * (size_t)s->N * s->KR);
+  tm_free(ctx, s->d_sr, sizeof(float) * (size_t)s->N * s->KR);
+  tm_free(ctx, s->d_nbr_a, sizeof(uint32_t) * (size_t)s->N * s->KA);
+  tm_free(ctx, s->d_rev_a, sizeof(int32_t) * (size_t)s->N * s->KA);
+  tm_free(ctx, s->d_va, sizeof(float4) * (size_t)s->N * s->KA);
+  s->bytes -= (sizeof(uint32_t) + sizeof(int32_t) + sizeof(float)) * (size_t)s->N * s->KR +
+              (sizeof(uint32_t) + sizeof(int32_t) + sizeof(float4)) * (size_t)s->N * s->KA;
+  s->KR = KR;
+  s->KA = KA;
+  if ((rc = tm_alloc(ctx, (void**)&s->d_nbr_r, sizeof(uint32_t) * (size_t)s->N * KR)) ||
+      (rc = tm_alloc(ctx, (void**)&s->d_rev_r, sizeof(int32_t) * (size_t)s->N * KR)) ||
+      (rc = tm_alloc(ctx, (void**)&s->d_sr, sizeof(float) * (size_t)s->N * KR)) ||
+      (rc = tm_alloc(ctx, (void**)&s->d_nbr_a, sizeof(uint32_t) * (size_t)s->N * KA)) ||
+      (rc = tm_alloc(ctx, (void**)&s->d_rev_a, sizeof(int32_t) * (size_t)s->N * KA)) ||
+      (rc = tm_alloc(ctx, (void**)&s->d_va, sizeof(float4) * (size_t)s->N * KA)))
+    return rc;
+  s->bytes += (sizeof(uint32_t) + sizeof(int32_t) + sizeof(float)) * (size_t)s->N * KR +
+              (sizeof(uint32_t) + sizeof(int32_t) + sizeof(float4)) * (size_t)s->N * KA;
+  s->nlist_valid = false;
+  *grew = true;
+  return TM_OK;
+}
+
+int tm_count_nlist(tm_system* s, int64_t counts[4]) {
+  tm_ctx* ctx = s->ctx;
+  std::vector<int32_t> cr(s->N), ca(s->N);
+  int rc;
+  if ((rc = tm_cuda_check(ctx, cudaMemcpyAsync(cr.data(), s->d_cnt_r, sizeof(int32_t) * s->N, cudaMemcpyDeviceToHost, ctx->stream), "cnt")) ||
+      (rc = tm_cuda_check(ctx, cudaMemcpyAsync(ca.data(), s->d_cnt_a, sizeof(int32_t) * s->N, cudaMemcpyDeviceToHost, ctx->stream), "cnt")) ||
+      (rc = tm_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "cnt")))
+    return rc;
+  int64_t P = 0, T = 0, mx = 0;
+  for (int i = 0; i < s->N; ++i) {
+    P += cr[i];
+    T += (int64_t)ca[i] * (ca[i] - 1) / 2;
+    mx = cr[i] > mx ? cr[i] : mx;
+  }
+  int64_t ee = 0;
+  if ((rc = tm_count_ee(s, &ee))) return rc;
+  counts[0] = P; counts[1] = T; counts[2] = ee; counts[3] = mx;
+  return TM_OK;
+}
+
+int tm_launch_export_nlist(tm_system* s, int64_t* radp, int64_t* angt, int64_t* mil_j,
+                           int64_t* mil_jk, int64_t P, int64_t T) {
+  tm_ctx* ctx = s->ctx;
+  cudaStream_t st = ctx->stream;
+  int rc;
+  int64_t *pr = nullptr, *pt = nullptr, *sr = nullptr, *stt = nullptr;
+  const size_t nb = sizeof(int64_t) * (size_t)(s->N + 1);
+  if ((rc = tm_alloc(ctx, (void**)&pr, nb)) || (rc = tm_alloc(ctx, (void**)&pt, nb)) ||
+      (rc = tm_alloc(ctx, (void**)&sr, nb)) || (rc = tm_alloc(ctx, (void**)&stt, nb)))
+    return rc;
+  k_export_sizes<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_cnt_r, s->d_cnt_a, sr, stt, s->N);
+  ctx->launches++;
+  if ((rc = scan_exclusive<int64_t>(ctx, sr, pr, s->N, nullptr)) ||
+      (rc = scan_exclusive<int64_t>(ctx, stt, pt, s->N, nullptr)))
+    return rc;
+  ExportArgs a;
+  a.nbr_r = s->d_nbr_r; a.nbr_a = s->d_nbr_a; a.cnt_r = s->d_cnt_r; a.cnt_a = s->d_cnt_a;
+  a.elem = s->d_elem; a.mol = s->d_mol; a.off = s->d_off; a.pr = pr; a.pt = pt;
+  a.radp = radp; a.milj = mil_j; a.angt = angt; a.miljk = mil_jk;
+  a.N = s->N; a.KR = s->KR; a.KA = s->KA; a.nele = s->model->k.nele;
+  a.nreal_stride = 0;
+  for (int p = 0; p < TM_MAX_ELE; ++p)
+    for (int q = 0; q < TM_MAX_ELE; ++q) a.elepair[p][q] = s->model->k.elepair[p][q];
+  k_export_lists<<<tm_div_up(s->N, 4), 128, 0, st>>>(a);
+  ctx->launches++;
+  rc = tm_cuda_check(ctx, cudaStreamSynchronize(st), "export");
+  tm_free(ctx, pr, nb); tm_free(ctx, pt, nb); tm_free(ctx, sr, nb); tm_free(ctx, stt, nb);
+  (void)P; (void)T;
+  return rc;
+}
+
+static EEArgs make_ee_args(tm_system* s) {
+  const tm_consts& k = s->model->k;
+  EEArgs a;
+  a.x = s->d_x; a.xhi = s->d_xhi; a.xlo = s->d_xlo; a.mol = s->d_mol; a.grid = s->d_grid;
+  a.cell_of = s->d_cell_of_atom; a.cell_start = s->d_cell_start; a.cell_atoms = s->d_cell_atoms;
+  a.offs = nullptr; a.count = nullptr; a.out = nullptr; a.N = s->N; a.ree = k.ree_d;
+  a.ree2_lo = (float)(k.ree_d * k.ree_d) * (1.f - kBand);
+  a.ree2_hi = (float)(k.ree_d * k.ree_d) * (1.f + kBand);
+  for (int q = 0; q < 9; ++q) a.lat[q] = s->lat[q];
+  a.periodic = s->periodic ? 1 : 0;
+  return a;
+}
+
+int tm_count_ee(tm_system* s, int64_t* npairs) {
+  tm_ctx* ctx = s->ctx;
+  int rc;
+  int64_t *cnt = nullptr, *offs = nullptr, *tot = nullptr;
+  const size_t nb = sizeof(int64_t) * (size_t)(s->N + 1);
+  if ((rc = tm_alloc(ctx, (void**)&cnt, nb)) || (rc = tm_alloc(ctx, (void**)&offs, nb)) ||
+      (rc = tm_alloc(ctx, (void**)&tot, sizeof(int64_t))))
+    return rc;
+  EEArgs a = make_ee_args(s);
+  a.count = cnt;
+  k_ee_pairs<false><<<tm_div_up(s->N, 4), 128, 0, ctx->stream>>>(a);
+  ctx->launches++;
+  if ((rc = scan_exclusive<int64_t>(ctx, cnt, offs, s->N, tot))) return rc;
+  int64_t h = 0;
+  if ((rc = tm_cuda_check(ctx, cudaMemcpyAsync(&h, tot, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream), "ee")) ||
+      (rc = tm_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "ee")))
+    return rc;
+  *npairs = h;
+  tm_free(ctx, cnt, nb); tm_free(ctx, offs, nb); tm_free(ctx, tot, sizeof(int64_t));
+  return TM_OK;
+}
+
+int tm_launch_export_ee(tm_system* s, int64_t* eep, int64_t cap) {
+  tm_ctx* ctx = s->ctx;
+  int rc;
+  int64_t *cnt = nullptr, *offs = nullptr, *tot = nullptr;
+  const size_t nb = sizeof(int64_t) * (size_t)(s->N + 1);
+  if ((rc = tm_alloc(ctx, (void**)&cnt, nb)) || (rc = tm_alloc(ctx, (void**)&offs, nb)) ||
+      (rc = tm_alloc(ctx, (void**)&tot, sizeof(int64_t))))
+    return rc;
+  EEArgs a = make_ee_args(s);
+  a.count = cnt;
+  k_ee_pairs<false><<<tm_div_up(s->N, 4), 128, 0, ctx->stream>>>(a);
+  ctx->launches++;
+  if ((rc = scan_exclusive<int64_t>(ctx, cnt, offs, s->N, tot))) return rc;
+  int64_t h = 0;
+  if ((rc = tm_cuda_check(ctx, cudaMemcpyAsync(&h, tot, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream), "ee")) ||
+      (rc = tm_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "ee")))
+    return rc;
+  if (h > cap) {
+    tm_free(ctx, cnt, nb); tm_free(ctx, offs, nb); tm_free(ctx, tot, sizeof(int64_t));
+    return tm_fail(ctx, TM_E_CAPACITY, "ee export buffer too small");
+  }
+  a.offs = offs;
+  a.out = eep;
+  k_ee_pairs<true><<<tm_div_up(s->N, 4), 128, 0, ctx->stream>>>(a);
+  ctx->launches++;
+  rc = tm_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "ee fill");
+  tm_free(ctx, cnt, nb); tm_free(ctx, offs, nb); tm_free(ctx, tot, sizeof(int64_t));
+  return rc;
+}

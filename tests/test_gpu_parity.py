@@ -1,0 +1,180 @@
+"""GPU parity of the CUDA path (through the C ABI) against the oracle.
+
+Tolerances (FP32 path vs the FP64 oracle): energies 1e-5 eV/atom, forces
+1e-4 eV/A max-abs; neighbour sets bit-exact. The BF16 path's error is
+measured and stated, not asserted against those bounds.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import reference as orc
+from tensormol_gb300 import systems
+from tensormol_gb300.params import EV_PER_HARTREE, JOULEPERHARTREE, PARAMS, descriptor_width
+
+pytestmark = pytest.mark.gpu
+
+E_TOL = 1e-5   # eV / atom
+F_TOL = 1e-4   # eV / A
+
+
+def _params(act="relu", **kw):
+    p = dict(PARAMS)
+    p["NeuronType"] = act
+    p.update(kw)
+    return p
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from tensormol_gb300 import model
+    return model
+
+
+def _model(gpu, eles, act="relu", prec="fp32", seed=7, **kw):
+    p = _params(act, **kw)
+    W = systems.random_weights(eles, descriptor_width(len(eles)), seed=seed)
+    return gpu.BPEEModel(eles, W, params=p, precision=prec), orc.Model(eles, W, params=p)
+
+
+def _errors(out, ref, natoms_per_mol):
+    dE = np.max(np.abs(out["Etotal"] - ref["Etotal"]) * EV_PER_HARTREE / natoms_per_mol)
+    dF = np.abs(out["force"] - ref["force"]).max() / JOULEPERHARTREE * EV_PER_HARTREE
+    return dE, dF
+
+
+# ---------------------------------------------------------------------------
+def test_tensor_core_gemm_selftest(gpu):
+    rng = np.random.default_rng(0)
+    M, N, K = 256, 512, 512
+    A = rng.normal(size=(M, K)).astype(np.float32)
+    B = rng.normal(size=(N, K)).astype(np.float32) * 0.05
+    ref = A.astype(np.float64) @ B.astype(np.float64).T
+    ctx = gpu.default_context()
+    for prec, tol in ((0, 2e-5), (1, 2e-2)):
+        C = np.zeros((M, N), np.float32)
+        ctx.check(ctx.lib.tm_selftest_gemm(ctx.h, prec, M, N, K, A.ctypes.data, B.ctypes.data,
+                                           C.ctypes.data))
+        err = np.abs(C - ref).max() / np.abs(ref).max()
+        assert err < tol, (prec, err)
+
+
+@pytest.mark.parametrize("name,eles", [("water60", [1, 8]), ("chno6", [1, 6, 7, 8])])
+def test_nlist_bit_exact_vs_reference(gpu, golden_loader, name, eles):
+    g = golden_loader(name)
+    m, _ = _model(gpu, eles)
+    s = m.system(g["x"], g["Z"], g["offsets"])
+    s.build_nlist()
+    radp, angt, milj, miljk = s.export_nlist()
+    assert np.array_equal(radp, g["RadpEle"].astype(np.int64))
+    assert np.array_equal(angt, g["AngtEle"].astype(np.int64))
+    assert np.array_equal(milj, g["mil_j"].astype(np.int64))
+    assert np.array_equal(miljk, g["mil_jk"].astype(np.int64))
+    ee = s.export_ee()
+    ref = g["rad_eep"].astype(np.int64)
+    key = lambda a: a[np.lexsort((a[:, 2], a[:, 1], a[:, 0]))]
+    assert np.array_equal(key(ee), key(ref))
+
+
+def test_nlist_bit_exact_water3000(gpu):
+    w = systems.water(1000, seed=11)
+    m, _ = _model(gpu, [1, 8])
+    s = m.system(w.x, w.Z, w.offsets)
+    s.build_nlist()
+    radp, angt, milj, miljk = s.export_nlist()
+    P, T, mj, mjk = orc.pairs_and_triples([(w.x, w.Z)], [1, 8])
+    assert np.array_equal(radp, P) and np.array_equal(angt, T)
+    assert np.array_equal(milj, mj) and np.array_equal(miljk, mjk)
+    ee = s.export_ee()
+    ref = orc.ee_pairs([(w.x, w.Z)], 15.0)
+    key = lambda a: a[np.lexsort((a[:, 2], a[:, 1], a[:, 0]))]
+    assert np.array_equal(key(ee), key(ref))
+
+
+def test_nlist_periodic_bit_exact(gpu):
+    L = 49.7 / 2.0
+    b = systems.water(512, seed=5, spacing=L / 8.0, box=L, n_side=8)
+    lat = np.eye(3) * L
+    x = orc.modulo_lattice(b.x, lat)
+    m, _ = _model(gpu, [1, 8], EECutoffOff=9.0)
+    s = m.system(x, b.Z, None, lat)
+    s.build_nlist()
+    radp, angt, milj, miljk = s.export_nlist()
+    xt = orc.tessellate(x, lat)
+    Zt = np.tile(b.Z, 27)
+    P, T, mj, mjk = orc.pairs_and_triples([(xt, Zt)], [1, 8], nreal=[len(b.Z)])
+    assert np.array_equal(radp, P) and np.array_equal(angt, T)
+    assert np.array_equal(milj, mj) and np.array_equal(miljk, mjk)
+    ee = s.export_ee()
+    ref = orc.ee_pairs([(xt, Zt)], 9.0, nreal=[len(b.Z)], doperms=True)
+    key = lambda a: a[np.lexsort((a[:, 2], a[:, 1], a[:, 0]))]
+    assert np.array_equal(key(ee), key(ref))
+
+
+def test_descriptors_match_oracle(gpu, golden_loader):
+    for name, eles in (("water60", [1, 8]), ("chno6", [1, 6, 7, 8])):
+        g = golden_loader(name)
+        m, om = _model(gpu, eles)
+        s = m.system(g["x"], g["Z"], g["offsets"])
+        G = s.descriptors()
+        ref = orc.OpenSystemOracle(om, g["x"], g["Z"], g["offsets"]).terms(g["x"], grad=False)["G"]
+        err = np.abs(G - ref).max() / max(1.0, np.abs(ref).max())
+        assert err < 2e-5, (name, err)
+
+
+@pytest.mark.parametrize("act", ["relu", "sigmoid_with_param"])
+def test_energy_force_water60(gpu, act):
+    w = systems.water_cluster_60(seed=0)
+    m, om = _model(gpu, [1, 8], act)
+    s = m.system(w.x, w.Z, w.offsets)
+    out = s.energy_force(w.x, True, charges=True)
+    ref = orc.OpenSystemOracle(om, w.x, w.Z, w.offsets).terms(w.x)
+    dE, dF = _errors(out, ref, w.natoms)
+    assert dE < E_TOL and dF < F_TOL, (dE, dF)
+    np.testing.assert_allclose(out["Ecc"], ref["Ecc"], rtol=1e-4, atol=1e-9)
+    np.testing.assert_allclose(out["Evdw"], ref["Evdw"], rtol=1e-5, atol=1e-12)
+    np.testing.assert_allclose(out["charge"], ref["charge"], rtol=0, atol=2e-6)
+    np.testing.assert_allclose(out["Ebp_atom"], ref["Ebp_atom"], rtol=0, atol=2e-6)
+
+
+def test_energy_force_chno_batch(gpu):
+    b = systems.chno_batch(nmol=24, seed=3)
+    m, om = _model(gpu, [1, 6, 7, 8], "sigmoid_with_param")
+    s = m.system(b.x, b.Z, b.offsets)
+    out = s.energy_force(b.x, True)
+    ref = orc.OpenSystemOracle(om, b.x, b.Z, b.offsets).terms(b.x)
+    n_per = np.diff(b.offsets)
+    dE = np.max(np.abs(out["Etotal"] - ref["Etotal"]) * EV_PER_HARTREE / n_per)
+    dF = np.abs(out["force"] - ref["force"]).max() / JOULEPERHARTREE * EV_PER_HARTREE
+    assert dE < E_TOL and dF < F_TOL, (dE, dF)
+
+
+def test_energy_force_periodic(gpu):
+    L = 49.7 / 2.0
+    b = systems.water(512, seed=5, spacing=L / 8.0, box=L, n_side=8)
+    lat = np.eye(3) * L
+    x = orc.modulo_lattice(b.x, lat)
+    m, om = _model(gpu, [1, 8], "sigmoid_with_param", EECutoffOff=9.0)
+    s = m.system(x, b.Z, None, lat)
+    out = s.energy_force(x, True)
+    ref = orc.PeriodicOracle(om, x, b.Z, lat, ree_cut=9.0).terms(x)
+    dE, dF = _errors(out, ref, len(b.Z))
+    assert dE < E_TOL and dF < F_TOL, (dE, dF)
+    out_r = s.energy_force(x, True, reference_periodic_force=True)
+    dFr = np.abs(out_r["force"] - ref["force_ref"]).max() / JOULEPERHARTREE * EV_PER_HARTREE
+    assert dFr < F_TOL, dFr
+
+
+def test_bf16_error_is_reported(gpu):
+    w = systems.water_cluster_60(seed=0)
+    m, om = _model(gpu, [1, 8], "sigmoid_with_param", prec="bf16")
+    s = m.system(w.x, w.Z, w.offsets)
+    out = s.energy_force(w.x, True)
+    ref = orc.OpenSystemOracle(om, w.x, w.Z, w.offsets).terms(w.x)
+    dE, dF = _errors(out, ref, w.natoms)
+    print(f"BF16 water60: dE/atom={dE:.2e} eV  max|dF|={dF:.2e} eV/A")
+    assert np.isfinite(dE) and np.isfinite(dF) and dE < 1e-2 and dF < 1.0
