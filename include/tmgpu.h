@@ -204,6 +204,13 @@ int tm_selftest_gemm(tm_ctx *ctx, int precision, int M, int N, int K, const floa
  * TFSymSet_Scattered_Linear_WithEle_Release's SymList (RawSymFunc.py:2267-2309).
  */
 int tm_system_descriptors(tm_system *s, float *G_out);
+/*
+ * One energy(+force) evaluation of the resident positions with CUDA events on
+ * the ctx stream between stages; stage_ms[7] = (lists, descriptors, network
+ * forward, network backward, pair terms, adjoint + force gather, total) in ms.
+ * No counterpart in the reference (its TFMolManage timing is wall-clock).
+ */
+int tm_energy_force_profile(tm_system *s, unsigned flags, float *stage_ms);
 
 #ifdef __cplusplus
 }

@@ -239,7 +239,7 @@ class Model:
         fac1 = torch.exp(-self.p["AN1_eta"] * t * t)
         fac2 = 0.5 * (torch.cos(_PI_TF * r / self.p["AN1_r_Rc"]) + 1.0)
         g = fac1 * fac2[:, None]
-        out = torch.zeros(nrow * nele, nr, dtype=torch.float64)
+        out = torch.zeros(nrow * nele, nr, dtype=X.dtype)
         out = out.index_add(0, pi * nele + pl, g)
         return out.reshape(nrow, nele * nr)
 
@@ -264,12 +264,12 @@ class Model:
         fac3 = 0.5 * (torch.cos(_PI_TF * rij / rc) + 1.0)
         fac4 = 0.5 * (torch.cos(_PI_TF * rik / rc) + 1.0)
         g = fac1[:, :, None] * fac2[:, None, :] * (fac3 * fac4)[:, None, None]
-        out = torch.zeros(nrow * nelep, nt * na, dtype=torch.float64)
+        out = torch.zeros(nrow * nelep, nt * na, dtype=X.dtype)
         out = out.index_add(0, ti * nelep + tl, g.reshape(-1, nt * na))
         return out.reshape(nrow, nelep * nt * na)
 
     def mlp(self, net, G, Zc):
-        out = torch.zeros(G.shape[0], dtype=torch.float64)
+        out = torch.zeros(G.shape[0], dtype=G.dtype)
         for e in self.eles:
             idx = torch.nonzero(Zc == e).flatten()
             if idx.numel() == 0:
@@ -325,18 +325,19 @@ class Model:
         Ea = self.mlp("E", G, Zc)
         qa = self.mlp("Q", G, Zc)
         mol = mol_of_row[:nrow]
-        net = torch.zeros(nmol, dtype=torch.float64).index_add(0, mol, qa)
+        dt = Xall.dtype
+        net = torch.zeros(nmol, dtype=dt).index_add(0, mol, qa)
         qs = qa - (net / natom_of_mol)[mol]       # TFBehlerParinelloSymEE.py:1006-1009
-        Ebp = torch.zeros(nmol, dtype=torch.float64).index_add(0, mol, Ea)
+        Ebp = torch.zeros(nmol, dtype=dt).index_add(0, mol, Ea)
         Xb = Xall * BOHRPERA
-        dip = torch.zeros(nmol, 3, dtype=torch.float64).index_add(0, mol, Xb[:nrow] * qs[:, None])
+        dip = torch.zeros(nmol, 3, dtype=dt).index_add(0, mol, Xb[:nrow] * qs[:, None])
         ei, ej = nl["ee"]
         qall = qs if not periodic else qs.repeat(Xall.shape[0] // nrow)
         emol = mol_of_row[ei]
-        Ecc = torch.zeros(nmol, dtype=torch.float64)
+        Ecc = torch.zeros(nmol, dtype=dt)
         if self.p["AddEcc"]:
             Ecc = Ecc.index_add(0, emol, self.coulomb(Xb, qall, ei, ej))
-        Evdw = torch.zeros(nmol, dtype=torch.float64)
+        Evdw = torch.zeros(nmol, dtype=dt)
         if self.has_vdw:
             eidx = torch.tensor([self.eles.index(int(z)) for z in Z.tolist()], dtype=torch.int64)
             Evdw = Evdw.index_add(0, emol, self.vdw(Xb, eidx, ei, ej))

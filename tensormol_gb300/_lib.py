@@ -33,7 +33,7 @@ EXPORTS = [
     "tm_system_get_positions", "tm_system_build_nlist", "tm_system_nlist_counts",
     "tm_system_export_nlist", "tm_system_export_ee", "tm_energy_force",
     "tm_md_create", "tm_md_destroy", "tm_md_set_velocities", "tm_md_get_velocities", "tm_md_run",
-    "tm_selftest_gemm", "tm_system_descriptors",
+    "tm_selftest_gemm", "tm_system_descriptors", "tm_energy_force_profile",
 ]
 
 
@@ -95,6 +95,7 @@ def _declare(lib):
         "tm_md_run": (I, [P, I, D, P]),
         "tm_selftest_gemm": (I, [P, I, I, I, I, P, P, P]),
         "tm_system_descriptors": (I, [P, P]),
+        "tm_energy_force_profile": (I, [P, U, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

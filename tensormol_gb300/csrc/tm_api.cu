@@ -669,20 +669,56 @@ extern "C" int tm_system_export_ee(tm_system* s, int64_t* eep, int64_t cap, int 
 
 // Device-side pipeline of one energy(+force) evaluation; no host sync unless
 // the neighbour lists have to be (re)built.
-int tm_energy_force_device(tm_system* s, unsigned flags) {
+// ev (optional, 7 events): recorded on the ctx stream before the lists, the
+// descriptors, the network forward, the network backward, the pair terms, the
+// adjoint, and at the end.
+static int energy_force_pipeline(tm_system* s, unsigned flags, cudaEvent_t* ev) {
   int rc;
+  cudaStream_t st = s->ctx->stream;
+  const bool force = !(flags & TM_F_ENERGY_ONLY);
+  if (ev) cudaEventRecord(ev[0], st);
   if (!(flags & TM_F_REUSE_NLIST) || !s->nlist_valid) {
     if ((rc = tm_launch_nlist(s))) return rc;
   } else {
     if ((rc = tm_launch_positions(s))) return rc;
   }
-  const bool force = !(flags & TM_F_ENERGY_ONLY);
+  if (ev) cudaEventRecord(ev[1], st);
   if ((rc = tm_launch_descriptors(s))) return rc;
-  if ((rc = tm_launch_mlp(s, force))) return rc;
+  if (ev) cudaEventRecord(ev[2], st);
+  if (ev) {
+    if ((rc = tm_launch_mlp(s, false))) return rc;
+    cudaEventRecord(ev[3], st);
+    if (force && (rc = tm_launch_mlp_backward_only(s))) return rc;
+    cudaEventRecord(ev[4], st);
+  } else if ((rc = tm_launch_mlp(s, force))) {
+    return rc;
+  }
   if ((rc = tm_launch_mlp_finish(s))) return rc;
   if ((rc = tm_launch_coulomb(s, flags))) return rc;
+  if (ev) cudaEventRecord(ev[5], st);
   if (force && (rc = tm_launch_adjoint(s, flags))) return rc;
+  if (ev) cudaEventRecord(ev[6], st);
   return TM_OK;
+}
+
+int tm_energy_force_device(tm_system* s, unsigned flags) {
+  return energy_force_pipeline(s, flags, nullptr);
+}
+
+extern "C" int tm_energy_force_profile(tm_system* s, unsigned flags, float* stage_ms) {
+  if (!s || !stage_ms) return TM_E_ARG;
+  tm_ctx* ctx = s->ctx;
+  cudaEvent_t ev[7];
+  for (auto& e : ev) cudaEventCreate(&e);
+  int rc = energy_force_pipeline(s, flags & ~(unsigned)TM_F_DEVICE_IO, ev);
+  if (!rc) rc = tm_cuda_check(ctx, cudaEventSynchronize(ev[6]), "profile");
+  if (!rc) {
+    for (int q = 0; q < 6; ++q) cudaEventElapsedTime(&stage_ms[q], ev[q], ev[q + 1]);
+    cudaEventElapsedTime(&stage_ms[6], ev[0], ev[6]);
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (!rc) rc = tm_sync_status(ctx, "profile");
+  return rc;
 }
 
 extern "C" int tm_energy_force(tm_system* s, const double* x, unsigned flags, double* E_out,

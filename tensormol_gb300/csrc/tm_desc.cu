@@ -221,7 +221,12 @@ __global__ void __launch_bounds__(128) k_desc_fwd(const DescArgs a, const tm_con
         if (act) {
           const int sa = seg[ea] + pa, sb = seg[eb] + pb;
           const float c = w.ux[sa] * w.ux[sb] + w.uy[sa] * w.uy[sb] + w.uz[sa] * w.uz[sb];
-          const float sn = sqrtf(fmaxf(0.f, 1.f - c * c));
+          // sin(theta) = |u_a x u_b|: well conditioned for nearly collinear triples,
+          // where sqrt(1 - c^2) loses most of its digits in FP32
+          const float nx = w.uy[sa] * w.uz[sb] - w.uz[sa] * w.uy[sb];
+          const float ny = w.uz[sa] * w.ux[sb] - w.ux[sa] * w.uz[sb];
+          const float nz = w.ux[sa] * w.uy[sb] - w.uy[sa] * w.ux[sb];
+          const float sn = sqrtf(nx * nx + ny * ny + nz * nz);
           const float T = c * cth + sn * sth;
           float p, dp;
           powz(fmaxf(0.f, 1.f + T), k, p, dp);
@@ -355,11 +360,16 @@ __global__ void __launch_bounds__(128) k_desc_adj(const DescArgs a, const tm_con
         const bool act = tb + grp < npair;
         int sa = 0, sb = 0;
         float c = 0.f, sn = 0.f, A = 0.f, dA = 0.f, B = 0.f, Bd = 0.f;
+        float nx = 0.f, ny = 0.f, nz = 0.f;
         if (act) {
           sa = seg[ea] + pa;
           sb = seg[eb] + pb;
           c = w.ux[sa] * w.ux[sb] + w.uy[sa] * w.uy[sb] + w.uz[sa] * w.uz[sb];
-          sn = sqrtf(fmaxf(0.f, 1.f - c * c));
+          // n = u_a x u_b, sin(theta) = |n| (accurate near collinearity)
+          nx = w.uy[sa] * w.uz[sb] - w.uz[sa] * w.uy[sb];
+          ny = w.uz[sa] * w.ux[sb] - w.ux[sa] * w.uz[sb];
+          nz = w.ux[sa] * w.uy[sb] - w.uy[sa] * w.ux[sb];
+          sn = sqrtf(nx * nx + ny * ny + nz * nz);
           const float T = c * cth + sn * sth;
           const float dT = -(sn * cth - c * sth);   // d cos(theta - theta_m) / d theta
           float p, dp;
@@ -390,17 +400,21 @@ __global__ void __launch_bounds__(128) k_desc_adj(const DescArgs a, const tm_con
           const float dra = 0.5f * S2 * fcc + S1 * w.fcd[sa] * fb;
           const float drb = 0.5f * S2 * fcc + S1 * fa * w.fcd[sb];
           const float dth = S3 * fcc;
-          const float kc = -dth / fmaxf(sn, 1e-6f);   // dE/dc
+          // d theta / d d_a = -(u_b - c u_a) / (r_a sin theta); the in-plane
+          // directions are formed as n x u_a and u_b x n, whose length is sin theta
+          const float kc = -dth / fmaxf(sn, 1e-30f);
           const float ra = w.r[sa], rb = w.r[sb];
           const float uax = w.ux[sa], uay = w.uy[sa], uaz = w.uz[sa];
           const float ubx = w.ux[sb], uby = w.uy[sb], ubz = w.uz[sb];
+          const float pax = ny * uaz - nz * uay, pay = nz * uax - nx * uaz, paz = nx * uay - ny * uax;
+          const float pbx = uby * nz - ubz * ny, pby = ubz * nx - ubx * nz, pbz = ubx * ny - uby * nx;
           const float ka = kc / ra, kb = kc / rb;
-          const float gax = dra * uax + ka * (ubx - c * uax);
-          const float gay = dra * uay + ka * (uby - c * uay);
-          const float gaz = dra * uaz + ka * (ubz - c * uaz);
-          const float gbx = drb * ubx + kb * (uax - c * ubx);
-          const float gby = drb * uby + kb * (uay - c * uby);
-          const float gbz = drb * ubz + kb * (uaz - c * ubz);
+          const float gax = dra * uax + ka * pax;
+          const float gay = dra * uay + ka * pay;
+          const float gaz = dra * uaz + ka * paz;
+          const float gbx = drb * ubx + kb * pbx;
+          const float gby = drb * uby + kb * pby;
+          const float gbz = drb * ubz + kb * pbz;
           fx += gax + gbx;
           fy += gay + gby;
           fz += gaz + gbz;

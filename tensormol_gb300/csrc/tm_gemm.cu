@@ -460,7 +460,12 @@ int tm_make_tmap(tm_ctx* ctx, CUtensorMap* map, void* base, int elem_bytes, uint
 //   fwd 0..L-1 (last one: energy dot product + g_L = w_out * act'(z_L)),
 //   bwd L-1..1 (g_{l-1} = (g_l W_l^T) * act'(z_{l-1}), in place over h_{l-1}),
 //   bwd 0 (dE/dG = g_1 W_1^T, FP32).
-int tm_launch_mlp(tm_system* s, bool backward) {
+static int mlp_layers(tm_system* s, bool forward, bool backward);
+
+int tm_launch_mlp(tm_system* s, bool backward) { return mlp_layers(s, true, backward); }
+int tm_launch_mlp_backward_only(tm_system* s) { return mlp_layers(s, false, true); }
+
+static int mlp_layers(tm_system* s, bool forward, bool backward) {
   tm_model* m = s->model;
   tm_ctx* ctx = s->ctx;
   const int L = m->nlayer;
@@ -481,7 +486,7 @@ int tm_launch_mlp(tm_system* s, bool backward) {
   g.act = m->k.act;
   g.alpha = m->k.alpha_sig;
   g.st = ctx->d_status;
-  for (int l = 0; l < L; ++l) {
+  for (int l = 0; forward && l < L; ++l) {
     const bool last = (l == L - 1);
     const CUtensorMap* const* A = l == 0 ? lv0 : lvH[l - 1];
     g.a0 = *A[0];

@@ -178,6 +178,7 @@ int tm_launch_adjoint(tm_system* s, unsigned flags);
 int tm_make_tmap(tm_ctx* ctx, CUtensorMap* map, void* base, int elem_bytes, uint64_t rows,
                  uint64_t cols, uint32_t box_rows);
 int tm_launch_mlp(tm_system* s, bool backward);
+int tm_launch_mlp_backward_only(tm_system* s);
 int tm_gemm_selftest(tm_ctx* ctx, int prec, int M, int N, int K, const float* A,
                      const float* B, float* C);
 // tm_coulomb.cu
