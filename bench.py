@@ -216,8 +216,32 @@ def oracle_eval(w, eles, W):
 def errors(E, F, ref, natoms):
     from tensormol_gb300.params import EV_PER_HARTREE, JOULEPERHARTREE
     dE = abs(float(np.ravel(E)[0]) - float(ref["Etotal"][0])) * EV_PER_HARTREE / natoms
-    dF = float(np.abs(F - ref["force"]).max() / JOULEPERHARTREE * EV_PER_HARTREE)
-    return {"dE_per_atom_eV": dE, "max_dF_eV_per_A": dF}
+    per_atom = np.abs(F - ref["force"]).max(1) / JOULEPERHARTREE * EV_PER_HARTREE
+    return {"dE_per_atom_eV": dE, "max_dF_eV_per_A": float(per_atom.max()),
+            "p999_dF_eV_per_A": float(np.quantile(per_atom, 0.999)),
+            "frac_atoms_within_1e-4": float(np.mean(per_atom < 1e-4))}
+
+
+def smooth_accuracy(w, eles, flush, torch):
+    """Fused FP32 path vs the FP64 oracle with the smooth activation of the
+    reference's released networks (sigmoid_with_param, alpha = 100): with relu
+    the FP64 forces themselves jump by ~0.1 eV/A under 1e-6 A perturbations
+    (units at their kink), so a max-abs bound is only meaningful here."""
+    from tensormol_gb300 import systems
+    from tensormol_gb300.model import BPEEModel
+    from tensormol_gb300.params import PARAMS, descriptor_width
+    p = dict(PARAMS)
+    p["NeuronType"] = "sigmoid_with_param"
+    W = systems.random_weights(eles, descriptor_width(2), seed=7)
+    m = BPEEModel(eles, W, params=p, precision="fp32")
+    s = m.system(w.x, w.Z, w.offsets)
+    o = s.energy_force(w.x, True)
+    s.close()
+    m.close()
+    torch.set_num_threads(os.cpu_count() or 1)
+    from oracle import reference as orc
+    ref = orc.OpenSystemOracle(orc.Model(eles, W, p), w.x, w.Z, w.offsets).terms(w.x)
+    return errors(o["Etotal"], o["force"], ref, w.natoms)
 
 
 def run_reference(args):
@@ -363,6 +387,8 @@ def main():
         acc = {"fused_fp32": errors(E, F, ref, natoms), "bf16": errors(E16, F16, ref, natoms)}
         if plain is not None:
             acc["plain_autograd"] = errors(Ep, Fp, ref, natoms)
+        acc["activation"] = "relu"
+        acc["fused_fp32_sigmoid_with_param"] = smooth_accuracy(w, eles, flush, torch)
         line["accuracy_vs_fp64_oracle"] = acc
     if ws > 1:
         torch.distributed.barrier()

@@ -461,6 +461,23 @@ extern "C" int tm_system_create(tm_model* m, int N, int nmol, const int32_t* Z,
     for (int d = 0; d < 3; ++d) nc *= (long)floor(s->lat[4 * d] / k.r_rc_d);
     s->ncell_cap = (int)nc;
   }
+  // Coulomb grid: about 24 atoms per cell; a periodic edge gets the fewest
+  // cells of at least that size for which the +-R cell search visits no cell
+  // twice (2R + 1 <= n)
+  s->ecell_cap = N + 64 * nmol;
+  if (s->periodic) {
+    const double vol = s->lat[0] * s->lat[4] * s->lat[8];
+    const double cs = std::max(2.0, cbrt(24.0 * vol / N));
+    long nc = 1;
+    for (int d = 0; d < 3; ++d) {
+      const double L = s->lat[4 * d];
+      int n = std::max(1, (int)floor(L / cs));
+      while (2 * (int)ceil(k.ree_d / (L / n)) + 1 > n && n < 4096) ++n;
+      s->ee_dims[d] = n;
+      nc *= n;
+    }
+    s->ecell_cap = (int)nc;
+  }
   const int H = m->H, Dp = k.Dp;
   const size_t es = m->elem_size;
   const size_t Mp = s->Mpad;
@@ -484,6 +501,16 @@ extern "C" int tm_system_create(tm_model* m, int N, int nmol, const int32_t* Z,
   A.get(&s->d_cell_start, sizeof(int32_t) * (s->ncell_cap + 1));
   A.get(&s->d_cell_atoms, sizeof(int32_t) * N);
   A.get(&s->d_cell_of_atom, sizeof(int32_t) * N);
+  A.get(&s->d_egrid, sizeof(tm_grid) * nmol);
+  A.get(&s->d_encell, sizeof(int32_t));
+  A.get(&s->d_encell_m, sizeof(int32_t) * nmol);
+  A.get(&s->d_ecell_cnt, sizeof(int32_t) * (s->ecell_cap + 1));
+  A.get(&s->d_ecell_start, sizeof(int32_t) * (s->ecell_cap + 1));
+  A.get(&s->d_ecell_atoms, sizeof(int32_t) * N);
+  A.get(&s->d_ecell_of_atom, sizeof(int32_t) * N);
+  A.get(&s->d_epos, sizeof(int32_t) * N);
+  A.get(&s->d_exhi, sizeof(float4) * N);
+  A.get(&s->d_exlo, sizeof(float4) * N);
   A.get(&s->d_cnt_r, sizeof(int32_t) * N);
   A.get(&s->d_cnt_a, sizeof(int32_t) * N);
   A.get(&s->d_nbr_r, sizeof(uint32_t) * (size_t)N * s->KR);
@@ -555,6 +582,8 @@ static void system_free(tm_system* s) {
   // sizes are not needed by cudaFreeAsync; budget accounting uses s->bytes
   void* ptrs[] = {s->row_of_atom, s->atom_of_row, s->tile_elem, s->d_Z, s->d_elem, s->d_mol,
                   s->d_off, s->d_x, s->d_xhi, s->d_xlo, s->d_x_at_build, s->d_grid, s->d_ncell, s->d_ncell_m, s->d_need,
+                  s->d_egrid, s->d_encell, s->d_encell_m, s->d_ecell_cnt, s->d_ecell_start,
+                  s->d_ecell_atoms, s->d_ecell_of_atom, s->d_epos, s->d_exhi, s->d_exlo,
                   s->d_cell_cnt, s->d_cell_start, s->d_cell_atoms, s->d_cell_of_atom, s->d_cnt_r,
                   s->d_cnt_a, s->d_nbr_r, s->d_nbr_a, s->d_rev_r, s->d_rev_a, s->d_sr, s->d_va,
                   s->dEdG, s->epart, s->d_Eatom, s->d_qraw, s->d_q, s->d_dEdq, s->d_fself,

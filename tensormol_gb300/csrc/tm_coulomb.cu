@@ -6,13 +6,14 @@
 // RawSymFunc.py:1307-1359), TFVdwPolyLR (RawSymFunc.py:1361-1414); periodic
 // halving TFBehlerParinelloSymEE.py:1550, 1620.
 //
-// Pair terms are evaluated without a stored pair list: each warp takes up to
-// eight atoms of one cell and sweeps the cells whose boxes come within the
-// Coulomb cutoff, lanes striding over candidate atoms. Every pair is evaluated
-// from both ends (a gather), so per-atom sums need no atomics and are
-// deterministic. Membership uses the same FP32 screen + exact FP64 rule as the
-// neighbour lists. Energies are returned as half-pair sums per atom and
-// reduced per molecule in FP64.
+// Pair terms are evaluated without a stored pair list, on a second cell grid
+// sized for about 24 atoms per cell with the atoms packed in cell order: one
+// warp per cell, lane = centre atom; the cells whose boxes come within the
+// Coulomb cutoff are staged 32 atoms at a time in shared memory and read by
+// all lanes as broadcasts. Every pair is evaluated from both ends (a gather),
+// so per-atom sums need no atomics and are deterministic. Membership uses the
+// same FP32 screen + exact FP64 rule as the neighbour lists. Energies are
+// returned as half-pair sums per atom and reduced per molecule in FP64.
 #include <cuda_runtime.h>
 
 #include "tm_internal.h"
@@ -20,7 +21,6 @@
 namespace {
 
 constexpr float kBand = 1e-5f;
-constexpr int GI = 8;   // centre atoms per warp
 
 __global__ void k_mlp_finish(const float* __restrict__ epart, const double* __restrict__ bout,
                              const int32_t* __restrict__ row_of_atom,
@@ -67,32 +67,34 @@ __global__ void k_mol_sum1(const int32_t* __restrict__ off, const double* __rest
 
 __global__ void k_neutralize(const int32_t* __restrict__ mol, const int32_t* __restrict__ off,
                              const float* __restrict__ qraw, const double* __restrict__ aux,
-                             float* __restrict__ q, int N) {
+                             float* __restrict__ q, const int32_t* __restrict__ epos,
+                             float4* __restrict__ exlo, int N) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   const int m = mol[i];
   const double n = (double)(off[m + 1] - off[m]);
-  q[i] = (float)((double)qraw[i] - aux[8 * m] / n);   // TFBehlerParinelloSymEE.py:1006-1009
+  const float qi = (float)((double)qraw[i] - aux[8 * m] / n);   // TFBehlerParinelloSymEE.py:1006-1009
+  q[i] = qi;
+  exlo[epos[i]].w = qi;
 }
 
 struct CoulArgs {
   const double* x;
-  const float4* xhi;
-  const float4* xlo;
-  const float* q;
+  const float4* exhi;       // cell-ordered hi parts (w = element)
+  const float4* exlo;       // cell-ordered lo parts (w = charge)
+  const int32_t* eatom;     // cell-ordered atom index
   const int32_t* mol;
-  const tm_grid* grid;
+  const tm_grid* grid;      // Coulomb grid per molecule
   const int32_t* cell_start;
-  const int32_t* cell_atoms;
   const int32_t* ncell;
   int ncell_cap;
-  double* ecv;       // [N][2]
-  float* dEdqt;      // [N]  dE/d q~_i
-  float4* fcv;       // [N]  dE/dx_i of the pair terms
-  int ref_periodic;  // image pairs contribute half the force (reference gradient)
+  double* ecv;              // [N][2]
+  float* dEdqt;             // [N]  dE/d q~_i
+  float4* fcv;              // [N]  dE/dx_i of the pair terms
+  int ref_periodic;         // image pairs contribute half the force (reference gradient)
   int periodic;
   double ree;
-  float ree2_lo, ree2_hi;
+  float ree2, ree2_lo, ree2_hi;
   double lat[9];
   float sh_hi[27][3];
   float sh_lo[27][3];
@@ -117,8 +119,9 @@ __device__ __forceinline__ PairOut pair_terms(float r, float qi, float qj, int e
       } else {
         const float ar = k.alpha * rb;
         const float ec = erfcf(ar);
-        kc = ec / rb - k.zz + (rb - k.r_lr) * (k.zz / k.r_lr + k.yy);
-        dkc = -(ec / (rb * rb) + 1.1283791671f * k.alpha * expf(-ar * ar) / rb) +
+        const float ir = 1.f / rb;
+        kc = ec * ir - k.zz + (rb - k.r_lr) * (k.zz / k.r_lr + k.yy);
+        dkc = -(ec * ir * ir + 1.1283791671f * k.alpha * expf(-ar * ar) * ir) +
               (k.zz / k.r_lr + k.yy);
       }
     } else {
@@ -144,55 +147,48 @@ __device__ __forceinline__ PairOut pair_terms(float r, float qi, float qj, int e
     const float inv6 = inv2 * inv2 * inv2;
     const float xr = R0 * inv;                       // (rp/R0)^-1
     const float x2 = xr * xr, x4 = x2 * x2, x12 = x4 * x4 * x4;
-    const float den = 1.f + 6.f * x12;
-    const float damp = 1.f / den;
+    const float damp = 1.f / (1.f + 6.f * x12);
     const float K = -cut * s6 * inv6 * damp;
-    // d damp / d rp = 72 x12 / (rp den^2)
-    const float dK = -s6 * (dcut * inv6 * damp - 6.f * cut * inv6 * inv * damp +
-                            cut * inv6 * 72.f * x12 * inv * damp * damp);
+    // d damp / d rp = 72 x12 / (rp (1 + 6 x12)^2)
+    const float dK = -s6 * inv6 * damp * (dcut - 6.f * cut * inv + 72.f * cut * x12 * inv * damp);
     o.e_vdw = K;
     o.dedr += dK * b2;
   }
   return o;
 }
 
+// One warp per Coulomb-grid cell; lane = centre atom (cells with more than 32
+// atoms loop). Candidate cells are culled by box distance and staged 32 atoms
+// at a time in shared memory, read back as broadcasts by every lane.
 __global__ void __launch_bounds__(128) k_coulomb(const CoulArgs a, const tm_consts k) {
+  __shared__ float4 sh[4][2][32];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int c = blockIdx.x * (blockDim.x >> 5) + wib;
-  if (c >= *a.ncell) return;
+  if (c >= a.ncell_cap || c >= *a.ncell) return;
   const int t0 = a.cell_start[c], t1 = a.cell_start[c + 1];
   if (t1 <= t0) return;
-  const int m = a.mol[a.cell_atoms[t0]];
-  const tm_grid g = a.grid[m];
+  const tm_grid g = a.grid[a.mol[a.eatom[t0]]];
   const int lc = c - g.cell_off;
   const int iz = lc % g.nz, iy = (lc / g.nz) % g.ny, ix = lc / (g.nz * g.ny);
+  const float cx = (float)g.cx, cy = (float)g.cy, cz = (float)g.cz;
   const int Rx = (int)ceil(a.ree / g.cx), Ry = (int)ceil(a.ree / g.cy), Rz = (int)ceil(a.ree / g.cz);
-  const double ree2 = a.ree * a.ree;
-  for (int gb = t0; gb < t1; gb += GI) {
-    const int ng = min(GI, t1 - gb);
-    int ia[GI];
-    float4 hi[GI], lo[GI];
-    float qi[GI];
-    int ei[GI];
-    float acc_cc[GI], acc_vdw[GI], gx[GI], gy[GI], gz[GI];
-#pragma unroll
-    for (int u = 0; u < GI; ++u) {
-      const int t = gb + (u < ng ? u : 0);
-      ia[u] = a.cell_atoms[t];
-      hi[u] = a.xhi[ia[u]];
-      lo[u] = a.xlo[ia[u]];
-      qi[u] = a.q[ia[u]];
-      ei[u] = __float_as_int(hi[u].w);
-      acc_cc[u] = acc_vdw[u] = gx[u] = gy[u] = gz[u] = 0.f;
-    }
+  float4* sj_hi = sh[wib][0];
+  float4* sj_lo = sh[wib][1];
+  for (int ib = t0; ib < t1; ib += 32) {
+    const int ti = ib + lane;
+    const bool have = ti < t1;
+    const float4 hi = a.exhi[have ? ti : t0];
+    const float4 lo = a.exlo[have ? ti : t0];
+    const int ei = __float_as_int(hi.w);
+    const float qi = lo.w;
+    float acc_cc = 0.f, acc_vdw = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
     for (int ox = -Rx; ox <= Rx; ++ox) {
-      const double gapx = fmax(0.0, fabs((double)ox) - 1.0) * g.cx;
+      const float gapx = fmaxf(0.f, (float)(abs(ox) - 1)) * cx;
       for (int oy = -Ry; oy <= Ry; ++oy) {
-        const double gapy = fmax(0.0, fabs((double)oy) - 1.0) * g.cy;
+        const float gapy = fmaxf(0.f, (float)(abs(oy) - 1)) * cy;
         for (int oz = -Rz; oz <= Rz; ++oz) {
-          const double gapz = fmax(0.0, fabs((double)oz) - 1.0) * g.cz;
-          // boxes of the two cells are at least this far apart
-          if (gapx * gapx + gapy * gapy + gapz * gapz > ree2) continue;
+          const float gapz = fmaxf(0.f, (float)(abs(oz) - 1)) * cz;
+          if (gapx * gapx + gapy * gapy + gapz * gapz > a.ree2_hi) continue;
           int jx = ix + ox, jy = iy + oy, jz = iz + oz, sx = 0, sy = 0, sz = 0;
           if (a.periodic) {
             if (jx < 0) { jx += g.nx; sx = -1; } else if (jx >= g.nx) { jx -= g.nx; sx = 1; }
@@ -203,28 +199,29 @@ __global__ void __launch_bounds__(128) k_coulomb(const CoulArgs a, const tm_cons
           }
           const int cj = g.cell_off + (jx * g.ny + jy) * g.nz + jz;
           const int r = 9 * (sx + 1) + 3 * (sy + 1) + (sz + 1);
-          const float shh[3] = {a.sh_hi[r][0], a.sh_hi[r][1], a.sh_hi[r][2]};
-          const float shl[3] = {a.sh_lo[r][0], a.sh_lo[r][1], a.sh_lo[r][2]};
+          const float shx = a.sh_hi[r][0], shy = a.sh_hi[r][1], shz = a.sh_hi[r][2];
+          const float slx = a.sh_lo[r][0], sly = a.sh_lo[r][1], slz = a.sh_lo[r][2];
           const float fscale = (a.ref_periodic && r != TM_IMG_SELF) ? 0.5f : 1.f;
           const int u0 = a.cell_start[cj], u1 = a.cell_start[cj + 1];
-          for (int tb = u0; tb < u1; tb += 32) {
-            const int t = tb + lane;
-            if (t >= u1) continue;
-            const int j = a.cell_atoms[t];
-            const float4 hj = a.xhi[j], lj = a.xlo[j];
-            const float qj = a.q[j];
-            const int ej = __float_as_int(hj.w);
-#pragma unroll
-            for (int u = 0; u < GI; ++u) {
-              if (u >= ng) continue;
-              if (j == ia[u] && r == TM_IMG_SELF) continue;
-              const float dx = ds_sub_shift(hi[u].x, lo[u].x, hj.x, lj.x, shh[0], shl[0]);
-              const float dy = ds_sub_shift(hi[u].y, lo[u].y, hj.y, lj.y, shh[1], shl[1]);
-              const float dz = ds_sub_shift(hi[u].z, lo[u].z, hj.z, lj.z, shh[2], shl[2]);
+          for (int jb = u0; jb < u1; jb += 32) {
+            const int nj = min(32, u1 - jb);
+            __syncwarp();
+            if (lane < nj) {
+              sj_hi[lane] = a.exhi[jb + lane];
+              sj_lo[lane] = a.exlo[jb + lane];
+            }
+            __syncwarp();
+            if (!have) continue;
+            for (int q = 0; q < nj; ++q) {
+              if (cj == c && jb + q == ti && r == TM_IMG_SELF) continue;   // the atom itself
+              const float4 hj = sj_hi[q], lj = sj_lo[q];
+              const float dx = ds_sub_shift(hi.x, lo.x, hj.x, lj.x, shx, slx);
+              const float dy = ds_sub_shift(hi.y, lo.y, hj.y, lj.y, shy, sly);
+              const float dz = ds_sub_shift(hi.z, lo.z, hj.z, lj.z, shz, slz);
               const float d2 = dx * dx + dy * dy + dz * dz;
               if (d2 > a.ree2_hi) continue;
-              if (d2 >= a.ree2_lo) {
-                const int i = ia[u];
+              if (d2 >= a.ree2_lo) {   // within 1e-5 of the cutoff: the exact FP64 rule
+                const int i = a.eatom[ti], j = a.eatom[jb + q];
                 double xj = a.x[3 * j], yj = a.x[3 * j + 1], zj = a.x[3 * j + 2];
                 if (a.periodic) {
                   xj = tm_image_coord(xj, sx, sy, sz, a.lat[0], a.lat[3], a.lat[6]);
@@ -235,32 +232,24 @@ __global__ void __launch_bounds__(128) k_coulomb(const CoulArgs a, const tm_cons
                   continue;
               }
               const float rr = sqrtf(d2);
-              const PairOut po = pair_terms(rr, qi[u], qj, ei[u], ej, k);
-              acc_cc[u] += po.e_cc;
-              acc_vdw[u] += po.e_vdw;
-              const float s = fscale * po.dedr / rr;
-              gx[u] += s * dx;
-              gy[u] += s * dy;
-              gz[u] += s * dz;
+              const PairOut po = pair_terms(rr, qi, lj.w, ei, __float_as_int(hj.w), k);
+              acc_cc += po.e_cc;
+              acc_vdw += po.e_vdw;
+              const float sc = fscale * po.dedr / rr;
+              gx += sc * dx;
+              gy += sc * dy;
+              gz += sc * dz;
             }
           }
         }
       }
     }
-#pragma unroll
-    for (int u = 0; u < GI; ++u) {
-      const float c0 = warp_sum(acc_cc[u]);
-      const float c1 = warp_sum(acc_vdw[u]);
-      const float fx = warp_sum(gx[u]);
-      const float fy = warp_sum(gy[u]);
-      const float fz = warp_sum(gz[u]);
-      if (lane == 0 && u < ng) {
-        const int i = ia[u];
-        a.ecv[2 * i + 0] = 0.5 * (double)qi[u] * (double)c0;
-        a.ecv[2 * i + 1] = 0.5 * (double)c1;
-        a.dEdqt[i] = c0;
-        a.fcv[i] = make_float4(fx, fy, fz, 0.f);
-      }
+    if (have) {
+      const int i = a.eatom[ti];
+      a.ecv[2 * i + 0] = 0.5 * (double)qi * (double)acc_cc;
+      a.ecv[2 * i + 1] = 0.5 * (double)acc_vdw;
+      a.dEdqt[i] = acc_cc;
+      a.fcv[i] = make_float4(gx, gy, gz, 0.f);
     }
   }
 }
@@ -324,7 +313,8 @@ int tm_launch_mlp_finish(tm_system* s) {
   k_mol_sum1<<<s->nmol, 256, 0, ctx->stream>>>(s->d_off, s->d_Eatom, s->d_qraw, s->d_mol_E,
                                                s->d_mol_aux);
   k_neutralize<<<tm_div_up(s->N, 256), 256, 0, ctx->stream>>>(s->d_mol, s->d_off, s->d_qraw,
-                                                              s->d_mol_aux, s->d_q, s->N);
+                                                              s->d_mol_aux, s->d_q, s->d_epos,
+                                                              s->d_exlo, s->N);
   ctx->launches += 3;
   return tm_cuda_check(ctx, cudaGetLastError(), "mlp finish");
 }
@@ -333,18 +323,18 @@ int tm_launch_coulomb(tm_system* s, unsigned flags) {
   tm_ctx* ctx = s->ctx;
   const tm_consts& k = s->model->k;
   CoulArgs a;
-  a.x = s->d_x; a.xhi = s->d_xhi; a.xlo = s->d_xlo; a.q = s->d_q; a.mol = s->d_mol;
-  a.grid = s->d_grid; a.cell_start = s->d_cell_start; a.cell_atoms = s->d_cell_atoms;
-  a.ncell = s->d_ncell; a.ncell_cap = s->ncell_cap; a.ecv = s->d_ecv; a.dEdqt = s->d_dEdq;
-  a.fcv = s->d_fcv;
+  a.x = s->d_x; a.exhi = s->d_exhi; a.exlo = s->d_exlo; a.eatom = s->d_ecell_atoms;
+  a.mol = s->d_mol; a.grid = s->d_egrid; a.cell_start = s->d_ecell_start; a.ncell = s->d_encell;
+  a.ncell_cap = s->ecell_cap; a.ecv = s->d_ecv; a.dEdqt = s->d_dEdq; a.fcv = s->d_fcv;
   a.ref_periodic = (s->periodic && (flags & TM_F_REFERENCE_PERIODIC_FORCE)) ? 1 : 0;
   a.periodic = s->periodic ? 1 : 0;
   a.ree = k.ree_d;
-  a.ree2_lo = (float)(k.ree_d * k.ree_d) * (1.f - kBand);
-  a.ree2_hi = (float)(k.ree_d * k.ree_d) * (1.f + kBand);
+  a.ree2 = (float)(k.ree_d * k.ree_d);
+  a.ree2_lo = a.ree2 * (1.f - kBand);
+  a.ree2_hi = a.ree2 * (1.f + kBand);
   for (int q = 0; q < 9; ++q) a.lat[q] = s->lat[q];
   tm_fill_shifts(s, a.sh_hi, a.sh_lo);
-  k_coulomb<<<tm_div_up(s->ncell_cap, 4), 128, 0, ctx->stream>>>(a, k);
+  k_coulomb<<<tm_div_up(s->ecell_cap, 4), 128, 0, ctx->stream>>>(a, k);
   k_mol_sum2<<<s->nmol, 256, 0, ctx->stream>>>(s->d_off, s->d_ecv, s->d_dEdq, s->d_q, s->d_x,
                                                (double)k.bohr, s->d_mol_E, s->d_mol_aux);
   k_dq<<<tm_div_up(s->N, 256), 256, 0, ctx->stream>>>(s->d_mol, s->d_off, s->d_mol_aux, s->d_dEdq,

@@ -119,6 +119,19 @@ struct tm_system {
   int32_t* d_cell_start = nullptr;     // [ncell_cap+1]
   int32_t* d_cell_atoms = nullptr;     // [N]
   int32_t* d_cell_of_atom = nullptr;   // [N]
+  // coarser grid for the Coulomb/vdW pair terms (about 24 atoms per cell)
+  int ee_dims[3] = {0, 0, 0};          // periodic: host-chosen cells per edge
+  int ecell_cap = 0;
+  tm_grid* d_egrid = nullptr;          // [nmol]
+  int32_t* d_encell = nullptr;         // total cells (device scalar)
+  int32_t* d_encell_m = nullptr;       // [nmol]
+  int32_t* d_ecell_cnt = nullptr;      // [ecell_cap+1]
+  int32_t* d_ecell_start = nullptr;    // [ecell_cap+1]
+  int32_t* d_ecell_atoms = nullptr;    // [N] atoms in cell order
+  int32_t* d_ecell_of_atom = nullptr;  // [N]
+  int32_t* d_epos = nullptr;           // [N] position of an atom in cell order
+  float4* d_exhi = nullptr;            // [N] cell-ordered hi parts (w = element)
+  float4* d_exlo = nullptr;            // [N] cell-ordered lo parts (w = charge)
   // neighbour lists (ELL, per centre sorted by (element, reference index))
   int KR = 64, KA = 48;
   int32_t* d_cnt_r = nullptr;

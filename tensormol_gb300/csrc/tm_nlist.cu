@@ -46,9 +46,13 @@ __global__ void k_positions(const double* __restrict__ x, const int32_t* __restr
 // ---------------------------------------------------------------------------
 // per-molecule grid set-up (block per molecule)
 // ---------------------------------------------------------------------------
+// rc: smallest cell edge. occ > 0 sizes open-boundary cells for about occ
+// atoms each (Coulomb grid); cap_a * n + cap_c bounds the cells of a molecule.
+// Periodic grids take pn[] cells per edge when given, else floor(L / rc).
 __global__ void k_grid_setup(const double* __restrict__ x, const int32_t* __restrict__ off,
                              tm_grid* __restrict__ grid, int32_t* __restrict__ ncell_m,
-                             double rc, int periodic, double Lx, double Ly, double Lz) {
+                             double rc, int periodic, double Lx, double Ly, double Lz,
+                             double occ, double cap_a, double cap_c, int pnx, int pny, int pnz) {
   const int m = blockIdx.x;
   const int a0 = off[m], a1 = off[m + 1];
   __shared__ double smin[3][32], smax[3][32];
@@ -81,9 +85,9 @@ __global__ void k_grid_setup(const double* __restrict__ x, const int32_t* __rest
     g.pad = 0;
     if (periodic) {
       g.ox = g.oy = g.oz = 0.0;
-      g.nx = max(1, (int)floor(Lx / rc));
-      g.ny = max(1, (int)floor(Ly / rc));
-      g.nz = max(1, (int)floor(Lz / rc));
+      g.nx = pnx > 0 ? pnx : max(1, (int)floor(Lx / rc));
+      g.ny = pny > 0 ? pny : max(1, (int)floor(Ly / rc));
+      g.nz = pnz > 0 ? pnz : max(1, (int)floor(Lz / rc));
       g.cx = Lx / g.nx; g.cy = Ly / g.ny; g.cz = Lz / g.nz;
     } else {
       if (a1 <= a0) { mn[0] = mn[1] = mn[2] = 0.0; mx[0] = mx[1] = mx[2] = 0.0; }
@@ -95,8 +99,12 @@ __global__ void k_grid_setup(const double* __restrict__ x, const int32_t* __rest
         if (!(ext[d] >= 0.0 && ext[d] < 1e7)) { ext[d] = 0.0; mn[d] = 0.0; }
       }
       g.ox = mn[0]; g.oy = mn[1]; g.oz = mn[2];
-      const double cap = 2.0 * (a1 - a0) + 64.0;
+      const double cap = cap_a * (a1 - a0) + cap_c;
       double cs = rc;
+      if (occ > 0.0) {
+        const double vol = fmax(ext[0], rc) * fmax(ext[1], rc) * fmax(ext[2], rc);
+        cs = fmax(rc, cbrt(occ * vol / fmax(1.0, (double)(a1 - a0))));
+      }
       for (int it = 0; it < 200; ++it) {
         const double p = (floor(ext[0] / cs) + 1.0) * (floor(ext[1] / cs) + 1.0) * (floor(ext[2] / cs) + 1.0);
         if (p <= cap) break;
@@ -157,6 +165,19 @@ __global__ void k_cell_sort(const int32_t* __restrict__ start, int32_t* __restri
     while (q >= a && atoms[q] > v) { atoms[q + 1] = atoms[q]; --q; }
     atoms[q + 1] = v;
   }
+}
+
+// Cell-ordered copies of the double-single positions for the pair kernel;
+// the charge slot (lo.w) is filled after the charge network runs.
+__global__ void k_ee_pack(const int32_t* __restrict__ order, const float4* __restrict__ xhi,
+                          const float4* __restrict__ xlo, int32_t* __restrict__ pos,
+                          float4* __restrict__ ohi, float4* __restrict__ olo, int N) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= N) return;
+  const int a = order[p];
+  pos[a] = p;
+  ohi[p] = xhi[a];
+  olo[p] = xlo[a];
 }
 
 __global__ void k_grid_offsets(tm_grid* __restrict__ grid, const int32_t* __restrict__ ncell_m,
@@ -698,7 +719,8 @@ int tm_launch_nlist(tm_system* s) {
   int rc;
   if ((rc = tm_launch_positions(s))) return rc;
   k_grid_setup<<<s->nmol, 256, 0, st>>>(s->d_x, s->d_off, s->d_grid, s->d_ncell_m, k.r_rc_d,
-                                          s->periodic ? 1 : 0, s->lat[0], s->lat[4], s->lat[8]);
+                                          s->periodic ? 1 : 0, s->lat[0], s->lat[4], s->lat[8],
+                                          0.0, 2.0, 64.0, 0, 0, 0);
   k_grid_offsets<<<1, 32, 0, st>>>(s->d_grid, s->d_ncell_m, s->nmol, s->d_ncell, s->ncell_cap,
                                    ctx->d_status);
   ctx->launches += 2;
@@ -731,6 +753,28 @@ int tm_launch_nlist(tm_system* s) {
                                                     s->d_mol, s->d_off, s->N, s->KR);
   k_nbr_reverse<<<tm_div_up(s->N, 4), 128, 0, st>>>(s->d_nbr_a, s->d_cnt_a, s->d_rev_a, s->d_elem,
                                                     s->d_mol, s->d_off, s->N, s->KA);
+  ctx->launches += 3;
+  // Coulomb grid: about 24 atoms per cell, atoms packed in cell order
+  k_grid_setup<<<s->nmol, 256, 0, st>>>(s->d_x, s->d_off, s->d_egrid, s->d_encell_m, 2.0,
+                                          s->periodic ? 1 : 0, s->lat[0], s->lat[4], s->lat[8],
+                                          24.0, 1.0, 64.0, s->ee_dims[0], s->ee_dims[1], s->ee_dims[2]);
+  k_grid_offsets<<<1, 32, 0, st>>>(s->d_egrid, s->d_encell_m, s->nmol, s->d_encell, s->ecell_cap,
+                                   ctx->d_status);
+  cudaMemsetAsync(s->d_ecell_cnt, 0, sizeof(int32_t) * (s->ecell_cap + 1), st);
+  k_cell_count<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_x, s->d_mol, s->d_egrid, s->d_ecell_cnt,
+                                                      s->d_ecell_of_atom, s->N, s->ecell_cap,
+                                                      ctx->d_status);
+  ctx->launches += 3;
+  if ((rc = scan_exclusive<int32_t>(ctx, s->d_ecell_cnt, s->d_ecell_start, s->ecell_cap + 1,
+                                    nullptr)))
+    return rc;
+  cudaMemsetAsync(s->d_ecell_cnt, 0, sizeof(int32_t) * (s->ecell_cap + 1), st);
+  k_cell_fill<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_ecell_of_atom, s->d_ecell_start,
+                                                     s->d_ecell_cnt, s->d_ecell_atoms, s->N);
+  k_cell_sort<<<tm_div_up(s->ecell_cap, 128), 128, 0, st>>>(s->d_ecell_start, s->d_ecell_atoms,
+                                                              s->d_encell, s->ecell_cap);
+  k_ee_pack<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_ecell_atoms, s->d_xhi, s->d_xlo, s->d_epos,
+                                                  s->d_exhi, s->d_exlo, s->N);
   ctx->launches += 3;
   cudaMemcpyAsync(s->d_x_at_build, s->d_x, sizeof(double) * 3 * s->N, cudaMemcpyDeviceToDevice, st);
   s->nlist_valid = true;

@@ -178,3 +178,27 @@ def test_bf16_error_is_reported(gpu):
     dE, dF = _errors(out, ref, w.natoms)
     print(f"BF16 water60: dE/atom={dE:.2e} eV  max|dF|={dF:.2e} eV/A")
     assert np.isfinite(dE) and np.isfinite(dF) and dE < 1e-2 and dF < 1.0
+
+
+def test_energy_force_water24k_smooth(gpu):
+    """Full-size water cube: FP32 fused path within 1e-5 eV/atom and 1e-4 eV/A
+    of the FP64 oracle with the smooth activation (sigmoid_with_param)."""
+    w = systems.water_cube_24k(seed=1)
+    m, om = _model(gpu, [1, 8], "sigmoid_with_param")
+    s = m.system(w.x, w.Z, w.offsets)
+    out = s.energy_force(w.x, True)
+    ref = orc.OpenSystemOracle(om, w.x, w.Z, w.offsets).terms(w.x)
+    dE, dF = _errors(out, ref, w.natoms)
+    assert dE < E_TOL and dF < F_TOL, (dE, dF)
+
+
+def test_energy_force_chno128_smooth(gpu):
+    b = systems.chno_batch(nmol=128, seed=3)
+    m, om = _model(gpu, [1, 6, 7, 8], "sigmoid_with_param")
+    s = m.system(b.x, b.Z, b.offsets)
+    out = s.energy_force(b.x, True)
+    ref = orc.OpenSystemOracle(om, b.x, b.Z, b.offsets).terms(b.x)
+    n_per = np.diff(b.offsets)
+    dE = np.max(np.abs(out["Etotal"] - ref["Etotal"]) * EV_PER_HARTREE / n_per)
+    dF = np.abs(out["force"] - ref["force"]).max() / JOULEPERHARTREE * EV_PER_HARTREE
+    assert dE < E_TOL and dF < F_TOL, (dE, dF)
