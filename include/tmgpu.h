@@ -190,6 +190,34 @@ int tm_md_get_velocities(tm_md *md, double *v, int on_device);
  */
 int tm_md_run(tm_md *md, int nsteps, double skin, double *log);
 
+/* ---- allocation-free entry point ---------------------------------------- */
+/*
+ * No counterpart in the reference. The radial/angular neighbour-list build of
+ * tm_system_build_nlist for ONE open-boundary molecule, for callers that cannot
+ * let a library call cudaMalloc: a host MD engine or plugin that owns a fixed
+ * device arena, or a serving process whose memory is budgeted up front. It
+ * allocates nothing (no cudaMalloc/cudaFree, no allocating library routine);
+ * its scratch is one file-scope device array sized for at most 32768 atoms
+ * (about 2 MB, reserved on every GPU that loads the library until exit).
+ *
+ * All array arguments are device pointers the caller allocated: x[natoms][3]
+ * (Angstrom, FP64), elem[natoms] (element index, 0-based, sorted by Z as in the
+ * model), outputs cnt_r[natoms], nbr_r[natoms][KR], cnt_a[natoms],
+ * nbr_a[natoms][KA] in the library's row layout (per centre sorted by
+ * (element, index); the low 27 bits of an entry are the neighbour's atom index,
+ * the high bits the image code 13 of an open system). needed (host, may be NULL)
+ * receives the largest radial and angular counts when a row overflowed, else
+ * zeros. Returns TM_E_ARG for natoms > 32768, TM_E_CAPACITY when a row
+ * overflowed (then retry with KR/KA >= needed). Runs on `stream` and
+ * synchronises it before returning.
+ * The first call on a device looks up the scratch's device address, so make
+ * it before any stream capture. Every call reuses the same scratch (it clears
+ * what must start at zero); calls that overlap on the GPU race.
+ */
+int tm_nlist_build_static(const double *x, const int32_t *elem, int natoms, double r_rc,
+                          double a_rc, int32_t *cnt_r, uint32_t *nbr_r, int KR, int32_t *cnt_a,
+                          uint32_t *nbr_a, int KA, int32_t needed[2], void *stream);
+
 /* ---- diagnostics (used by the test-suite) ------------------------------ */
 /*
  * Runs the tensor-core layer kernel alone: C[M][N] = A[M][K] . B[N][K]^T on

@@ -34,6 +34,7 @@ EXPORTS = [
     "tm_system_export_nlist", "tm_system_export_ee", "tm_energy_force",
     "tm_md_create", "tm_md_destroy", "tm_md_set_velocities", "tm_md_get_velocities", "tm_md_run",
     "tm_selftest_gemm", "tm_system_descriptors", "tm_energy_force_profile",
+    "tm_nlist_build_static",
 ]
 
 
@@ -96,6 +97,7 @@ def _declare(lib):
         "tm_selftest_gemm": (I, [P, I, I, I, I, P, P, P]),
         "tm_system_descriptors": (I, [P, P]),
         "tm_energy_force_profile": (I, [P, U, P]),
+        "tm_nlist_build_static": (I, [P, P, I, D, D, P, P, I, P, P, I, P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -933,3 +933,145 @@ int tm_launch_export_ee(tm_system* s, int64_t* eep, int64_t cap) {
   tm_free(ctx, cnt, nb); tm_free(ctx, offs, nb); tm_free(ctx, tot, sizeof(int64_t));
   return rc;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free neighbour-list build (tm_nlist_build_static)
+//
+// For callers that own every byte of device memory themselves and cannot let
+// a library call cudaMalloc (a host MD engine or plugin that hands the GPU a
+// fixed arena, a serving process whose memory is budgeted up front): the
+// scratch of the cell-list build lives in one file-scope device array of fixed
+// size, reserved on every GPU that loads this library until the process exits.
+// ---------------------------------------------------------------------------
+#define TM_STATIC_MAX_ATOMS 32768
+#define TM_STATIC_MAX_CELLS (2 * TM_STATIC_MAX_ATOMS + 64)
+
+namespace {
+
+struct StaticScratch {
+  float4 xhi[TM_STATIC_MAX_ATOMS];
+  float4 xlo[TM_STATIC_MAX_ATOMS];
+  int32_t mol[TM_STATIC_MAX_ATOMS];
+  int32_t cell_atoms[TM_STATIC_MAX_ATOMS];
+  int32_t cell_of_atom[TM_STATIC_MAX_ATOMS];
+  int32_t cell_cnt[TM_STATIC_MAX_CELLS + 1];
+  int32_t cell_start[TM_STATIC_MAX_CELLS + 1];
+  tm_grid grid;
+  tm_dev_status status;
+  int32_t off[2];
+  int32_t ncell;
+  int32_t ncell_m;
+  int32_t need[2];
+};
+
+// Every call shares this array; it keeps the previous call's contents.
+static __device__ __align__(256) StaticScratch g_static_scratch;
+
+constexpr int kMaxDevices = 64;
+StaticScratch* g_static_ptr[kMaxDevices] = {};
+
+__global__ void k_static_init(StaticScratch* s, int N) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) s->mol[i] = 0;
+  if (i == 0) {
+    s->off[0] = 0;
+    s->off[1] = N;
+    s->need[0] = 0;
+    s->need[1] = 0;
+    s->status.code = 0;
+    s->status.detail = 0;
+    s->status.where = 0;
+  }
+}
+
+// single-block exclusive scan of n <= 1024 * 80 ints (the cell counts)
+__global__ void k_scan_single(const int32_t* __restrict__ in, int32_t* __restrict__ out, int n) {
+  __shared__ int32_t part[1024];
+  const int per = (n + 1023) / 1024;
+  const int b = threadIdx.x * per;
+  int32_t sum = 0;
+  for (int q = 0; q < per; ++q)
+    if (b + q < n) sum += in[b + q];
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    const int32_t t = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+    __syncthreads();
+    part[threadIdx.x] += t;
+    __syncthreads();
+  }
+  int32_t run = part[threadIdx.x] - sum;
+  for (int q = 0; q < per; ++q)
+    if (b + q < n) {
+      out[b + q] = run;
+      run += in[b + q];
+    }
+}
+
+}  // namespace
+
+extern "C" int tm_nlist_build_static(const double* x, const int32_t* elem, int natoms,
+                                     double r_rc, double a_rc, int32_t* cnt_r, uint32_t* nbr_r,
+                                     int KR, int32_t* cnt_a, uint32_t* nbr_a, int KA,
+                                     int32_t needed[2], void* stream) {
+  if (!x || !elem || !cnt_r || !nbr_r || !cnt_a || !nbr_a || natoms <= 0 || KR <= 0 || KA <= 0)
+    return TM_E_ARG;
+  if (natoms > TM_STATIC_MAX_ATOMS) return TM_E_ARG;          // beyond the fixed scratch
+  if (!(a_rc > 0.0 && a_rc <= r_rc)) return TM_E_ARG;
+  if ((size_t)4 * (KR + KA) * sizeof(uint64_t) > 200 * 1024) return TM_E_ARG;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return TM_E_CUDA;
+  // first call on this device: resolve the device address of the scratch
+  // (the host-side symbol is only a stand-in and must never reach a kernel)
+  if (!g_static_ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_static_scratch) != cudaSuccess || !p) return TM_E_CUDA;
+    g_static_ptr[dev] = static_cast<StaticScratch*>(p);
+  }
+  StaticScratch* S = g_static_ptr[dev];
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int N = natoms;
+  const int cap = 2 * N + 64;
+  k_static_init<<<tm_div_up(N, 256), 256, 0, st>>>(S, N);
+  k_positions<<<tm_div_up(N, 256), 256, 0, st>>>(x, elem, S->xhi, S->xlo, N, &S->status);
+  k_grid_setup<<<1, 256, 0, st>>>(x, S->off, &S->grid, &S->ncell_m, r_rc, 0, 0.0, 0.0, 0.0, 0.0,
+                                  2.0, 64.0, 0, 0, 0);
+  k_grid_offsets<<<1, 32, 0, st>>>(&S->grid, &S->ncell_m, 1, &S->ncell, cap, &S->status);
+  cudaMemsetAsync(S->cell_cnt, 0, sizeof(int32_t) * (cap + 1), st);
+  k_cell_count<<<tm_div_up(N, 256), 256, 0, st>>>(x, S->mol, &S->grid, S->cell_cnt, S->cell_of_atom,
+                                                   N, cap, &S->status);
+  k_scan_single<<<1, 1024, 0, st>>>(S->cell_cnt, S->cell_start, cap + 1);
+  cudaMemsetAsync(S->cell_cnt, 0, sizeof(int32_t) * (cap + 1), st);
+  k_cell_fill<<<tm_div_up(N, 256), 256, 0, st>>>(S->cell_of_atom, S->cell_start, S->cell_cnt,
+                                                  S->cell_atoms, N);
+  k_cell_sort<<<tm_div_up(cap, 128), 128, 0, st>>>(S->cell_start, S->cell_atoms, &S->ncell, cap);
+  NbrArgs a;
+  a.x = x; a.xhi = S->xhi; a.xlo = S->xlo; a.mol = S->mol; a.elem = elem; a.grid = &S->grid;
+  a.cell_of = S->cell_of_atom; a.cell_start = S->cell_start; a.cell_atoms = S->cell_atoms;
+  a.cnt_r = cnt_r; a.cnt_a = cnt_a; a.nbr_r = nbr_r; a.nbr_a = nbr_a; a.need = S->need;
+  a.N = N; a.KR = KR; a.KA = KA; a.rr = r_rc; a.ra = a_rc;
+  a.rr2_lo = (float)(r_rc * r_rc) * (1.f - kBand);
+  a.rr2_hi = (float)(r_rc * r_rc) * (1.f + kBand);
+  a.ra2_lo = (float)(a_rc * a_rc) * (1.f - kBand);
+  a.ra2_hi = (float)(a_rc * a_rc) * (1.f + kBand);
+  for (int q = 0; q < 9; ++q) a.lat[q] = 0.0;
+  const size_t shm = (size_t)4 * (KR + KA) * sizeof(uint64_t);
+  if (shm > 48 * 1024)
+    cudaFuncSetAttribute(k_nbr_build<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  k_nbr_build<false><<<tm_div_up(N, 4), 128, shm, st>>>(a);
+  if (cudaGetLastError() != cudaSuccess) return TM_E_CUDA;
+  // the counters the caller needs to size its rows, and the status word
+  int32_t h[2] = {0, 0};
+  tm_dev_status hs;
+  if (cudaMemcpyAsync(h, S->need, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(&hs, &S->status, sizeof(hs), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return TM_E_CUDA;
+  if (needed) {
+    needed[0] = h[0];
+    needed[1] = h[1];
+  }
+  if (hs.code) return hs.code;
+  if (h[0] > KR || h[1] > KA) return TM_E_CAPACITY;
+  return TM_OK;
+}
