@@ -464,7 +464,10 @@ extern "C" int tm_system_create(tm_model* m, int N, int nmol, const int32_t* Z,
   // Coulomb grid: about 24 atoms per cell; a periodic edge gets the fewest
   // cells of at least that size for which the +-R cell search visits no cell
   // twice (2R + 1 <= n)
-  s->ecell_cap = N + 64 * nmol;
+  // open: at most n/8 + 8 cells per molecule (the device grows the cell size
+  // until a molecule fits, with the same bound)
+  s->ecell_cap = 0;
+  for (int q = 0; q < nmol; ++q) s->ecell_cap += (int)((off[q + 1] - off[q]) / 8) + 8;
   if (s->periodic) {
     const double vol = s->lat[0] * s->lat[4] * s->lat[8];
     const double cs = std::max(2.0, cbrt(24.0 * vol / N));
@@ -478,6 +481,15 @@ extern "C" int tm_system_create(tm_model* m, int N, int nmol, const int32_t* Z,
     }
     s->ecell_cap = (int)nc;
   }
+  std::vector<int2> chunks;
+  std::vector<int32_t> mol_chunk(nmol + 1, 0);
+  for (int q = 0; q < nmol; ++q) {
+    mol_chunk[q] = (int32_t)chunks.size();
+    for (int64_t b = off[q]; b < off[q + 1]; b += 1024)
+      chunks.push_back(make_int2((int)b, (int)std::min<int64_t>(b + 1024, off[q + 1])));
+  }
+  mol_chunk[nmol] = (int32_t)chunks.size();
+  s->nchunk = (int)chunks.size();
   const int H = m->H, Dp = k.Dp;
   const size_t es = m->elem_size;
   const size_t Mp = s->Mpad;
@@ -501,6 +513,10 @@ extern "C" int tm_system_create(tm_model* m, int N, int nmol, const int32_t* Z,
   A.get(&s->d_cell_start, sizeof(int32_t) * (s->ncell_cap + 1));
   A.get(&s->d_cell_atoms, sizeof(int32_t) * N);
   A.get(&s->d_cell_of_atom, sizeof(int32_t) * N);
+  A.get(&s->d_chunk, sizeof(int2) * s->nchunk);
+  A.get(&s->d_mol_chunk, sizeof(int32_t) * (nmol + 1));
+  A.get(&s->d_part, sizeof(double) * 8 * s->nchunk);
+  A.get(&s->d_cbox, sizeof(float) * 8 * s->nchunk);
   A.get(&s->d_egrid, sizeof(tm_grid) * nmol);
   A.get(&s->d_encell, sizeof(int32_t));
   A.get(&s->d_encell_m, sizeof(int32_t) * nmol);
@@ -511,6 +527,7 @@ extern "C" int tm_system_create(tm_model* m, int N, int nmol, const int32_t* Z,
   A.get(&s->d_epos, sizeof(int32_t) * N);
   A.get(&s->d_exhi, sizeof(float4) * N);
   A.get(&s->d_exlo, sizeof(float4) * N);
+  A.get(&s->d_cpart, sizeof(float4) * 2 * (size_t)TM_EE_SPLIT * N);
   A.get(&s->d_cnt_r, sizeof(int32_t) * N);
   A.get(&s->d_cnt_a, sizeof(int32_t) * N);
   A.get(&s->d_nbr_r, sizeof(uint32_t) * (size_t)N * s->KR);
@@ -553,6 +570,9 @@ extern "C" int tm_system_create(tm_model* m, int N, int nmol, const int32_t* Z,
   cudaMemcpyAsync(s->d_elem, s->elem_h.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(s->d_mol, mol.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(s->d_off, off32.data(), sizeof(int32_t) * (nmol + 1), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s->d_chunk, chunks.data(), sizeof(int2) * s->nchunk, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s->d_mol_chunk, mol_chunk.data(), sizeof(int32_t) * (nmol + 1),
+                  cudaMemcpyHostToDevice, st);
   for (int h = 0; h < 2; ++h) {
     if (m->desc.precision == TM_PREC_BF16 && h == 1) break;
     cudaMemsetAsync(s->G[h], 0, Mp * Dp * es, st);
@@ -582,8 +602,10 @@ static void system_free(tm_system* s) {
   // sizes are not needed by cudaFreeAsync; budget accounting uses s->bytes
   void* ptrs[] = {s->row_of_atom, s->atom_of_row, s->tile_elem, s->d_Z, s->d_elem, s->d_mol,
                   s->d_off, s->d_x, s->d_xhi, s->d_xlo, s->d_x_at_build, s->d_grid, s->d_ncell, s->d_ncell_m, s->d_need,
+                  s->d_chunk, s->d_mol_chunk, s->d_part, s->d_cbox,
                   s->d_egrid, s->d_encell, s->d_encell_m, s->d_ecell_cnt, s->d_ecell_start,
                   s->d_ecell_atoms, s->d_ecell_of_atom, s->d_epos, s->d_exhi, s->d_exlo,
+                  s->d_cpart,
                   s->d_cell_cnt, s->d_cell_start, s->d_cell_atoms, s->d_cell_of_atom, s->d_cnt_r,
                   s->d_cnt_a, s->d_nbr_r, s->d_nbr_a, s->d_rev_r, s->d_rev_a, s->d_sr, s->d_va,
                   s->dEdG, s->epart, s->d_Eatom, s->d_qraw, s->d_q, s->d_dEdq, s->d_fself,

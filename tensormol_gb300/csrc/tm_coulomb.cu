@@ -38,31 +38,45 @@ __global__ void k_mlp_finish(const float* __restrict__ epart, const double* __re
   qraw[i] = (float)q;
 }
 
-// block per molecule: aux[m][0] = sum q_raw, mol_E[m][1] = Ebp
-__global__ void k_mol_sum1(const int32_t* __restrict__ off, const double* __restrict__ Eatom,
-                           const float* __restrict__ qraw, double* __restrict__ molE,
-                           double* __restrict__ aux) {
-  const int m = blockIdx.x;
-  __shared__ double s0[256], s1[256];
-  double a = 0.0, b = 0.0;
-  for (int i = off[m] + threadIdx.x; i < off[m + 1]; i += blockDim.x) {
-    a += Eatom[i];
-    b += (double)qraw[i];
-  }
-  s0[threadIdx.x] = a;
-  s1[threadIdx.x] = b;
+// Per-molecule sums in two fixed-order levels: one block per chunk of at most
+// 1024 atoms of one molecule, then one thread per molecule over its chunks.
+template <int NV>
+__device__ __forceinline__ void block_sum_store(double (&v)[NV], double* __restrict__ dst) {
+  __shared__ double sh[NV][256];
+  for (int c = 0; c < NV; ++c) sh[c][threadIdx.x] = v[c];
   __syncthreads();
   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o) {
-      s0[threadIdx.x] += s0[threadIdx.x + o];
-      s1[threadIdx.x] += s1[threadIdx.x + o];
-    }
+    if (threadIdx.x < o)
+      for (int c = 0; c < NV; ++c) sh[c][threadIdx.x] += sh[c][threadIdx.x + o];
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    molE[4 * m + 1] = s0[0];
-    aux[8 * m + 0] = s1[0];
+  if (threadIdx.x == 0)
+    for (int c = 0; c < NV; ++c) dst[c] = sh[c][0];
+}
+
+// chunk partials [c][0] = sum Eatom, [c][1] = sum q_raw
+__global__ void k_chunk_sum1(const int2* __restrict__ chunk, const double* __restrict__ Eatom,
+                             const float* __restrict__ qraw, double* __restrict__ part) {
+  const int2 ch = chunk[blockIdx.x];
+  double v[2] = {0.0, 0.0};
+  for (int i = ch.x + threadIdx.x; i < ch.y; i += blockDim.x) {
+    v[0] += Eatom[i];
+    v[1] += (double)qraw[i];
   }
+  block_sum_store<2>(v, part + 8 * (size_t)blockIdx.x);
+}
+
+__global__ void k_mol_final1(const int32_t* __restrict__ mol_chunk, const double* __restrict__ part,
+                             double* __restrict__ molE, double* __restrict__ aux, int nmol) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nmol) return;
+  double e = 0.0, q = 0.0;
+  for (int c = mol_chunk[m]; c < mol_chunk[m + 1]; ++c) {
+    e += part[8 * (size_t)c];
+    q += part[8 * (size_t)c + 1];
+  }
+  molE[4 * m + 1] = e;
+  aux[8 * m + 0] = q;
 }
 
 __global__ void k_neutralize(const int32_t* __restrict__ mol, const int32_t* __restrict__ off,
@@ -91,10 +105,12 @@ struct CoulArgs {
   double* ecv;              // [N][2]
   float* dEdqt;             // [N]  dE/d q~_i
   float4* fcv;              // [N]  dE/dx_i of the pair terms
+  float4* part;             // [TM_EE_SPLIT][N][2] partial sums per stencil split
+  int natoms;
   int ref_periodic;         // image pairs contribute half the force (reference gradient)
   int periodic;
   double ree;
-  float ree2, ree2_lo, ree2_hi;
+  float ree2, ree2_lo, ree2_hi, ree2_screen;
   double lat[9];
   float sh_hi[27][3];
   float sh_lo[27][3];
@@ -163,7 +179,8 @@ __device__ __forceinline__ PairOut pair_terms(float r, float qi, float qj, int e
 __global__ void __launch_bounds__(128) k_coulomb(const CoulArgs a, const tm_consts k) {
   __shared__ float4 sh[4][2][32];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int c = blockIdx.x * (blockDim.x >> 5) + wib;
+  const int wg = blockIdx.x * (blockDim.x >> 5) + wib;
+  const int c = wg / TM_EE_SPLIT, split = wg % TM_EE_SPLIT;
   if (c >= a.ncell_cap || c >= *a.ncell) return;
   const int t0 = a.cell_start[c], t1 = a.cell_start[c + 1];
   if (t1 <= t0) return;
@@ -182,9 +199,12 @@ __global__ void __launch_bounds__(128) k_coulomb(const CoulArgs a, const tm_cons
     const int ei = __float_as_int(hi.w);
     const float qi = lo.w;
     float acc_cc = 0.f, acc_vdw = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
-    for (int ox = -Rx; ox <= Rx; ++ox) {
+    // this warp's share of the stencil: every TM_EE_SPLIT-th (ox, oy) column
+    const int ncol = (2 * Rx + 1) * (2 * Ry + 1);
+    for (int col = split; col < ncol; col += TM_EE_SPLIT) {
+      const int ox = col / (2 * Ry + 1) - Rx, oy = col % (2 * Ry + 1) - Ry;
       const float gapx = fmaxf(0.f, (float)(abs(ox) - 1)) * cx;
-      for (int oy = -Ry; oy <= Ry; ++oy) {
+      {
         const float gapy = fmaxf(0.f, (float)(abs(oy) - 1)) * cy;
         for (int oz = -Rz; oz <= Rz; ++oz) {
           const float gapz = fmaxf(0.f, (float)(abs(oz) - 1)) * cz;
@@ -212,8 +232,19 @@ __global__ void __launch_bounds__(128) k_coulomb(const CoulArgs a, const tm_cons
             }
             __syncwarp();
             if (!have) continue;
+            // cheap screen on the FP32 hi parts (error well below the margin
+            // in ree2_screen); only candidates that pass take the accurate path
+            uint32_t mask = 0;
             for (int q = 0; q < nj; ++q) {
-              if (cj == c && jb + q == ti && r == TM_IMG_SELF) continue;   // the atom itself
+              const float4 hj = sj_hi[q];
+              const float ex = hi.x - hj.x - shx, ey = hi.y - hj.y - shy, ez = hi.z - hj.z - shz;
+              if (ex * ex + ey * ey + ez * ez <= a.ree2_screen) mask |= 1u << q;
+            }
+            if (cj == c && r == TM_IMG_SELF && ti >= jb && ti < jb + nj)
+              mask &= ~(1u << (ti - jb));                                   // the atom itself
+            while (mask) {
+              const int q = __ffs(mask) - 1;
+              mask &= mask - 1;
               const float4 hj = sj_hi[q], lj = sj_lo[q];
               const float dx = ds_sub_shift(hi.x, lo.x, hj.x, lj.x, shx, slx);
               const float dy = ds_sub_shift(hi.y, lo.y, hj.y, lj.y, shy, sly);
@@ -245,24 +276,42 @@ __global__ void __launch_bounds__(128) k_coulomb(const CoulArgs a, const tm_cons
       }
     }
     if (have) {
-      const int i = a.eatom[ti];
-      a.ecv[2 * i + 0] = 0.5 * (double)qi * (double)acc_cc;
-      a.ecv[2 * i + 1] = 0.5 * (double)acc_vdw;
-      a.dEdqt[i] = acc_cc;
-      a.fcv[i] = make_float4(gx, gy, gz, 0.f);
+      float4* dst = a.part + 2 * ((size_t)split * a.natoms + ti);
+      dst[0] = make_float4(acc_cc, acc_vdw, gx, gy);
+      dst[1] = make_float4(gz, 0.f, 0.f, 0.f);
     }
   }
 }
 
-// block per molecule: Ecc, Evdw, Etotal, dipole, sum dE/dq~
-__global__ void k_mol_sum2(const int32_t* __restrict__ off, const double* __restrict__ ecv,
-                           const float* __restrict__ dEdqt, const float* __restrict__ q,
-                           const double* __restrict__ x, double bohr, double* __restrict__ molE,
-                           double* __restrict__ aux) {
-  const int m = blockIdx.x;
-  __shared__ double s[6][256];
+// Per atom (cell order): the stencil splits' partial sums added in split order.
+__global__ void k_coulomb_finish(const CoulArgs a) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.natoms) return;
+  float cc = 0.f, vdw = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
+  for (int s = 0; s < TM_EE_SPLIT; ++s) {
+    const float4* src = a.part + 2 * ((size_t)s * a.natoms + p);
+    const float4 u = src[0], v = src[1];
+    cc += u.x;
+    vdw += u.y;
+    gx += u.z;
+    gy += u.w;
+    gz += v.x;
+  }
+  const int i = a.eatom[p];
+  const float qi = a.exlo[p].w;
+  a.ecv[2 * i + 0] = 0.5 * (double)qi * (double)cc;
+  a.ecv[2 * i + 1] = 0.5 * (double)vdw;
+  a.dEdqt[i] = cc;
+  a.fcv[i] = make_float4(gx, gy, gz, 0.f);
+}
+
+// chunk partials: Ecc, Evdw, sum dE/dq~, dipole xyz
+__global__ void k_chunk_sum2(const int2* __restrict__ chunk, const double* __restrict__ ecv,
+                             const float* __restrict__ dEdqt, const float* __restrict__ q,
+                             const double* __restrict__ x, double bohr, double* __restrict__ part) {
+  const int2 ch = chunk[blockIdx.x];
   double v[6] = {0, 0, 0, 0, 0, 0};
-  for (int i = off[m] + threadIdx.x; i < off[m + 1]; i += blockDim.x) {
+  for (int i = ch.x + threadIdx.x; i < ch.y; i += blockDim.x) {
     v[0] += ecv[2 * i];
     v[1] += ecv[2 * i + 1];
     v[2] += (double)dEdqt[i];
@@ -271,22 +320,23 @@ __global__ void k_mol_sum2(const int32_t* __restrict__ off, const double* __rest
     v[4] += qq * x[3 * i + 1] * bohr;
     v[5] += qq * x[3 * i + 2] * bohr;
   }
-  for (int c = 0; c < 6; ++c) s[c][threadIdx.x] = v[c];
-  __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o)
-      for (int c = 0; c < 6; ++c) s[c][threadIdx.x] += s[c][threadIdx.x + o];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    molE[4 * m + 2] = s[0][0];
-    molE[4 * m + 3] = s[1][0];
-    molE[4 * m + 0] = molE[4 * m + 1] + s[0][0] + s[1][0];
-    aux[8 * m + 1] = s[2][0];
-    aux[8 * m + 2] = s[3][0];
-    aux[8 * m + 3] = s[4][0];
-    aux[8 * m + 4] = s[5][0];
-  }
+  block_sum_store<6>(v, part + 8 * (size_t)blockIdx.x);
+}
+
+__global__ void k_mol_final2(const int32_t* __restrict__ mol_chunk, const double* __restrict__ part,
+                             double* __restrict__ molE, double* __restrict__ aux, int nmol) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nmol) return;
+  double v[6] = {0, 0, 0, 0, 0, 0};
+  for (int c = mol_chunk[m]; c < mol_chunk[m + 1]; ++c)
+    for (int t = 0; t < 6; ++t) v[t] += part[8 * (size_t)c + t];
+  molE[4 * m + 2] = v[0];
+  molE[4 * m + 3] = v[1];
+  molE[4 * m + 0] = molE[4 * m + 1] + v[0] + v[1];
+  aux[8 * m + 1] = v[2];
+  aux[8 * m + 2] = v[3];
+  aux[8 * m + 3] = v[4];
+  aux[8 * m + 4] = v[5];
 }
 
 // dE/dq_i = dE/dq~_i - (1/N) sum_k dE/dq~_k (adjoint of the neutralisation)
@@ -310,12 +360,13 @@ int tm_launch_mlp_finish(tm_system* s) {
   k_mlp_finish<<<tm_div_up(s->N, 256), 256, 0, ctx->stream>>>(
       s->epart, m->bout, s->row_of_atom, s->d_elem, nsplit, s->Mpad, m->k.nele, s->N, s->d_Eatom,
       s->d_qraw);
-  k_mol_sum1<<<s->nmol, 256, 0, ctx->stream>>>(s->d_off, s->d_Eatom, s->d_qraw, s->d_mol_E,
-                                               s->d_mol_aux);
+  k_chunk_sum1<<<s->nchunk, 256, 0, ctx->stream>>>(s->d_chunk, s->d_Eatom, s->d_qraw, s->d_part);
+  k_mol_final1<<<tm_div_up(s->nmol, 128), 128, 0, ctx->stream>>>(s->d_mol_chunk, s->d_part,
+                                                                 s->d_mol_E, s->d_mol_aux, s->nmol);
   k_neutralize<<<tm_div_up(s->N, 256), 256, 0, ctx->stream>>>(s->d_mol, s->d_off, s->d_qraw,
                                                               s->d_mol_aux, s->d_q, s->d_epos,
                                                               s->d_exlo, s->N);
-  ctx->launches += 3;
+  ctx->launches += 4;
   return tm_cuda_check(ctx, cudaGetLastError(), "mlp finish");
 }
 
@@ -326,19 +377,27 @@ int tm_launch_coulomb(tm_system* s, unsigned flags) {
   a.x = s->d_x; a.exhi = s->d_exhi; a.exlo = s->d_exlo; a.eatom = s->d_ecell_atoms;
   a.mol = s->d_mol; a.grid = s->d_egrid; a.cell_start = s->d_ecell_start; a.ncell = s->d_encell;
   a.ncell_cap = s->ecell_cap; a.ecv = s->d_ecv; a.dEdqt = s->d_dEdq; a.fcv = s->d_fcv;
+  a.part = s->d_cpart; a.natoms = s->N;
   a.ref_periodic = (s->periodic && (flags & TM_F_REFERENCE_PERIODIC_FORCE)) ? 1 : 0;
   a.periodic = s->periodic ? 1 : 0;
   a.ree = k.ree_d;
   a.ree2 = (float)(k.ree_d * k.ree_d);
   a.ree2_lo = a.ree2 * (1.f - kBand);
   a.ree2_hi = a.ree2 * (1.f + kBand);
+  // hi parts of coordinates below 1e4 A are within 5e-4 A of the truth, so a
+  // hi-part distance errs by under 2e-3 A, inside this margin
+  a.ree2_screen = (float)((k.ree_d * (1.0 + 1e-4) + 5e-3) * (k.ree_d * (1.0 + 1e-4) + 5e-3));
   for (int q = 0; q < 9; ++q) a.lat[q] = s->lat[q];
   tm_fill_shifts(s, a.sh_hi, a.sh_lo);
-  k_coulomb<<<tm_div_up(s->ecell_cap, 4), 128, 0, ctx->stream>>>(a, k);
-  k_mol_sum2<<<s->nmol, 256, 0, ctx->stream>>>(s->d_off, s->d_ecv, s->d_dEdq, s->d_q, s->d_x,
-                                               (double)k.bohr, s->d_mol_E, s->d_mol_aux);
+  k_coulomb<<<tm_div_up(s->ecell_cap * TM_EE_SPLIT, 4), 128, 0, ctx->stream>>>(a, k);
+  k_coulomb_finish<<<tm_div_up(s->N, 256), 256, 0, ctx->stream>>>(a);
+  ctx->launches++;
+  k_chunk_sum2<<<s->nchunk, 256, 0, ctx->stream>>>(s->d_chunk, s->d_ecv, s->d_dEdq, s->d_q,
+                                                   s->d_x, 1.889725989, s->d_part);
+  k_mol_final2<<<tm_div_up(s->nmol, 128), 128, 0, ctx->stream>>>(s->d_mol_chunk, s->d_part,
+                                                                 s->d_mol_E, s->d_mol_aux, s->nmol);
   k_dq<<<tm_div_up(s->N, 256), 256, 0, ctx->stream>>>(s->d_mol, s->d_off, s->d_mol_aux, s->d_dEdq,
                                                       s->N);
-  ctx->launches += 3;
+  ctx->launches += 4;
   return tm_cuda_check(ctx, cudaGetLastError(), "coulomb");
 }

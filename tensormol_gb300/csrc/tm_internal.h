@@ -15,6 +15,7 @@
 #define TM_MAX_HIDDEN 4
 #define TM_BN 256          // GEMM N tile
 #define TM_BM 128          // GEMM M tile (rows per element are padded to this)
+#define TM_EE_SPLIT 8      // warps sharing one Coulomb cell's candidate stencil
 
 // Constants of the model read by the device kernels (passed by value).
 struct tm_consts {
@@ -132,6 +133,7 @@ struct tm_system {
   int32_t* d_epos = nullptr;           // [N] position of an atom in cell order
   float4* d_exhi = nullptr;            // [N] cell-ordered hi parts (w = element)
   float4* d_exlo = nullptr;            // [N] cell-ordered lo parts (w = charge)
+  float4* d_cpart = nullptr;           // [TM_EE_SPLIT][N][2] pair-term partial sums
   // neighbour lists (ELL, per centre sorted by (element, reference index))
   int KR = 64, KA = 48;
   int32_t* d_cnt_r = nullptr;
@@ -162,6 +164,12 @@ struct tm_system {
   double* d_F = nullptr;               // [N][3] force (J/mol/A)
   double* d_mol_E = nullptr;           // [nmol][4]
   double* d_mol_aux = nullptr;         // [nmol][8]: sum q, sum dEdq~, dipole xyz
+  // chunks of at most 1024 atoms of one molecule (two-level reductions)
+  int nchunk = 0;
+  int2* d_chunk = nullptr;             // [nchunk] (begin, end)
+  int32_t* d_mol_chunk = nullptr;      // [nmol+1] first chunk of each molecule
+  double* d_part = nullptr;            // [nchunk][8] partial sums
+  float* d_cbox = nullptr;             // [nchunk][8] partial bounding boxes
   // export scratch
   int64_t* d_exp_off = nullptr;        // [N+1]
   size_t bytes = 0;

@@ -46,6 +46,10 @@ __global__ void k_positions(const double* __restrict__ x, const int32_t* __restr
 // ---------------------------------------------------------------------------
 // per-molecule grid set-up (block per molecule)
 // ---------------------------------------------------------------------------
+__device__ tm_grid grid_from_bbox(double* mn, double* mx, int a0, int a1, double rc, int periodic,
+                                  double Lx, double Ly, double Lz, double occ, double cap_a,
+                                  double cap_c, int pnx, int pny, int pnz);
+
 // rc: smallest cell edge. occ > 0 sizes open-boundary cells for about occ
 // atoms each (Coulomb grid); cap_a * n + cap_c bounds the cells of a molecule.
 // Periodic grids take pn[] cells per edge when given, else floor(L / rc).
@@ -78,6 +82,18 @@ __global__ void k_grid_setup(const double* __restrict__ x, const int32_t* __rest
     for (int d = 0; d < 3; ++d) {
       for (int q = 1; q < nw; ++q) { mn[d] = fmin(mn[d], smin[d][q]); mx[d] = fmax(mx[d], smax[d][q]); }
     }
+    grid[m] = grid_from_bbox(mn, mx, a0, a1, rc, periodic, Lx, Ly, Lz, occ, cap_a, cap_c, pnx, pny, pnz);
+    ncell_m[m] = grid[m].nx * grid[m].ny * grid[m].nz;
+  }
+}
+
+// Grid of one molecule from its bounding box (see k_grid_setup for the
+// parameters). Open-boundary cells start at rc (or at the occupancy-based size)
+// and grow by 1.25x until the molecule has at most cap_a * n + cap_c cells.
+__device__ tm_grid grid_from_bbox(double* mn, double* mx, int a0, int a1, double rc, int periodic,
+                                  double Lx, double Ly, double Lz, double occ, double cap_a,
+                                  double cap_c, int pnx, int pny, int pnz) {
+  {
     tm_grid g;
     g.atom_off = a0;
     g.natom = a1 - a0;
@@ -117,9 +133,69 @@ __global__ void k_grid_setup(const double* __restrict__ x, const int32_t* __rest
       if ((double)g.nx * g.ny * g.nz > cap) g.nx = g.ny = g.nz = 1;
     }
     g.cell_off = 0;
-    grid[m] = g;
-    ncell_m[m] = g.nx * g.ny * g.nz;
+    return g;
   }
+}
+
+// Partial bounding boxes of chunks (<= 1024 atoms of one molecule) from the
+// FP32 hi parts: the grid origin only has to be close to the minimum, since an
+// atom a rounding error outside the box is clamped into the edge cell, which
+// keeps every pair within the cutoff in adjacent cells.
+__global__ void k_cbox_chunks(const int2* __restrict__ chunk, const float4* __restrict__ xhi,
+                              float* __restrict__ cbox) {
+  const int2 ch = chunk[blockIdx.x];
+  float mn[3] = {3e38f, 3e38f, 3e38f}, mx[3] = {-3e38f, -3e38f, -3e38f};
+  for (int a = ch.x + threadIdx.x; a < ch.y; a += blockDim.x) {
+    const float4 h = xhi[a];
+    mn[0] = fminf(mn[0], h.x); mx[0] = fmaxf(mx[0], h.x);
+    mn[1] = fminf(mn[1], h.y); mx[1] = fmaxf(mx[1], h.y);
+    mn[2] = fminf(mn[2], h.z); mx[2] = fmaxf(mx[2], h.z);
+  }
+  __shared__ float sh[6][8];
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  for (int d = 0; d < 3; ++d) {
+    for (int o = 16; o > 0; o >>= 1) {
+      mn[d] = fminf(mn[d], __shfl_xor_sync(TM_FULL, mn[d], o));
+      mx[d] = fmaxf(mx[d], __shfl_xor_sync(TM_FULL, mx[d], o));
+    }
+    if (l == 0) { sh[d][w] = mn[d]; sh[3 + d][w] = mx[d]; }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int d = 0; d < 3; ++d) {
+      for (int q = 1; q < (int)(blockDim.x >> 5); ++q) {
+        mn[d] = fminf(mn[d], sh[d][q]);
+        mx[d] = fmaxf(mx[d], sh[3 + d][q]);
+      }
+      cbox[8 * blockIdx.x + d] = mn[d];
+      cbox[8 * blockIdx.x + 3 + d] = mx[d];
+    }
+  }
+}
+
+// One thread per molecule: combine its chunk boxes (widened by a relative
+// 1e-6 + 1e-5 A margin) and set up the grid.
+__global__ void k_grid_from_chunks(const float* __restrict__ cbox, const int32_t* __restrict__ mol_chunk,
+                                   const int32_t* __restrict__ off, tm_grid* __restrict__ grid,
+                                   int32_t* __restrict__ ncell_m, int nmol, double rc, int periodic,
+                                   double Lx, double Ly, double Lz, double occ, double cap_a,
+                                   double cap_c, int pnx, int pny, int pnz) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nmol) return;
+  double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+  for (int c = mol_chunk[m]; c < mol_chunk[m + 1]; ++c)
+    for (int d = 0; d < 3; ++d) {
+      mn[d] = fmin(mn[d], (double)cbox[8 * c + d]);
+      mx[d] = fmax(mx[d], (double)cbox[8 * c + 3 + d]);
+    }
+  for (int d = 0; d < 3; ++d) {
+    mn[d] -= 1e-5 + 1e-6 * fabs(mn[d]);
+    mx[d] += 1e-5 + 1e-6 * fabs(mx[d]);
+  }
+  const tm_grid g = grid_from_bbox(mn, mx, off[m], off[m + 1], rc, periodic, Lx, Ly, Lz, occ,
+                                   cap_a, cap_c, pnx, pny, pnz);
+  grid[m] = g;
+  ncell_m[m] = g.nx * g.ny * g.nz;
 }
 
 __device__ __forceinline__ int cell_coord(double v, double o, double c, int n) {
@@ -718,9 +794,11 @@ int tm_launch_nlist(tm_system* s) {
   const tm_consts& k = s->model->k;
   int rc;
   if ((rc = tm_launch_positions(s))) return rc;
-  k_grid_setup<<<s->nmol, 256, 0, st>>>(s->d_x, s->d_off, s->d_grid, s->d_ncell_m, k.r_rc_d,
-                                          s->periodic ? 1 : 0, s->lat[0], s->lat[4], s->lat[8],
-                                          0.0, 2.0, 64.0, 0, 0, 0);
+  k_cbox_chunks<<<s->nchunk, 256, 0, st>>>(s->d_chunk, s->d_xhi, s->d_cbox);
+  k_grid_from_chunks<<<tm_div_up(s->nmol, 128), 128, 0, st>>>(
+      s->d_cbox, s->d_mol_chunk, s->d_off, s->d_grid, s->d_ncell_m, s->nmol, k.r_rc_d,
+      s->periodic ? 1 : 0, s->lat[0], s->lat[4], s->lat[8], 0.0, 2.0, 64.0, 0, 0, 0);
+  ctx->launches++;
   k_grid_offsets<<<1, 32, 0, st>>>(s->d_grid, s->d_ncell_m, s->nmol, s->d_ncell, s->ncell_cap,
                                    ctx->d_status);
   ctx->launches += 2;
@@ -755,9 +833,10 @@ int tm_launch_nlist(tm_system* s) {
                                                     s->d_mol, s->d_off, s->N, s->KA);
   ctx->launches += 3;
   // Coulomb grid: about 24 atoms per cell, atoms packed in cell order
-  k_grid_setup<<<s->nmol, 256, 0, st>>>(s->d_x, s->d_off, s->d_egrid, s->d_encell_m, 2.0,
-                                          s->periodic ? 1 : 0, s->lat[0], s->lat[4], s->lat[8],
-                                          24.0, 1.0, 64.0, s->ee_dims[0], s->ee_dims[1], s->ee_dims[2]);
+  k_grid_from_chunks<<<tm_div_up(s->nmol, 128), 128, 0, st>>>(
+      s->d_cbox, s->d_mol_chunk, s->d_off, s->d_egrid, s->d_encell_m, s->nmol, 2.0,
+      s->periodic ? 1 : 0, s->lat[0], s->lat[4], s->lat[8], 24.0, 0.125, 8.0, s->ee_dims[0],
+      s->ee_dims[1], s->ee_dims[2]);
   k_grid_offsets<<<1, 32, 0, st>>>(s->d_egrid, s->d_encell_m, s->nmol, s->d_encell, s->ecell_cap,
                                    ctx->d_status);
   cudaMemsetAsync(s->d_ecell_cnt, 0, sizeof(int32_t) * (s->ecell_cap + 1), st);
