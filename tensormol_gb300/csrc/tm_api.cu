@@ -76,7 +76,12 @@ extern "C" int tm_ctx_create(int device, size_t budget, tm_ctx** out) {
   c->device = device;
   c->budget = budget;
   int rc;
-  if ((rc = tm_cuda_check(c, cudaSetDevice(device), "cudaSetDevice"))) { delete c; return rc; }
+  if ((rc = tm_cuda_check(c, cudaSetDevice(device), "cudaSetDevice")) ||
+      (rc = tm_cuda_check(c, cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount,
+                                                    device), "SM count"))) {
+    delete c;
+    return rc;
+  }
   if ((rc = tm_cuda_check(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream"))) {
     delete c;
     return rc;

@@ -52,6 +52,7 @@ struct GemmArgs {
   const void* hprev0;
   const void* hprev1;
   tm_dev_status* st;
+  int mtiles, ntiles;   // tiles per net along M and N
 };
 
 // ---- PTX wrappers ---------------------------------------------------------
@@ -258,10 +259,20 @@ struct Cfg {
   static constexpr int B_TILE = BN * 128;             // 32 KB
   static constexpr int STAGE = NSPLIT * (A_TILE + B_TILE);
   static constexpr int NSTAGE = PREC == TM_PREC_FP32 ? 2 : 4;
-  static constexpr int SMEM = NSTAGE * STAGE + 1024 + 256;
+  static constexpr int SMEM = NSTAGE * STAGE + 1024 + 256;   // stages, alignment, barriers
   static constexpr uint32_t IDESC = make_idesc(PREC == TM_PREC_FP32 ? 2 : 1, BM, BN);
 };
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+
+// Persistent, warp-specialised layer kernel. Each CTA walks tiles
+// t = blockIdx.x, blockIdx.x + gridDim.x, ... in (net, m_tile, n_tile) order
+// (n fastest, so the N-tiles of one M-tile run on neighbouring CTAs and share
+// A through L2). The producer streams K-slices through the stage ring across
+// tile boundaries; the MMA issuer alternates between two 256-column TMEM
+// accumulators, so the epilogue of tile t overlaps the MMAs of tile t + 1.
 template <int PREC, int EPI>
 __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArgs g) {
   using C = Cfg<PREC>;
@@ -270,26 +281,32 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
                                              ~static_cast<uintptr_t>(1023));
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + C::NSTAGE * C::STAGE);
   uint64_t* empty = full + C::NSTAGE;
-  uint64_t* accf = empty + C::NSTAGE;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accf + 1);
+  uint64_t* accf = empty + C::NSTAGE;   // [2] accumulator ready
+  uint64_t* acce = accf + 2;            // [2] accumulator drained
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acce + 2);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m_tile = blockIdx.x, n_tile = blockIdx.y, net = blockIdx.z;
   const int nk = g.K / C::BK;
-  const int elem = g.tile_elem[m_tile];
+  const int per_net = g.mtiles * g.ntiles;
+  const int total = 2 * per_net;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < C::NSTAGE; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(accf, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], 4);   // one arrival per epilogue warp
+    }
+    *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
-                 "r"(BN)
+                 "r"(2 * BN)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -300,73 +317,100 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
 
   if (warp == 4) {
     if (lane == 0) {
-      const int a_row = net * g.a_net_rows + m_tile * BM;
-      const int b_row = (net * g.nele + elem) * g.N + n_tile * BN;
-      for (int kb = 0; kb < nk; ++kb) {
-        const int s = kb % C::NSTAGE;
-        if (kb >= C::NSTAGE) {
-          if (!mbar_wait(&empty[s], ((kb / C::NSTAGE) - 1) & 1)) {
-            tm_flag(g.st, TM_E_TIMEOUT, kb, 100);
+      int it = 0;
+      for (int t = blockIdx.x; t < total && !*abort_flag; t += gridDim.x) {
+        const int net = t / per_net, rem = t % per_net;
+        const int m_tile = rem / g.ntiles, n_tile = rem % g.ntiles;
+        const int elem = g.tile_elem[m_tile];
+        const int a_row = net * g.a_net_rows + m_tile * BM;
+        const int b_row = (net * g.nele + elem) * g.N + n_tile * BN;
+        for (int kb = 0; kb < nk; ++kb, ++it) {
+          const int s = it % C::NSTAGE;
+          if (it >= C::NSTAGE && !mbar_wait(&empty[s], ((it / C::NSTAGE) - 1) & 1)) {
+            tm_flag(g.st, TM_E_TIMEOUT, t, 100);
+            *abort_flag = 1;
             break;
           }
-        }
-        uint8_t* st = smem + s * C::STAGE;
-        mbar_expect_tx(&full[s], C::STAGE);
-        const int x = kb * C::BK;
-        tma_load_2d(st, &g.a0, x, a_row, &full[s]);
-        tma_load_2d(st + C::NSPLIT * C::A_TILE, &g.b0, x, b_row, &full[s]);
-        if (C::NSPLIT == 2) {
-          tma_load_2d(st + C::A_TILE, &g.a1, x, a_row, &full[s]);
-          tma_load_2d(st + 2 * C::A_TILE + C::B_TILE, &g.b1, x, b_row, &full[s]);
+          uint8_t* st = smem + s * C::STAGE;
+          mbar_expect_tx(&full[s], C::STAGE);
+          const int x = kb * C::BK;
+          tma_load_2d(st, &g.a0, x, a_row, &full[s]);
+          tma_load_2d(st + C::NSPLIT * C::A_TILE, &g.b0, x, b_row, &full[s]);
+          if (C::NSPLIT == 2) {
+            tma_load_2d(st + C::A_TILE, &g.a1, x, a_row, &full[s]);
+            tma_load_2d(st + 2 * C::A_TILE + C::B_TILE, &g.b1, x, b_row, &full[s]);
+          }
         }
       }
     }
   } else if (warp == 5) {
     if (lane == 0) {
-      bool ok = true;
-      for (int kb = 0; kb < nk; ++kb) {
-        const int s = kb % C::NSTAGE;
-        if (!mbar_wait(&full[s], (kb / C::NSTAGE) & 1)) {
-          tm_flag(g.st, TM_E_TIMEOUT, kb, 101);
-          ok = false;
+      int it = 0, lt = 0;
+      for (int t = blockIdx.x; t < total && !*abort_flag; t += gridDim.x, ++lt) {
+        const int buf = lt & 1;
+        if (lt >= 2 && !mbar_wait(&acce[buf], ((lt >> 1) - 1) & 1)) {
+          tm_flag(g.st, TM_E_TIMEOUT, t, 103);
+          *abort_flag = 1;
           break;
         }
         tc_fence_after();
-        const uint32_t base = smem_u32(smem + s * C::STAGE);
-        const uint32_t a0 = base;
-        const uint32_t a1 = base + C::A_TILE;
-        const uint32_t b0 = base + C::NSPLIT * C::A_TILE;
-        const uint32_t b1 = b0 + C::B_TILE;
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-          const uint64_t ad0 = sw128_desc(a0 + kk * 32), bd0 = sw128_desc(b0 + kk * 32);
-          const uint32_t acc = (kb | kk) ? 1u : 0u;
-          if (PREC == TM_PREC_FP32) {
-            const uint64_t ad1 = sw128_desc(a1 + kk * 32), bd1 = sw128_desc(b1 + kk * 32);
-            umma_tf32(tmem, ad0, bd0, C::IDESC, acc);
-            umma_tf32(tmem, ad0, bd1, C::IDESC, 1u);
-            umma_tf32(tmem, ad1, bd0, C::IDESC, 1u);
-          } else {
-            umma_f16(tmem, ad0, bd0, C::IDESC, acc);
+        const uint32_t d = tmem + (uint32_t)(buf * BN);
+        bool ok = true;
+        for (int kb = 0; kb < nk; ++kb, ++it) {
+          const int s = it % C::NSTAGE;
+          if (!mbar_wait(&full[s], (it / C::NSTAGE) & 1)) {
+            tm_flag(g.st, TM_E_TIMEOUT, t, 101);
+            *abort_flag = 1;
+            ok = false;
+            break;
           }
+          tc_fence_after();
+          const uint32_t base = smem_u32(smem + s * C::STAGE);
+          const uint32_t a0 = base;
+          const uint32_t a1 = base + C::A_TILE;
+          const uint32_t b0 = base + C::NSPLIT * C::A_TILE;
+          const uint32_t b1 = b0 + C::B_TILE;
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk) {
+            const uint64_t ad0 = sw128_desc(a0 + kk * 32), bd0 = sw128_desc(b0 + kk * 32);
+            const uint32_t acc = (kb | kk) ? 1u : 0u;
+            if (PREC == TM_PREC_FP32) {
+              const uint64_t ad1 = sw128_desc(a1 + kk * 32), bd1 = sw128_desc(b1 + kk * 32);
+              umma_tf32(d, ad0, bd0, C::IDESC, acc);
+              umma_tf32(d, ad0, bd1, C::IDESC, 1u);
+              umma_tf32(d, ad1, bd0, C::IDESC, 1u);
+            } else {
+              umma_f16(d, ad0, bd0, C::IDESC, acc);
+            }
+          }
+          umma_commit(&empty[s]);
         }
-        umma_commit(&empty[s]);
+        if (!ok) break;
+        umma_commit(&accf[buf]);
       }
-      if (ok) umma_commit(accf);
     }
   } else {
     // ---- epilogue: warps 0..3, thread = accumulator row ----
-    const bool ready = mbar_wait(accf, 0);
-    if (!ready) tm_flag(g.st, TM_E_TIMEOUT, m_tile, 102);
-    tc_fence_after();
-    if (ready) {
+    int lt = 0;
+    for (int t = blockIdx.x; t < total; t += gridDim.x, ++lt) {
+      const int buf = lt & 1;
+      if (!mbar_wait(&accf[buf], (lt >> 1) & 1)) {
+        tm_flag(g.st, TM_E_TIMEOUT, t, 102);
+        *abort_flag = 1;
+        break;
+      }
+      tc_fence_after();
+      const int net = t / per_net, rem = t % per_net;
+      const int m_tile = rem / g.ntiles, n_tile = rem % g.ntiles;
+      const int elem = g.tile_elem[m_tile];
       const int row = m_tile * BM + warp * 32 + lane;          // row in this net
       const size_t orow = (size_t)net * g.Mpad + row;
       const int pblk = (net * g.nele + elem) * g.N;
+      const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(buf * BN);
       float esum = 0.f;
       for (int c = 0; c < BN; c += 32) {
         uint32_t r[32];
-        tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, r);
+        tmem_ld32(tbase + (uint32_t)c, r);
         const int col = n_tile * BN + c;
         float v[32];
         if (EPI == EPI_FWD || EPI == EPI_FWD_LAST) {
@@ -398,24 +442,32 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
         }
       }
       if (EPI == EPI_FWD_LAST) g.epart[orow * (g.N / BN) + n_tile] = esum;
+      // this warp has read its 32 lanes of the accumulator: hand it back
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acce[buf]);
     }
   }
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN)
                  : "memory");
   }
 }
 
 template <int PREC, int EPI>
-int launch_gemm(tm_ctx* ctx, const GemmArgs& g, int mtiles, int ntiles) {
+int launch_gemm(tm_ctx* ctx, const GemmArgs& g0, int mtiles, int ntiles) {
   using C = Cfg<PREC>;
   cudaError_t e = cudaFuncSetAttribute(k_gemm<PREC, EPI>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
   if (e != cudaSuccess) return tm_cuda_check(ctx, e, "gemm attr");
-  dim3 grid(mtiles, ntiles, 2);
+  GemmArgs g = g0;
+  g.mtiles = mtiles;
+  g.ntiles = ntiles;
+  const int total = 2 * mtiles * ntiles;
+  const int grid = total < ctx->num_sms ? total : ctx->num_sms;
   k_gemm<PREC, EPI><<<grid, 192, C::SMEM, ctx->stream>>>(g);
   ctx->launches++;
   return tm_cuda_check(ctx, cudaGetLastError(), "gemm");

@@ -49,6 +49,7 @@ struct tm_grid {
 
 struct tm_ctx {
   int device = 0;
+  int num_sms = 1;                     // streaming multiprocessors of the device
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   size_t budget = 0, in_use = 0;
