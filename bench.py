@@ -295,6 +295,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle leg")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--fused-only", action="store_true",
+                    help="time only the device-resident fused E+F (for profiler launch lists)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -323,6 +325,12 @@ def main():
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     value = ws * w.natoms / (ms / 1000.0)
+    if args.fused_only:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+                              "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+                              "gpu_launches": int(launches), "note": "fused E+F only"}))
+        return 0
     # stage breakdown (one profiled evaluation)
     import ctypes
     st = np.zeros(7, dtype=np.float32)

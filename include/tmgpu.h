@@ -183,9 +183,10 @@ int tm_md_destroy(tm_md *md);
 int tm_md_set_velocities(tm_md *md, const double *v, int on_device);
 int tm_md_get_velocities(tm_md *md, double *v, int on_device);
 /*
- * nsteps integrator steps, each with one energy+force evaluation and a
- * neighbour-list rebuild when any atom moved more than skin/2 since the last
- * build (skin = 0: rebuild every step). log[nsteps][4] (host, may be NULL) =
+ * nsteps integrator steps, each with one energy+force evaluation and a fresh
+ * neighbour-list build (the reference builds its lists on every call,
+ * TFMolManage.py:1418-1431). skin is reserved and must be 0 or positive; it is
+ * not used. log[nsteps][4] (host, may be NULL) =
  * (potential Hartree, kinetic J/mol per atom, conserved J/mol, T_eff K).
  */
 int tm_md_run(tm_md *md, int nsteps, double skin, double *log);

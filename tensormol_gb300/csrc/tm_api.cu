@@ -274,13 +274,7 @@ static int upload_split(tm_model* m, const std::vector<float>& host, void* out[2
   int rc;
   if (m->desc.precision == TM_PREC_FP32) {
     std::vector<float> hi(n), lo(n);
-    for (size_t q = 0; q < n; ++q) {
-      uint32_t u;
-      memcpy(&u, &host[q], 4);
-      u &= 0xffffe000u;
-      memcpy(&hi[q], &u, 4);
-      lo[q] = host[q] - hi[q];
-    }
+    for (size_t q = 0; q < n; ++q) tm_tf32_split(host[q], hi[q], lo[q]);
     if ((rc = tm_alloc(ctx, &out[0], n * 4)) || (rc = tm_alloc(ctx, &out[1], n * 4))) return rc;
     cudaMemcpyAsync(out[0], hi.data(), n * 4, cudaMemcpyHostToDevice, ctx->stream);
     cudaMemcpyAsync(out[1], lo.data(), n * 4, cudaMemcpyHostToDevice, ctx->stream);
@@ -324,10 +318,11 @@ extern "C" int tm_model_finalize(tm_model* m) {
     if ((rc = tm_alloc(ctx, (void**)&m->bias[l], bias.size() * 4))) return rc;
     cudaMemcpyAsync(m->bias[l], bias.data(), bias.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
     const int eb = (int)m->elem_size;
-    if ((rc = tm_make_tmap(ctx, &m->tm_wf[l][0], m->w_fwd[l][0], eb, (uint64_t)2 * nele * H, Kin, TM_BN)) ||
-        (rc = tm_make_tmap(ctx, &m->tm_wf[l][1], m->w_fwd[l][1], eb, (uint64_t)2 * nele * H, Kin, TM_BN)) ||
-        (rc = tm_make_tmap(ctx, &m->tm_wb[l][0], m->w_bwd[l][0], eb, (uint64_t)2 * nele * Kin, H, TM_BN)) ||
-        (rc = tm_make_tmap(ctx, &m->tm_wb[l][1], m->w_bwd[l][1], eb, (uint64_t)2 * nele * Kin, H, TM_BN)))
+    const uint32_t bn = (uint32_t)tm_gemm_bn(m->desc.precision);   // B tile rows
+    if ((rc = tm_make_tmap(ctx, &m->tm_wf[l][0], m->w_fwd[l][0], eb, (uint64_t)2 * nele * H, Kin, bn)) ||
+        (rc = tm_make_tmap(ctx, &m->tm_wf[l][1], m->w_fwd[l][1], eb, (uint64_t)2 * nele * H, Kin, bn)) ||
+        (rc = tm_make_tmap(ctx, &m->tm_wb[l][0], m->w_bwd[l][0], eb, (uint64_t)2 * nele * Kin, H, bn)) ||
+        (rc = tm_make_tmap(ctx, &m->tm_wb[l][1], m->w_bwd[l][1], eb, (uint64_t)2 * nele * Kin, H, bn)))
       return rc;
   }
   std::vector<float> wout((size_t)2 * nele * H, 0.f);
@@ -417,15 +412,10 @@ extern "C" int tm_system_create(tm_model* m, int N, int nmol, const int32_t* Z,
       delete s;
       return tm_fail(ctx, TM_E_ARG, "cell edges must be at least twice the largest cutoff");
     }
-    for (int d = 0; d < 3; ++d) {
-      const double L = cell[4 * d];
-      const int n = (int)floor(L / k.r_rc_d);
-      const int R = (int)ceil(k.ree_d / (L / n));
-      if (n < 3 || 2 * R + 1 > n) {
-        delete s;
-        return tm_fail(ctx, TM_E_ARG, "cell too small for the minimum-image cell search");
-      }
-    }
+    // With edges >= 2 * cutoff, a +-R cell search (R = ceil(cutoff / cell
+    // edge) <= ceil(n / 2) <= n) wraps at most once per axis and reaches each
+    // (cell, image) at most once; the exact distance test keeps the one image
+    // within the cutoff.
     s->periodic = true;
   }
   // elements and element-sorted rows
@@ -466,11 +456,9 @@ extern "C" int tm_system_create(tm_model* m, int N, int nmol, const int32_t* Z,
     for (int d = 0; d < 3; ++d) nc *= (long)floor(s->lat[4 * d] / k.r_rc_d);
     s->ncell_cap = (int)nc;
   }
-  // Coulomb grid: about 24 atoms per cell; a periodic edge gets the fewest
-  // cells of at least that size for which the +-R cell search visits no cell
-  // twice (2R + 1 <= n)
-  // open: at most n/8 + 8 cells per molecule (the device grows the cell size
-  // until a molecule fits, with the same bound)
+  // Coulomb grid: about 24 atoms per cell (periodic: floor(L / size) cells per
+  // edge); open: at most n/8 + 8 cells per molecule (the device grows the cell
+  // size until a molecule fits, with the same bound)
   s->ecell_cap = 0;
   for (int q = 0; q < nmol; ++q) s->ecell_cap += (int)((off[q + 1] - off[q]) / 8) + 8;
   if (s->periodic) {
@@ -479,8 +467,7 @@ extern "C" int tm_system_create(tm_model* m, int N, int nmol, const int32_t* Z,
     long nc = 1;
     for (int d = 0; d < 3; ++d) {
       const double L = s->lat[4 * d];
-      int n = std::max(1, (int)floor(L / cs));
-      while (2 * (int)ceil(k.ree_d / (L / n)) + 1 > n && n < 4096) ++n;
+      const int n = std::max(1, std::min(4096, (int)floor(L / cs)));
       s->ee_dims[d] = n;
       nc *= n;
     }
@@ -552,7 +539,7 @@ extern "C" int tm_system_create(tm_model* m, int N, int nmol, const int32_t* Z,
     A.get(&s->G3[h], 2 * Mp * H * es);
   }
   A.get(&s->dEdG, sizeof(float) * 2 * Mp * Dp);
-  A.get(&s->epart, sizeof(float) * 2 * Mp * (H / TM_BN));
+  A.get(&s->epart, sizeof(float) * 2 * Mp * (H / tm_gemm_bn(m->desc.precision)));
   A.get(&s->d_Eatom, sizeof(double) * N);
   A.get(&s->d_qraw, sizeof(float) * N);
   A.get(&s->d_q, sizeof(float) * N);

@@ -3,6 +3,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "../../include/tmgpu.h"
 
@@ -111,4 +112,22 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(TM_FULL, v, o);
   return v;
+}
+
+// Split of an FP32 value into two TF32 values for the 3-pass tensor-core
+// product: hi = x rounded to nearest TF32 (10 mantissa bits; add half an ulp
+// of the kept bits, clear the 13 low bits), lo = x - hi (exact in FP32) rounded
+// the same way. Rounding to nearest (rather than truncating) keeps both parts'
+// errors unbiased; |x - hi - lo| <= 2^-23 |x|.
+__host__ __device__ __forceinline__ float tm_tf32_rn(float x) {
+  uint32_t u;
+  memcpy(&u, &x, 4);
+  u = (u + 0x1000u) & 0xffffe000u;
+  float r;
+  memcpy(&r, &u, 4);
+  return r;
+}
+__host__ __device__ __forceinline__ void tm_tf32_split(float x, float& hi, float& lo) {
+  hi = tm_tf32_rn(x);
+  lo = tm_tf32_rn(x - hi);
 }

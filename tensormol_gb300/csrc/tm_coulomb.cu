@@ -188,7 +188,10 @@ __global__ void __launch_bounds__(128) k_coulomb(const CoulArgs a, const tm_cons
   const int lc = c - g.cell_off;
   const int iz = lc % g.nz, iy = (lc / g.nz) % g.ny, ix = lc / (g.nz * g.ny);
   const float cx = (float)g.cx, cy = (float)g.cy, cz = (float)g.cz;
-  const int Rx = (int)ceil(a.ree / g.cx), Ry = (int)ceil(a.ree / g.cy), Rz = (int)ceil(a.ree / g.cz);
+  // periodic: at most one wrap per axis (R <= n; edges are >= 2 * cutoff)
+  const int Rx = a.periodic ? min((int)ceil(a.ree / g.cx), g.nx) : (int)ceil(a.ree / g.cx);
+  const int Ry = a.periodic ? min((int)ceil(a.ree / g.cy), g.ny) : (int)ceil(a.ree / g.cy);
+  const int Rz = a.periodic ? min((int)ceil(a.ree / g.cz), g.nz) : (int)ceil(a.ree / g.cz);
   float4* sj_hi = sh[wib][0];
   float4* sj_lo = sh[wib][1];
   for (int ib = t0; ib < t1; ib += 32) {
@@ -356,7 +359,7 @@ void tm_fill_shifts(const tm_system* s, float hi[27][3], float lo[27][3]);
 int tm_launch_mlp_finish(tm_system* s) {
   tm_ctx* ctx = s->ctx;
   tm_model* m = s->model;
-  const int nsplit = m->H / TM_BN;
+  const int nsplit = m->H / tm_gemm_bn(m->desc.precision);
   k_mlp_finish<<<tm_div_up(s->N, 256), 256, 0, ctx->stream>>>(
       s->epart, m->bout, s->row_of_atom, s->d_elem, nsplit, s->Mpad, m->k.nele, s->N, s->d_Eatom,
       s->d_qraw);

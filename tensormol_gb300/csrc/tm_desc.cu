@@ -261,13 +261,13 @@ __global__ void __launch_bounds__(128) k_desc_fwd(const DescArgs a, const tm_con
     float4* o1 = reinterpret_cast<float4*>(static_cast<float*>(a.out1) + (size_t)row * k.Dp);
     for (int c = lane; c < k.Dp / 4; c += 32) {
       float4 v = reinterpret_cast<const float4*>(w.row)[c];
-      float4 h;
-      h.x = __uint_as_float(__float_as_uint(v.x) & 0xffffe000u);
-      h.y = __uint_as_float(__float_as_uint(v.y) & 0xffffe000u);
-      h.z = __uint_as_float(__float_as_uint(v.z) & 0xffffe000u);
-      h.w = __uint_as_float(__float_as_uint(v.w) & 0xffffe000u);
+      float4 h, l;
+      tm_tf32_split(v.x, h.x, l.x);
+      tm_tf32_split(v.y, h.y, l.y);
+      tm_tf32_split(v.z, h.z, l.z);
+      tm_tf32_split(v.w, h.w, l.w);
       o0[c] = h;
-      o1[c] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+      o1[c] = l;
     }
   } else {
     uint2* o0 = reinterpret_cast<uint2*>(static_cast<uint16_t*>(a.out0) + (size_t)row * k.Dp);

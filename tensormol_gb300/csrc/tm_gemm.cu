@@ -1,25 +1,30 @@
 // Per-element BP network layers as tcgen05 tensor-core GEMMs (sm_103a).
 //
 // One launch computes one layer for every element and both networks
-// (grid.z = 0: EnergyNet, 1: DipoleNet; TFBehlerParinelloSymEE.py:884-944,
-// 946-1015): C[128 x 256 tile] = A[rows of one element, K] . W^T, with the
+// (net 0: EnergyNet, 1: DipoleNet; TFBehlerParinelloSymEE.py:884-944,
+// 946-1015): C[128 x BN tile] = A[rows of one element, K] . W^T, with the
 // element of each 128-row tile taken from a table (rows of each element are
 // padded to 128, so no tile mixes elements).
 //
-// Pipeline per CTA (192 threads):
+// Persistent CTAs (one per SM, 192 threads) walk the tiles:
 //   warp 4       TMA producer: K-slices of A and B into a ring of 128-byte-
 //                swizzled shared-memory stages (cp.async.bulk.tensor, mbarriers)
-//   warp 5       MMA issuer: one elected thread issues tcgen05.mma into a
-//                128 x 256 FP32 accumulator in tensor memory
+//   warp 5       MMA issuer: one elected thread issues tcgen05.mma into FP32
+//                accumulators in tensor memory (two tile buffers)
 //   warps 0..3   epilogue: tcgen05.ld 32 columns at a time, fused bias +
 //                activation (forward) or activation-derivative product
 //                (backward), stores to global.
 // Precision modes:
-//   TM_PREC_FP32  kind::tf32 with operands split as x = hi + lo (hi = x with
-//                 the 13 low mantissa bits cleared); D += Ahi Bhi + Ahi Blo +
-//                 Alo Bhi, FP32 accumulate. Measured on CPU emulation to give
-//                 FP32-level energy/force error.
-//   TM_PREC_BF16  kind::f16 with BF16 operands, one pass, FP32 accumulate.
+//   TM_PREC_FP32  kind::tf32 with operands split as x = hi + lo (both rounded
+//                 to nearest TF32, tm_tf32_split); BN = 128. The large term
+//                 Ahi Bhi and the two small terms Ahi Blo + Alo Bhi go to
+//                 separate accumulators that the epilogue adds: the tensor
+//                 core's accumulation drops low-order bits at every
+//                 instruction (measured: a bias toward zero growing with K),
+//                 and keeping the correction terms out of the large
+//                 accumulator removes two thirds of those roundings.
+//   TM_PREC_BF16  kind::f16 with BF16 operands, one pass, FP32 accumulate;
+//                 BN = 256.
 // All waits on mbarriers are bounded (about 2 s); a timeout sets the device
 // status word to TM_E_TIMEOUT and the CTA still frees its tensor memory.
 #include <cuda.h>
@@ -30,7 +35,7 @@
 
 namespace {
 
-constexpr int BM = TM_BM, BN = TM_BN;
+constexpr int BM = TM_BM;
 constexpr int EPI_FWD = 0, EPI_FWD_LAST = 1, EPI_BWD = 2, EPI_OUT = 3;
 
 struct GemmArgs {
@@ -45,7 +50,7 @@ struct GemmArgs {
   float alpha;
   const float* bias;   // [2][nele][N]
   const float* wout;   // [2][nele][N]
-  float* epart;        // [2][Mpad][N/BN]
+  float* epart;        // [2][Mpad][N/BN], BN of the precision mode
   void* out0;
   void* out1;
   int ldo;
@@ -156,41 +161,37 @@ __host__ __device__ constexpr uint32_t make_idesc(int ab_format, int M, int N) {
          ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-// ---- activations ----------------------------------------------------------
-__device__ __forceinline__ float act_f(float z, int act, float a) {
-  switch (act) {
-    case TM_ACT_RELU: return fmaxf(z, 0.f);
-    case TM_ACT_SIGMOID_WITH_PARAM: {
-      const float t = a * z;
-      return (fmaxf(t, 0.f) + log1pf(expf(-fabsf(t)))) / a;
-    }
-    case TM_ACT_SOFTPLUS: return fmaxf(z, 0.f) + log1pf(expf(-fabsf(z)));
-    case TM_ACT_TANH: return tanhf(z);
-    default: return z > 0.f ? z : expm1f(z);   // elu
+// ---- activations (Instance.AssignActivation, TFInstance.py:108-140) ------
+// The activation is a template parameter: a run-time switch over all five
+// inlined into the 32-wide unrolled epilogue made the forward kernels
+// instruction-fetch bound.
+template <int ACT>
+__device__ __forceinline__ float act_f(float z, float a) {
+  if constexpr (ACT == TM_ACT_RELU) return fmaxf(z, 0.f);
+  if constexpr (ACT == TM_ACT_SIGMOID_WITH_PARAM) {   // log(1 + exp(a z)) / a, Util.py:200-201
+    const float t = a * z;
+    return (fmaxf(t, 0.f) + log1pf(expf(-fabsf(t)))) / a;
   }
+  if constexpr (ACT == TM_ACT_SOFTPLUS) return fmaxf(z, 0.f) + log1pf(expf(-fabsf(z)));
+  if constexpr (ACT == TM_ACT_TANH) return tanhf(z);
+  return z > 0.f ? z : expm1f(z);   // elu
 }
-__device__ __forceinline__ float actd_z(float z, int act, float a) {
-  switch (act) {
-    case TM_ACT_RELU: return z > 0.f ? 1.f : 0.f;
-    case TM_ACT_SIGMOID_WITH_PARAM: return 1.f / (1.f + expf(-a * z));
-    case TM_ACT_SOFTPLUS: return 1.f / (1.f + expf(-z));
-    case TM_ACT_TANH: { const float t = tanhf(z); return 1.f - t * t; }
-    default: return z > 0.f ? 1.f : expf(z);
-  }
+template <int ACT>
+__device__ __forceinline__ float actd_z(float z, float a) {
+  if constexpr (ACT == TM_ACT_RELU) return z > 0.f ? 1.f : 0.f;
+  if constexpr (ACT == TM_ACT_SIGMOID_WITH_PARAM) return 1.f / (1.f + expf(-a * z));
+  if constexpr (ACT == TM_ACT_SOFTPLUS) return 1.f / (1.f + expf(-z));
+  if constexpr (ACT == TM_ACT_TANH) { const float t = tanhf(z); return 1.f - t * t; }
+  return z > 0.f ? 1.f : expf(z);
 }
 // derivative expressed through the activation's output h = act(z)
-__device__ __forceinline__ float actd_h(float h, int act, float a) {
-  switch (act) {
-    case TM_ACT_RELU: return h > 0.f ? 1.f : 0.f;
-    case TM_ACT_SIGMOID_WITH_PARAM: return -expm1f(-a * h);
-    case TM_ACT_SOFTPLUS: return -expm1f(-h);
-    case TM_ACT_TANH: return 1.f - h * h;
-    default: return h > 0.f ? 1.f : h + 1.f;
-  }
-}
-
-__device__ __forceinline__ float tf32_hi(float v) {
-  return __uint_as_float(__float_as_uint(v) & 0xffffe000u);
+template <int ACT>
+__device__ __forceinline__ float actd_h(float h, float a) {
+  if constexpr (ACT == TM_ACT_RELU) return h > 0.f ? 1.f : 0.f;
+  if constexpr (ACT == TM_ACT_SIGMOID_WITH_PARAM) return -expm1f(-a * h);
+  if constexpr (ACT == TM_ACT_SOFTPLUS) return -expm1f(-h);
+  if constexpr (ACT == TM_ACT_TANH) return 1.f - h * h;
+  return h > 0.f ? 1.f : h + 1.f;
 }
 
 template <int PREC>
@@ -200,11 +201,13 @@ __device__ __forceinline__ void store32(void* o0, void* o1, size_t idx, const fl
     float4* p1 = reinterpret_cast<float4*>(static_cast<float*>(o1) + idx);
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-      float4 h = make_float4(tf32_hi(v[4 * q]), tf32_hi(v[4 * q + 1]), tf32_hi(v[4 * q + 2]),
-                             tf32_hi(v[4 * q + 3]));
+      float4 h, l;
+      tm_tf32_split(v[4 * q], h.x, l.x);
+      tm_tf32_split(v[4 * q + 1], h.y, l.y);
+      tm_tf32_split(v[4 * q + 2], h.z, l.z);
+      tm_tf32_split(v[4 * q + 3], h.w, l.w);
       p0[q] = h;
-      p1[q] = make_float4(v[4 * q] - h.x, v[4 * q + 1] - h.y, v[4 * q + 2] - h.z,
-                          v[4 * q + 3] - h.w);
+      p1[q] = l;
     }
   } else {
     uint4* p0 = reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(o0) + idx);
@@ -255,10 +258,13 @@ struct Cfg {
   static constexpr int ELEM = PREC == TM_PREC_FP32 ? 4 : 2;
   static constexpr int BK = 128 / ELEM;               // one 128-byte swizzle row
   static constexpr int NSPLIT = PREC == TM_PREC_FP32 ? 2 : 1;
+  static constexpr int BN = PREC == TM_PREC_FP32 ? 128 : 256;   // N tile
+  static constexpr int NACC = NSPLIT;                 // accumulators per tile (main, correction)
+  static constexpr int ACC_COLS = NACC * BN;          // TMEM columns per tile buffer: 256
   static constexpr int A_TILE = BM * 128;             // 16 KB
-  static constexpr int B_TILE = BN * 128;             // 32 KB
-  static constexpr int STAGE = NSPLIT * (A_TILE + B_TILE);
-  static constexpr int NSTAGE = PREC == TM_PREC_FP32 ? 2 : 4;
+  static constexpr int B_TILE = BN * 128;             // 16 KB (tf32) or 32 KB (bf16)
+  static constexpr int STAGE = NSPLIT * (A_TILE + B_TILE);   // 64 KB or 48 KB
+  static constexpr int NSTAGE = PREC == TM_PREC_FP32 ? 3 : 4;
   static constexpr int SMEM = NSTAGE * STAGE + 1024 + 256;   // stages, alignment, barriers
   static constexpr uint32_t IDESC = make_idesc(PREC == TM_PREC_FP32 ? 2 : 1, BM, BN);
 };
@@ -272,10 +278,11 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* b) {
 // (n fastest, so the N-tiles of one M-tile run on neighbouring CTAs and share
 // A through L2). The producer streams K-slices through the stage ring across
 // tile boundaries; the MMA issuer alternates between two 256-column TMEM
-// accumulators, so the epilogue of tile t overlaps the MMAs of tile t + 1.
-template <int PREC, int EPI>
+// tile buffers, so the epilogue of tile t overlaps the MMAs of tile t + 1.
+template <int PREC, int EPI, int ACT>
 __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArgs g) {
   using C = Cfg<PREC>;
+  constexpr int BN = C::BN;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~static_cast<uintptr_t>(1023));
@@ -306,7 +313,7 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
-                 "r"(2 * BN)
+                 "r"(2 * C::ACC_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -354,7 +361,7 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
           break;
         }
         tc_fence_after();
-        const uint32_t d = tmem + (uint32_t)(buf * BN);
+        const uint32_t d = tmem + (uint32_t)(buf * C::ACC_COLS);   // main; correction at + BN
         bool ok = true;
         for (int kb = 0; kb < nk; ++kb, ++it) {
           const int s = it % C::NSTAGE;
@@ -377,8 +384,8 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
             if (PREC == TM_PREC_FP32) {
               const uint64_t ad1 = sw128_desc(a1 + kk * 32), bd1 = sw128_desc(b1 + kk * 32);
               umma_tf32(d, ad0, bd0, C::IDESC, acc);
-              umma_tf32(d, ad0, bd1, C::IDESC, 1u);
-              umma_tf32(d, ad1, bd0, C::IDESC, 1u);
+              umma_tf32(d + BN, ad0, bd1, C::IDESC, acc);
+              umma_tf32(d + BN, ad1, bd0, C::IDESC, 1u);
             } else {
               umma_f16(d, ad0, bd0, C::IDESC, acc);
             }
@@ -406,11 +413,18 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
       const int row = m_tile * BM + warp * 32 + lane;          // row in this net
       const size_t orow = (size_t)net * g.Mpad + row;
       const int pblk = (net * g.nele + elem) * g.N;
-      const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(buf * BN);
+      const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(buf * C::ACC_COLS);
       float esum = 0.f;
       for (int c = 0; c < BN; c += 32) {
         uint32_t r[32];
         tmem_ld32(tbase + (uint32_t)c, r);
+        if (C::NACC == 2) {
+          uint32_t r2[32];
+          tmem_ld32(tbase + (uint32_t)(BN + c), r2);
+#pragma unroll
+          for (int q = 0; q < 32; ++q)
+            r[q] = __float_as_uint(__uint_as_float(r[q]) + __uint_as_float(r2[q]));
+        }
         const int col = n_tile * BN + c;
         float v[32];
         if (EPI == EPI_FWD || EPI == EPI_FWD_LAST) {
@@ -419,11 +433,11 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
           for (int q = 0; q < 32; ++q) {
             const float z = __uint_as_float(r[q]) + __ldg(bias + q);
             if (EPI == EPI_FWD) {
-              v[q] = act_f(z, g.act, g.alpha);
+              v[q] = act_f<ACT>(z, g.alpha);
             } else {
               const float w = __ldg(g.wout + pblk + col + q);
-              esum += act_f(z, g.act, g.alpha) * w;
-              v[q] = w * actd_z(z, g.act, g.alpha);
+              esum += act_f<ACT>(z, g.alpha) * w;
+              v[q] = w * actd_z<ACT>(z, g.alpha);
             }
           }
           store32<PREC>(g.out0, g.out1, orow * g.ldo + col, v);
@@ -431,7 +445,7 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
           float h[32];
           load32<PREC>(g.hprev0, g.hprev1, orow * g.ldo + col, h);
 #pragma unroll
-          for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]) * actd_h(h[q], g.act, g.alpha);
+          for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]) * actd_h<ACT>(h[q], g.alpha);
           store32<PREC>(g.out0, g.out1, orow * g.ldo + col, v);
         } else {
           float4* o = reinterpret_cast<float4*>(static_cast<float*>(g.out0) + orow * g.ldo + col);
@@ -452,15 +466,17 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * C::ACC_COLS)
                  : "memory");
   }
 }
 
-template <int PREC, int EPI>
-int launch_gemm(tm_ctx* ctx, const GemmArgs& g0, int mtiles, int ntiles) {
+template <int PREC, int EPI, int ACT>
+int launch_gemm(tm_ctx* ctx, const GemmArgs& g0, int mtiles) {
   using C = Cfg<PREC>;
-  cudaError_t e = cudaFuncSetAttribute(k_gemm<PREC, EPI>,
+  if (g0.N % C::BN) return tm_fail(ctx, TM_E_ARG, "gemm width not a multiple of the N tile");
+  const int ntiles = g0.N / C::BN;
+  cudaError_t e = cudaFuncSetAttribute(k_gemm<PREC, EPI, ACT>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
   if (e != cudaSuccess) return tm_cuda_check(ctx, e, "gemm attr");
   GemmArgs g = g0;
@@ -468,27 +484,43 @@ int launch_gemm(tm_ctx* ctx, const GemmArgs& g0, int mtiles, int ntiles) {
   g.ntiles = ntiles;
   const int total = 2 * mtiles * ntiles;
   const int grid = total < ctx->num_sms ? total : ctx->num_sms;
-  k_gemm<PREC, EPI><<<grid, 192, C::SMEM, ctx->stream>>>(g);
+  k_gemm<PREC, EPI, ACT><<<grid, 192, C::SMEM, ctx->stream>>>(g);
   ctx->launches++;
   return tm_cuda_check(ctx, cudaGetLastError(), "gemm");
 }
 
-template <int PREC>
-int run_gemm(tm_ctx* ctx, int epi, const GemmArgs& g, int mtiles, int ntiles) {
+template <int PREC, int ACT>
+int run_gemm(tm_ctx* ctx, int epi, const GemmArgs& g, int mtiles) {
   switch (epi) {
-    case EPI_FWD: return launch_gemm<PREC, EPI_FWD>(ctx, g, mtiles, ntiles);
-    case EPI_FWD_LAST: return launch_gemm<PREC, EPI_FWD_LAST>(ctx, g, mtiles, ntiles);
-    case EPI_BWD: return launch_gemm<PREC, EPI_BWD>(ctx, g, mtiles, ntiles);
-    default: return launch_gemm<PREC, EPI_OUT>(ctx, g, mtiles, ntiles);
+    case EPI_FWD: return launch_gemm<PREC, EPI_FWD, ACT>(ctx, g, mtiles);
+    case EPI_FWD_LAST: return launch_gemm<PREC, EPI_FWD_LAST, ACT>(ctx, g, mtiles);
+    case EPI_BWD: return launch_gemm<PREC, EPI_BWD, ACT>(ctx, g, mtiles);
+    default: return launch_gemm<PREC, EPI_OUT, TM_ACT_RELU>(ctx, g, mtiles);
   }
 }
 
-int dispatch(tm_ctx* ctx, int prec, int epi, const GemmArgs& g, int mtiles, int ntiles) {
-  return prec == TM_PREC_FP32 ? run_gemm<TM_PREC_FP32>(ctx, epi, g, mtiles, ntiles)
-                              : run_gemm<TM_PREC_BF16>(ctx, epi, g, mtiles, ntiles);
+template <int PREC>
+int run_gemm_act(tm_ctx* ctx, int epi, const GemmArgs& g, int mtiles) {
+  switch (epi == EPI_OUT ? TM_ACT_RELU : g.act) {
+    case TM_ACT_RELU: return run_gemm<PREC, TM_ACT_RELU>(ctx, epi, g, mtiles);
+    case TM_ACT_SIGMOID_WITH_PARAM: return run_gemm<PREC, TM_ACT_SIGMOID_WITH_PARAM>(ctx, epi, g, mtiles);
+    case TM_ACT_SOFTPLUS: return run_gemm<PREC, TM_ACT_SOFTPLUS>(ctx, epi, g, mtiles);
+    case TM_ACT_TANH: return run_gemm<PREC, TM_ACT_TANH>(ctx, epi, g, mtiles);
+    case TM_ACT_ELU: return run_gemm<PREC, TM_ACT_ELU>(ctx, epi, g, mtiles);
+    default: return tm_fail(ctx, TM_E_ARG, "activation");
+  }
+}
+
+int dispatch(tm_ctx* ctx, int prec, int epi, const GemmArgs& g, int mtiles) {
+  return prec == TM_PREC_FP32 ? run_gemm_act<TM_PREC_FP32>(ctx, epi, g, mtiles)
+                              : run_gemm_act<TM_PREC_BF16>(ctx, epi, g, mtiles);
 }
 
 }  // namespace
+
+int tm_gemm_bn(int prec) {
+  return prec == TM_PREC_FP32 ? Cfg<TM_PREC_FP32>::BN : Cfg<TM_PREC_BF16>::BN;
+}
 
 int tm_make_tmap(tm_ctx* ctx, CUtensorMap* map, void* base, int elem_bytes, uint64_t rows,
                  uint64_t cols, uint32_t box_rows) {
@@ -554,7 +586,7 @@ static int mlp_layers(tm_system* s, bool forward, bool backward) {
     g.ldo = H;
     g.out0 = last ? s->G3[0] : bufH[l][0];
     g.out1 = last ? s->G3[1] : bufH[l][1];
-    if ((rc = dispatch(ctx, prec, last ? EPI_FWD_LAST : EPI_FWD, g, mt, H / BN))) return rc;
+    if ((rc = dispatch(ctx, prec, last ? EPI_FWD_LAST : EPI_FWD, g, mt))) return rc;
   }
   if (!backward) return TM_OK;
   for (int l = L - 1; l >= 0; --l) {
@@ -575,13 +607,13 @@ static int mlp_layers(tm_system* s, bool forward, bool backward) {
       g.hprev1 = bufH[l - 1][1];
       g.out0 = bufH[l - 1][0];
       g.out1 = bufH[l - 1][1];
-      if ((rc = dispatch(ctx, prec, EPI_BWD, g, mt, H / BN))) return rc;
+      if ((rc = dispatch(ctx, prec, EPI_BWD, g, mt))) return rc;
     } else {
       g.N = Dp;
       g.ldo = Dp;
       g.out0 = s->dEdG;
       g.out1 = nullptr;
-      if ((rc = dispatch(ctx, prec, EPI_OUT, g, mt, Dp / BN))) return rc;
+      if ((rc = dispatch(ctx, prec, EPI_OUT, g, mt))) return rc;
     }
   }
   return TM_OK;
@@ -591,6 +623,7 @@ static int mlp_layers(tm_system* s, bool forward, bool backward) {
 // single element and net 0 (host fp32 in/out). Used by the GPU tests.
 int tm_gemm_selftest(tm_ctx* ctx, int prec, int M, int N, int K, const float* A, const float* B,
                      float* Cout) {
+  const int BN = tm_gemm_bn(prec);
   if (M % BM || N % BN || K % 64) return tm_fail(ctx, TM_E_ARG, "selftest shape");
   const int eb = prec == TM_PREC_FP32 ? 4 : 2;
   const size_t nA = (size_t)M * K, nB = (size_t)N * K, nC = (size_t)M * N;
@@ -598,12 +631,8 @@ int tm_gemm_selftest(tm_ctx* ctx, int prec, int M, int N, int K, const float* A,
   auto split = [&](const float* src, size_t n, uint8_t* d0, uint8_t* d1) {
     for (size_t q = 0; q < n; ++q) {
       if (prec == TM_PREC_FP32) {
-        uint32_t u;
-        memcpy(&u, &src[q], 4);
-        u &= 0xffffe000u;
-        float h;
-        memcpy(&h, &u, 4);
-        float lo = src[q] - h;
+        float h, lo;
+        tm_tf32_split(src[q], h, lo);
         memcpy(d0 + 4 * q, &h, 4);
         memcpy(d1 + 4 * q, &lo, 4);
       } else {
@@ -642,7 +671,7 @@ int tm_gemm_selftest(tm_ctx* ctx, int prec, int M, int N, int K, const float* A,
     return rc;
   g.K = K; g.N = N; g.a_net_rows = M; g.nele = 1; g.tile_elem = dte; g.Mpad = M;
   g.out0 = dc; g.out1 = dc1; g.ldo = N; g.st = st;
-  rc = dispatch(ctx, prec, EPI_OUT, g, M / BM, N / BN);
+  rc = dispatch(ctx, prec, EPI_OUT, g, M / BM);
   if (!rc) rc = tm_cuda_check(ctx, cudaMemcpyAsync(Cout, dc, nC * 4, cudaMemcpyDeviceToHost, sm), "selftest d2h");
   if (!rc) rc = tm_sync_status(ctx, "gemm selftest");
   tm_free(ctx, da0, nA * eb * 2); tm_free(ctx, da1, nA * eb * 2);

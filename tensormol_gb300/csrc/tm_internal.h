@@ -13,7 +13,7 @@
 
 #define TM_MAX_ELE 8
 #define TM_MAX_HIDDEN 4
-#define TM_BN 256          // GEMM N tile
+#define TM_BN 256          // padding of the hidden width H and descriptor width Dp
 #define TM_BM 128          // GEMM M tile (rows per element are padded to this)
 #define TM_EE_SPLIT 8      // warps sharing one Coulomb cell's candidate stencil
 
@@ -150,7 +150,7 @@ struct tm_system {
   void* H2[2] = {};
   void* G3[2] = {};
   float* dEdG = nullptr;               // [2*Mpad][Dp]
-  float* epart = nullptr;              // [2][Mpad][H/TM_BN]
+  float* epart = nullptr;              // [2][Mpad][H/tm_gemm_bn(precision)]
   CUtensorMap tm_G[2], tm_H1[2], tm_H2[2], tm_G3[2];
   // per atom
   double* d_Eatom = nullptr;           // [N]
@@ -201,6 +201,7 @@ int tm_make_tmap(tm_ctx* ctx, CUtensorMap* map, void* base, int elem_bytes, uint
                  uint64_t cols, uint32_t box_rows);
 int tm_launch_mlp(tm_system* s, bool backward);
 int tm_launch_mlp_backward_only(tm_system* s);
+int tm_gemm_bn(int prec);   // GEMM N tile of a precision mode (128 or 256)
 int tm_gemm_selftest(tm_ctx* ctx, int prec, int M, int N, int K, const float* A,
                      const float* B, float* C);
 // tm_coulomb.cu

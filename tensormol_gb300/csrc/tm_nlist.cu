@@ -673,7 +673,10 @@ __global__ void __launch_bounds__(128) k_ee_pairs(const EEArgs a) {
   const double xi = a.x[3 * i], yi = a.x[3 * i + 1], zi = a.x[3 * i + 2];
   const int lc = a.cell_of[i] - g.cell_off;
   const int iz = lc % g.nz, iy = (lc / g.nz) % g.ny, ix = lc / (g.nz * g.ny);
-  const int Rx = (int)ceil(a.ree / g.cx), Ry = (int)ceil(a.ree / g.cy), Rz = (int)ceil(a.ree / g.cz);
+  // periodic: at most one wrap per axis (R <= n; edges are >= 2 * cutoff)
+  const int Rx = a.periodic ? min((int)ceil(a.ree / g.cx), g.nx) : (int)ceil(a.ree / g.cx);
+  const int Ry = a.periodic ? min((int)ceil(a.ree / g.cy), g.ny) : (int)ceil(a.ree / g.cy);
+  const int Rz = a.periodic ? min((int)ceil(a.ree / g.cz), g.nz) : (int)ceil(a.ree / g.cz);
   const int nreal = g.natom;
   int64_t n = 0;
   int64_t base = FILL ? a.offs[i] : 0;

@@ -351,6 +351,13 @@ def EnergyAndForce(manager, atoms, Rr_cut=None, Ra_cut=None, Ree_cut=None):
             return o["Etotal"][0], o["force"]
         return o["Etotal"][0]
 
+    def system_for(x_):
+        """The device system behind the closure, holding positions x_ (the
+        device integrators in ``tensormol_gb300.md`` drive it directly)."""
+        sysm.set_positions(np.asarray(x_, dtype=_F64))
+        return sysm
+
+    EnAndForce.system_for = system_for
     return EnAndForce
 
 

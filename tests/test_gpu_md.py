@@ -1,0 +1,229 @@
+"""GPU parity of the device integrators (tm_md_*, through the C ABI) against
+the oracle's FP64 restatement of Simulations/SimpleMD.py driven by the oracle's
+own FP64 forces.
+
+The two trajectories differ only through the FP32 force error (~1e-5 eV/A
+here), so after 20 steps of 0.5 fs they agree to well below the stated bounds:
+positions 1e-5 A, velocities 5e-6 A/fs, potential 1e-5 eV/atom, kinetic and
+conserved energies 0.5 J/mol per atom (about 1e-4 of the kinetic energy per
+atom at 300 K, 3.7 kJ/mol), T_eff 1e-4 relative. The smooth activation
+(sigmoid_with_param) is used: relu forces jump at kinks, which makes any two
+trajectories separate at the first kink crossing.
+"""
+import numpy as np
+import pytest
+
+from oracle import reference as orc
+from tensormol_gb300 import systems
+from tensormol_gb300.params import EV_PER_HARTREE, IDEALGASR, JOULEPERHARTREE, PARAMS, descriptor_width
+
+pytestmark = pytest.mark.gpu
+
+X_TOL = 1e-5       # A
+V_TOL = 5e-6       # A/fs
+E_TOL = 1e-5       # eV / atom (potential)
+J_TOL = 0.5        # J/mol per atom (kinetic, conserved)
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from tensormol_gb300 import md, model
+    return model, md
+
+
+def _models(model, eles, **kw):
+    p = dict(PARAMS)
+    p["NeuronType"] = "sigmoid_with_param"
+    p.update(kw)
+    W = systems.random_weights(eles, descriptor_width(len(eles)), seed=7)
+    return model.BPEEModel(eles, W, params=p, precision="fp32"), orc.Model(eles, W, params=p)
+
+
+def _open_ef(om, Z, off):
+    def ef(x):
+        o = orc.OpenSystemOracle(om, x, Z, off).terms(x)
+        return float(o["Etotal"].sum()), o["force"]
+    return ef
+
+
+def _compare(log, X, V, ref_x, ref_v, ref_log, n):
+    dx = np.abs(X - ref_x).max()
+    dv = np.abs(V - ref_v).max()
+    dpe = np.abs(log[:, 0] - ref_log[:, 0]).max() * EV_PER_HARTREE / n
+    dke = np.abs(log[:, 1] - ref_log[:, 1]).max()
+    dcons = np.abs(log[:, 2] - ref_log[:, 2]).max() / n
+    assert dx < X_TOL and dv < V_TOL, (dx, dv)
+    assert dpe < E_TOL and dke < J_TOL and dcons < J_TOL, (dpe, dke, dcons)
+    np.testing.assert_allclose(log[:, 3], ref_log[:, 3], rtol=1e-4, atol=1e-3)
+
+
+def _teff(ke_per_atom):
+    return (2.0 / 3.0) * ke_per_atom / IDEALGASR
+
+
+def test_nve_velocity_verlet_water60(gpu):
+    model, md = gpu
+    w = systems.water_cluster_60(seed=0)
+    m, om = _models(model, [1, 8])
+    s = m.system(w.x, w.Z, w.offsets)
+    v0 = systems.maxwell_boltzmann(w.Z, 300.0, seed=11)
+    dyn = md.DeviceMD(s, "nve", dt=0.5, T=300.0)
+    dyn.set_velocities(v0)
+    nst = 20
+    log = dyn.run(nst)
+    X, V = s.positions(), dyn.velocities()
+    # oracle: VelocityVerletStep with a0 = 0 (SimpleMD.py:14-38, :359)
+    ef = _open_ef(om, w.Z, w.offsets)
+    mass = systems.masses(w.Z)
+    x, v, a = w.x.copy(), v0.copy(), np.zeros_like(w.x)
+    ref = np.zeros((nst, 4))
+    for k in range(nst):
+        x, v, a, e = orc.vv_step(ef, a, x, v, mass, 0.5)
+        ke = orc.kinetic_energy(v, mass)
+        ref[k] = (e, ke, ke * w.natoms + e * JOULEPERHARTREE, _teff(ke))
+    _compare(log, X, V, x, v, ref, w.natoms)
+    dyn.close()
+    s.close()
+
+
+def test_nose_thermostat_water60(gpu):
+    model, md = gpu
+    w = systems.water_cluster_60(seed=0)
+    m, om = _models(model, [1, 8])
+    s = m.system(w.x, w.Z, w.offsets)
+    v0 = systems.maxwell_boltzmann(w.Z, 300.0, seed=12) * 1.5   # start hot: eta moves
+    dt, T, nst = 0.5, 300.0, 20
+    dyn = md.DeviceMD(s, "nose", dt=dt, T=T)
+    dyn.set_velocities(v0)
+    log = dyn.run(nst)
+    X, V = s.positions(), dyn.velocities()
+    ef = _open_ef(om, w.Z, w.offsets)
+    mass = systems.masses(w.Z)
+    th = orc.Nose(mass, T, dt)
+    x, v, a = w.x.copy(), v0.copy(), np.zeros_like(w.x)
+    ref = np.zeros((nst, 4))
+    xi = 0.0
+    for k in range(nst):
+        e0 = th.eta
+        x, v, a, e = th.step(ef, a, x, v)
+        xi += 0.5 * (e0 + th.eta) * dt
+        ke = orc.kinetic_energy(v, mass)
+        ext = (0.5 * th.Q * th.eta ** 2 + (3.0 * w.natoms + 1.0) * th.kT * xi) * 1e10
+        ref[k] = (e, ke, ke * w.natoms + e * JOULEPERHARTREE + ext, _teff(ke))
+    assert abs(th.eta) > 0.0
+    _compare(log, X, V, x, v, ref, w.natoms)
+    dyn.close()
+    s.close()
+
+
+def _nhc_reference(ef, x, v, mass, T, dt, nst, M=3, wrap=None):
+    th = orc.NoseHooverChain(mass, T, dt, M=M)
+    a = np.zeros_like(x)
+    ref = np.zeros((nst, 4))
+    n = len(mass)
+    for k in range(nst):
+        x, v, a, e = th.step(ef, a, x, v)
+        if wrap is not None:
+            x = wrap(x)
+        ke = orc.kinetic_energy(v, mass)
+        ref[k] = (e, ke, th.conserved(v, e * JOULEPERHARTREE), _teff(ke))
+    return x, v, ref
+
+
+def test_nose_hoover_chain_water60(gpu):
+    model, md = gpu
+    w = systems.water_cluster_60(seed=0)
+    m, om = _models(model, [1, 8])
+    s = m.system(w.x, w.Z, w.offsets)
+    v0 = systems.maxwell_boltzmann(w.Z, 300.0, seed=13) * 1.5
+    dt, T, nst = 0.5, 300.0, 20
+    dyn = md.DeviceMD(s, "nhc", dt=dt, T=T, chain=3)
+    dyn.set_velocities(v0)
+    log = dyn.run(nst)
+    X, V = s.positions(), dyn.velocities()
+    x, v, ref = _nhc_reference(_open_ef(om, w.Z, w.offsets), w.x.copy(), v0.copy(),
+                               systems.masses(w.Z), T, dt, nst)
+    _compare(log, X, V, x, v, ref, w.natoms)
+    dyn.close()
+    s.close()
+
+
+def test_nose_hoover_chain_periodic_box(gpu):
+    """NHC-3 in a periodic water box (216 H2O, 18.6 A cell, 9 A Coulomb
+    cutoff): positions wrapped into the cell each step, as Prop does with a
+    cellsize (SimpleMD.py:398-399)."""
+    model, md = gpu
+    L = 18.6
+    b = systems.water(216, seed=6, spacing=L / 6.0, box=L, n_side=6)
+    lat = np.eye(3) * L
+    x0 = orc.modulo_lattice(b.x, lat)
+    m, om = _models(model, [1, 8], EECutoffOff=9.0)
+    s = m.system(x0, b.Z, None, lat)
+    v0 = systems.maxwell_boltzmann(b.Z, 300.0, seed=14)
+    dt, T, nst = 0.5, 300.0, 10
+    dyn = md.DeviceMD(s, "nhc", dt=dt, T=T, chain=3)
+    dyn.set_velocities(v0)
+    log = dyn.run(nst)
+    X, V = s.positions(), dyn.velocities()
+
+    def ef(x):
+        o = orc.PeriodicOracle(om, x, b.Z, lat, ree_cut=9.0).terms(x)
+        return float(o["Etotal"].sum()), o["force"]
+
+    x, v, ref = _nhc_reference(ef, x0.copy(), v0.copy(), systems.masses(b.Z), T, dt, nst,
+                               wrap=lambda y: orc.modulo_lattice(y, lat))
+    d = X - x
+    d -= L * np.round(d / L)   # same point of the cell
+    X = x + d
+    _compare(log, X, V, x, v, ref, len(b.Z))
+    dyn.close()
+    s.close()
+
+
+def test_nve_100_steps_conserves_energy_water60(gpu):
+    """C0: E+F then 100 NVE steps of 0.5 fs; the conserved energy drifts by
+    less than 1% of the kinetic energy."""
+    model, md = gpu
+    w = systems.water_cluster_60(seed=0)
+    m, _ = _models(model, [1, 8])
+    s = m.system(w.x, w.Z, w.offsets)
+    dyn = md.DeviceMD(s, "nve", dt=0.5, T=300.0)
+    dyn.set_velocities(systems.maxwell_boltzmann(w.Z, 300.0, seed=11))
+    log = dyn.run(100)
+    ke_tot = log[:, 1].mean() * w.natoms
+    drift = abs(log[-1, 2] - log[0, 2])
+    print(f"NVE water60 100 steps: drift {drift:.3e} J/mol, <KE> {ke_tot:.3e} J/mol")
+    assert np.all(np.isfinite(log)) and drift < 0.01 * ke_tot
+    dyn.close()
+    s.close()
+
+
+def test_velocity_verlet_driver_mirror(gpu):
+    """tensormol_gb300.md.VelocityVerlet: the reference driver's interface
+    (SimpleMD.py:322-424) over the device integrator."""
+    model, md = gpu
+    from tensormol_gb300.model import EnergyAndForce, Mol, TFMolManage
+    w = systems.water_cluster_60(seed=0)
+    m, om = _models(model, [1, 8])
+    EF = EnergyAndForce(TFMolManage(m), w.Z)
+    saved = {k: PARAMS.get(k) for k in ("MDMaxStep", "MDdt", "MDThermostat", "MDV0")}
+    try:
+        PARAMS.update(MDMaxStep=10, MDdt=0.5, MDThermostat=None, MDV0=None)
+        vv = md.VelocityVerlet(None, Mol(w.Z, w.x), "w60", EF)
+        mdlog = vv.Prop()
+    finally:
+        PARAMS.update(saved)
+    ef = _open_ef(om, w.Z, w.offsets)
+    e0, _ = ef(w.x)
+    assert abs(vv.EPot0 - e0) * EV_PER_HARTREE / w.natoms < E_TOL
+    # zero initial velocities: the first step does not move the atoms (a0 = 0)
+    x, v, a = w.x.copy(), np.zeros_like(w.x), np.zeros_like(w.x)
+    mass = systems.masses(w.Z)
+    for _ in range(10):
+        x, v, a, e = orc.vv_step(ef, a, x, v, mass, 0.5)
+    assert np.abs(vv.x - x).max() < X_TOL
+    assert mdlog.shape == (10, 7) and mdlog[0, 4] == 0.0
+    assert abs(mdlog[-1, 5] - e) * EV_PER_HARTREE / w.natoms < E_TOL

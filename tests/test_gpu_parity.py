@@ -202,3 +202,28 @@ def test_energy_force_chno128_smooth(gpu):
     dE = np.max(np.abs(out["Etotal"] - ref["Etotal"]) * EV_PER_HARTREE / n_per)
     dF = np.abs(out["force"] - ref["force"]).max() / JOULEPERHARTREE * EV_PER_HARTREE
     assert dE < E_TOL and dF < F_TOL, (dE, dF)
+
+
+def test_energy_force_chno512_with_finite_differences(gpu):
+    """512 CHNO molecules of 8-64 atoms in one fused E+F: totals and forces
+    against the FP64 oracle, and forces of a few atoms against central finite
+    differences (h = 1e-4 A) of the oracle's energy."""
+    b = systems.chno_batch(nmol=512, seed=3)
+    m, om = _model(gpu, [1, 6, 7, 8], "sigmoid_with_param")
+    s = m.system(b.x, b.Z, b.offsets)
+    out = s.energy_force(b.x, True)
+    o = orc.OpenSystemOracle(om, b.x, b.Z, b.offsets)
+    ref = o.terms(b.x)
+    n_per = np.diff(b.offsets)
+    dE = np.max(np.abs(out["Etotal"] - ref["Etotal"]) * EV_PER_HARTREE / n_per)
+    dF = np.abs(out["force"] - ref["force"]).max() / JOULEPERHARTREE * EV_PER_HARTREE
+    assert dE < E_TOL and dF < F_TOL, (dE, dF)
+    # molecules are independent: differentiate each sampled atom's own molecule
+    rng = np.random.default_rng(0)
+    for mol in rng.choice(len(n_per), 4, replace=False):
+        a0, a1 = b.offsets[mol], b.offsets[mol + 1]
+        om1 = orc.OpenSystemOracle(om, b.x[a0:a1], b.Z[a0:a1], np.array([0, a1 - a0]))
+        atoms = rng.choice(a1 - a0, 2, replace=False)
+        fd = -om1.fd_gradient(b.x[a0:a1], atoms, h=1e-4) * JOULEPERHARTREE
+        dfd = np.abs(out["force"][a0 + atoms] - fd).max() / JOULEPERHARTREE * EV_PER_HARTREE
+        assert dfd < 1e-3, (mol, dfd)
