@@ -244,6 +244,72 @@ def smooth_accuracy(w, eles, flush, torch):
     return errors(o["Etotal"], o["force"], ref, w.natoms)
 
 
+def serve_workload(seed=4, nreq=160, nmin=10, nmax=5000, md_frac=0.8, md_steps=50):
+    """Serving requests: N log-uniform in [nmin, nmax] atoms (water clusters of
+    round(N/3) molecules), md_frac of them 50-step NVE runs, the rest single
+    energy+force evaluations; Maxwell-Boltzmann velocities at 300 K."""
+    from tensormol_gb300 import serve, systems
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for q in range(nreq):
+        n = float(np.exp(rng.uniform(np.log(nmin), np.log(nmax))))
+        nmol = max(4, int(round(n / 3.0)))
+        w = systems.water(nmol, seed=1000 + q, spacing=3.1)
+        md = rng.uniform() < md_frac
+        v = systems.maxwell_boltzmann(w.Z, 300.0, seed=5000 + q) if md else None
+        reqs.append(serve.Request(w.Z, w.x, kind="md" if md else "ef", nsteps=md_steps, v=v))
+    return reqs
+
+
+def time_serving(model, max_atoms=32768, max_mols=256, load=1.1):
+    """Offline: every request submitted at once, batches kept full. Online:
+    Poisson arrivals whose offered atom-steps/s is `load` x the offline rate;
+    step latency p50/p99 and achieved throughput under continuous batching."""
+    from tensormol_gb300 import serve
+    warm = serve.Server(model, max_atoms, max_mols)
+    for r in serve_workload(seed=9, nreq=8, nmax=2000, md_steps=5):
+        warm.submit(r)
+    warm.drain()
+    warm.close()
+    reqs = serve_workload()
+    work = sum(r.natoms * r.nsteps for r in reqs)
+    off = serve.Server(model, max_atoms, max_mols)
+    t0 = time.perf_counter()
+    for r in reqs:
+        off.submit(r, now=t0)
+    off.drain()
+    t_off = time.perf_counter() - t0
+    offline = off.stats(t_off)
+    off.close()
+    rate = offline["atom_steps_per_s"]
+    lam = load * rate / (work / len(reqs))                      # requests per second
+    rng = np.random.default_rng(44)
+    reqs = serve_workload()
+    t = 0.0
+    for r in reqs:
+        t += rng.exponential(1.0 / lam)
+        r.arrival = t
+    srv = serve.Server(model, max_atoms, max_mols)
+    wall = srv.run_arrivals(reqs)
+    online = srv.stats(wall)
+    lat = np.array([(r.t_done - r.t_submit) * 1e3 for r in reqs])
+    srv.close()
+    return {"requests": len(reqs), "atom_steps": int(work),
+            "capacity": {"max_atoms": max_atoms, "max_mols": max_mols},
+            "offline": {"atom_steps_per_s": rate, "p50_step_ms": offline["p50_ms"],
+                        "p99_step_ms": offline["p99_ms"], "steps": offline["steps"]},
+            "online": {"arrival_rate_per_s": lam, "offered_load_vs_offline": load,
+                       "atom_steps_per_s": online["atom_steps_per_s"],
+                       "p50_step_ms": online["p50_ms"], "p99_step_ms": online["p99_ms"],
+                       "p99_over_p50": online["p99_ms"] / online["p50_ms"],
+                       "throughput_vs_offline": online["atom_steps_per_s"] / rate,
+                       "mean_batch_atoms": online["mean_batch_atoms"],
+                       "request_latency_p50_ms": float(np.percentile(lat, 50)),
+                       "request_latency_p99_ms": float(np.percentile(lat, 99))},
+            "workload": "N log-uniform [10, 5000] atoms (water clusters), 80% 50-step NVE "
+                        "(dt 0.5 fs), 20% single E+F; Poisson arrivals"}
+
+
 def run_reference(args):
     """CPU implementation of the path (the oracle port), bounded sample."""
     ws, rank, _ = _dist()
@@ -295,6 +361,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle leg")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving-loop measurement")
     ap.add_argument("--fused-only", action="store_true",
                     help="time only the device-resident fused E+F (for profiler launch lists)")
     args = ap.parse_args()
@@ -340,6 +407,7 @@ def main():
     e2e_t, h2d, d2h = time_e2e(model, s, w, args.steps, args.warmup, torch)
     e2e_ms = sum(e2e_t) / len(e2e_t)
     s.close()
+    serving = None if args.no_serve else time_serving(model)
     # BF16 variant
     _, _, _, model16 = build_workload("bf16")
     s16, t16, _, _, E16, F16 = time_fused_device(model16, w, args.steps, args.warmup, flush, torch)
@@ -379,6 +447,7 @@ def main():
             "gpu_launches": int(launches), "clocks": clocks, "stages_ms": stages, "roofline": roof,
             "bf16": {"value": natoms / (ms16 / 1000.0), "ms_per_step": ms16},
             "plain_autograd": plain,
+            "serve": serving,
             "published_reference": {"value": 274.0, "unit": UNIT, "hardware": "2015 Core i7, 1 core",
                                     "source": "24,000 atoms / ~87.5 s read off doc/images/Timings.png"}}
     if rank == 0:

@@ -62,6 +62,7 @@ typedef struct tm_ctx tm_ctx;
 typedef struct tm_model tm_model;
 typedef struct tm_system tm_system;
 typedef struct tm_md tm_md;
+typedef struct tm_serve tm_serve;
 
 /*
  * Model description. Mirrors MolInstance_DirectBP_EE_SymFunction's
@@ -190,6 +191,38 @@ int tm_md_get_velocities(tm_md *md, double *v, int on_device);
  * (potential Hartree, kinetic J/mol per atom, conserved J/mol, T_eff K).
  */
 int tm_md_run(tm_md *md, int nsteps, double skin, double *log);
+
+/* ---- serving: continuous batching of requests -------------------------- */
+/*
+ * No single counterpart in the reference: its drivers call EnergyAndForce
+ * once per molecule and step (samples/test_tensormol01.py:61-69,
+ * SimpleMD.py:391-424). A tm_serve holds up to max_atoms atoms in up to
+ * max_mols molecules (one molecule per request in flight, device memory
+ * allocated once, against the context's HBM budget) and advances all of them
+ * with one fused energy+force evaluation per step.
+ */
+#define TM_SERVE_EF 0   /* energy + force at fixed positions          */
+#define TM_SERVE_MD 1   /* velocity-Verlet step (SimpleMD.py:14-38)   */
+int tm_serve_create(tm_model *m, int max_atoms, int max_mols, double dt_fs, tm_serve **out);
+int tm_serve_destroy(tm_serve *sv);
+int tm_serve_info(const tm_serve *sv, int *max_atoms, int *max_mols, int *natoms, int *nmol,
+                  size_t *bytes);
+/*
+ * New batch composition: nmol molecules (Z, offsets as tm_system_create,
+ * mode[nmol] = TM_SERVE_*). src[natoms] gives, per atom of the new layout, its
+ * index in the previous layout (its positions, velocities and accelerations
+ * are kept on the device) or -(k+1) for the k-th new atom, whose position and
+ * velocity are x_new[k], v_new[k] (host, packed) and whose acceleration starts
+ * at zero (SimpleMD.py:359). nmol = 0 empties the batch. TM_E_CAPACITY when
+ * the layout does not fit.
+ */
+int tm_serve_layout(tm_serve *sv, int nmol, const int32_t *Z, const int64_t *offsets,
+                    const int32_t *mode, const int32_t *src, const double *x_new,
+                    const double *v_new);
+/* One step of every molecule; E_out[nmol][4] (host, may be NULL) as tm_energy_force. */
+int tm_serve_step(tm_serve *sv, double *E_out);
+/* Positions, velocities, forces (J/mol/A) of molecule mol to host (each may be NULL). */
+int tm_serve_read(tm_serve *sv, int mol, double *x, double *v, double *F);
 
 /* ---- allocation-free entry point ---------------------------------------- */
 /*

@@ -22,6 +22,7 @@ TM_F_DEVICE_IO = 2
 TM_F_REUSE_NLIST = 4
 TM_F_REFERENCE_PERIODIC_FORCE = 8
 TM_MD = {"nve": 0, "nose": 1, "nhc": 2}
+TM_SERVE = {"ef": 0, "md": 1}
 
 # every symbol include/tmgpu.h declares
 EXPORTS = [
@@ -35,6 +36,8 @@ EXPORTS = [
     "tm_md_create", "tm_md_destroy", "tm_md_set_velocities", "tm_md_get_velocities", "tm_md_run",
     "tm_selftest_gemm", "tm_system_descriptors", "tm_energy_force_profile",
     "tm_nlist_build_static",
+    "tm_serve_create", "tm_serve_destroy", "tm_serve_info", "tm_serve_layout", "tm_serve_step",
+    "tm_serve_read",
 ]
 
 
@@ -98,6 +101,12 @@ def _declare(lib):
         "tm_system_descriptors": (I, [P, P]),
         "tm_energy_force_profile": (I, [P, U, P]),
         "tm_nlist_build_static": (I, [P, P, I, D, D, P, P, I, P, P, I, P, P]),
+        "tm_serve_create": (I, [P, I, I, D, PP]),
+        "tm_serve_destroy": (I, [P]),
+        "tm_serve_info": (I, [P, P, P, P, P, P]),
+        "tm_serve_layout": (I, [P, I, P, P, P, P, P, P]),
+        "tm_serve_step": (I, [P, P]),
+        "tm_serve_read": (I, [P, I, P, P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -381,114 +381,159 @@ struct AllocList {
 
 static void system_free(tm_system* s);
 
-extern "C" int tm_system_create(tm_model* m, int N, int nmol, const int32_t* Z,
-                                const int64_t* off, const double* cell, tm_system** out) {
-  *out = nullptr;
-  if (!m || !Z || !off || N <= 0 || nmol <= 0) return tm_fail(m ? m->ctx : nullptr, TM_E_ARG, "system args");
-  tm_ctx* ctx = m->ctx;
-  if (!m->final_) return tm_fail(ctx, TM_E_STATE, "model weights are not finalized");
+// Host-side tables of one layout: a batch of molecules in CSR order.
+struct SysLayout {
+  int N = 0, nmol = 0, Mpad = 0, ntiles = 0, nchunk = 0, ncell_cap = 0, ecell_cap = 0;
+  std::vector<int32_t> Z, elem, row_of_atom, atom_of_row, tile_elem, mol, off32, mol_chunk;
+  std::vector<int64_t> off;
+  std::vector<int2> chunks;
+};
+
+static int build_layout(tm_system* s, int N, int nmol, const int32_t* Z, const int64_t* off,
+                        SysLayout& L) {
+  tm_ctx* ctx = s->ctx;
+  const tm_consts& k = s->model->k;
+  if (N <= 0 || nmol <= 0 || !Z || !off) return tm_fail(ctx, TM_E_ARG, "system args");
   if (off[0] != 0 || off[nmol] != N) return tm_fail(ctx, TM_E_ARG, "mol_offsets must span 0..natoms");
   for (int q = 0; q < nmol; ++q)
     if (off[q + 1] <= off[q]) return tm_fail(ctx, TM_E_ARG, "empty or unsorted molecule");
   if (N >= (1 << 27)) return tm_fail(ctx, TM_E_ARG, "too many atoms");
-  tm_system* s = new tm_system();
-  s->model = m;
-  s->ctx = ctx;
-  s->N = N;
-  s->nmol = nmol;
-  s->Z.assign(Z, Z + N);
-  s->off.assign(off, off + nmol + 1);
-  const tm_consts& k = m->k;
-  if (cell) {
-    for (int q = 0; q < 9; ++q) s->lat[q] = cell[q];
-    if (cell[1] != 0 || cell[2] != 0 || cell[3] != 0 || cell[5] != 0 || cell[6] != 0 || cell[7] != 0) {
-      delete s;
-      return tm_fail(ctx, TM_E_UNSUPPORTED, "only orthorhombic cells are supported");
-    }
-    if (nmol != 1) { delete s; return tm_fail(ctx, TM_E_ARG, "a periodic system is one molecule"); }
-    const double Lmin = std::min(cell[0], std::min(cell[4], cell[8]));
-    const double rmax = std::max(k.r_rc_d, k.ree_d);
-    if (Lmin < 2.0 * rmax) {
-      delete s;
-      return tm_fail(ctx, TM_E_ARG, "cell edges must be at least twice the largest cutoff");
-    }
-    // With edges >= 2 * cutoff, a +-R cell search (R = ceil(cutoff / cell
-    // edge) <= ceil(n / 2) <= n) wraps at most once per axis and reaches each
-    // (cell, image) at most once; the exact distance test keeps the one image
-    // within the cutoff.
-    s->periodic = true;
-  }
-  // elements and element-sorted rows
-  s->elem_h.resize(N);
+  L.N = N;
+  L.nmol = nmol;
+  L.Z.assign(Z, Z + N);
+  L.off.assign(off, off + nmol + 1);
+  // elements and element-sorted rows (each element padded to TM_BM rows)
+  L.elem.resize(N);
   std::vector<int> count(k.nele, 0);
   for (int i = 0; i < N; ++i) {
     int e = -1;
     for (int q = 0; q < k.nele; ++q)
-      if (m->desc.elements[q] == Z[i]) e = q;
-    if (e < 0) { delete s; return tm_fail(ctx, TM_E_ARG, "atom element not in the model"); }
-    s->elem_h[i] = e;
+      if (s->model->desc.elements[q] == Z[i]) e = q;
+    if (e < 0) return tm_fail(ctx, TM_E_ARG, "atom element not in the model");
+    L.elem[i] = e;
     count[e]++;
   }
   std::vector<int> row_off(k.nele + 1, 0);
   for (int e = 0; e < k.nele; ++e) row_off[e + 1] = row_off[e] + ((count[e] + TM_BM - 1) / TM_BM) * TM_BM;
-  s->Mpad = row_off[k.nele];
-  s->ntiles = s->Mpad / TM_BM;
-  s->row_of_atom_h.resize(N);
+  L.Mpad = row_off[k.nele];
+  L.ntiles = L.Mpad / TM_BM;
+  L.row_of_atom.resize(N);
+  L.atom_of_row.assign(L.Mpad, -1);
   std::vector<int> fill(k.nele, 0);
-  std::vector<int32_t> atom_of_row(s->Mpad, -1);
   for (int i = 0; i < N; ++i) {
-    const int e = s->elem_h[i];
+    const int e = L.elem[i];
     const int r = row_off[e] + fill[e]++;
-    s->row_of_atom_h[i] = r;
-    atom_of_row[r] = i;
+    L.row_of_atom[i] = r;
+    L.atom_of_row[r] = i;
   }
-  s->tile_elem_h.resize(s->ntiles);
+  L.tile_elem.resize(L.ntiles);
   for (int e = 0; e < k.nele; ++e)
-    for (int r = row_off[e]; r < row_off[e + 1]; r += TM_BM) s->tile_elem_h[r / TM_BM] = e;
-  std::vector<int32_t> mol(N);
+    for (int r = row_off[e]; r < row_off[e + 1]; r += TM_BM) L.tile_elem[r / TM_BM] = e;
+  L.mol.resize(N);
   for (int q = 0; q < nmol; ++q)
-    for (int64_t i = off[q]; i < off[q + 1]; ++i) mol[i] = q;
-  std::vector<int32_t> off32(nmol + 1);
-  for (int q = 0; q <= nmol; ++q) off32[q] = (int32_t)off[q];
-  s->ncell_cap = s->periodic ? 0 : 2 * N + 64 * nmol;
-  if (s->periodic) {
-    long nc = 1;
-    for (int d = 0; d < 3; ++d) nc *= (long)floor(s->lat[4 * d] / k.r_rc_d);
-    s->ncell_cap = (int)nc;
-  }
-  // Coulomb grid: about 24 atoms per cell (periodic: floor(L / size) cells per
-  // edge); open: at most n/8 + 8 cells per molecule (the device grows the cell
-  // size until a molecule fits, with the same bound)
-  s->ecell_cap = 0;
-  for (int q = 0; q < nmol; ++q) s->ecell_cap += (int)((off[q + 1] - off[q]) / 8) + 8;
-  if (s->periodic) {
-    const double vol = s->lat[0] * s->lat[4] * s->lat[8];
-    const double cs = std::max(2.0, cbrt(24.0 * vol / N));
-    long nc = 1;
-    for (int d = 0; d < 3; ++d) {
-      const double L = s->lat[4 * d];
-      const int n = std::max(1, std::min(4096, (int)floor(L / cs)));
-      s->ee_dims[d] = n;
-      nc *= n;
-    }
-    s->ecell_cap = (int)nc;
-  }
-  std::vector<int2> chunks;
-  std::vector<int32_t> mol_chunk(nmol + 1, 0);
+    for (int64_t i = off[q]; i < off[q + 1]; ++i) L.mol[i] = q;
+  L.off32.resize(nmol + 1);
+  for (int q = 0; q <= nmol; ++q) L.off32[q] = (int32_t)off[q];
+  // chunks of at most 1024 atoms of one molecule (two-level reductions)
+  L.mol_chunk.assign(nmol + 1, 0);
   for (int q = 0; q < nmol; ++q) {
-    mol_chunk[q] = (int32_t)chunks.size();
+    L.mol_chunk[q] = (int32_t)L.chunks.size();
     for (int64_t b = off[q]; b < off[q + 1]; b += 1024)
-      chunks.push_back(make_int2((int)b, (int)std::min<int64_t>(b + 1024, off[q + 1])));
+      L.chunks.push_back(make_int2((int)b, (int)std::min<int64_t>(b + 1024, off[q + 1])));
   }
-  mol_chunk[nmol] = (int32_t)chunks.size();
-  s->nchunk = (int)chunks.size();
-  const int H = m->H, Dp = k.Dp;
+  L.mol_chunk[nmol] = (int32_t)L.chunks.size();
+  L.nchunk = (int)L.chunks.size();
+  // cell bounds: neighbour grid (open: at most 2n + 64 cells per molecule) and
+  // Coulomb grid (about 24 atoms per cell; open: at most n/8 + 8 per molecule,
+  // the device grows the cell size until a molecule fits within the bound)
+  if (s->periodic) {
+    long nc = 1, ne = 1;
+    for (int d = 0; d < 3; ++d) {
+      nc *= (long)floor(s->lat[4 * d] / k.r_rc_d);
+      ne *= s->ee_dims[d];
+    }
+    L.ncell_cap = (int)nc;
+    L.ecell_cap = (int)ne;
+  } else {
+    L.ncell_cap = 2 * N + 64 * nmol;
+    L.ecell_cap = 0;
+    for (int q = 0; q < nmol; ++q) L.ecell_cap += (int)((off[q + 1] - off[q]) / 8) + 8;
+  }
+  return TM_OK;
+}
+
+// Zero the descriptor rows of the padding rows (atom_of_row < 0), so that
+// rows left from an earlier layout never reach the networks.
+__global__ void k_zero_pad_rows(const int32_t* __restrict__ atom_of_row, int Mpad, int Dp,
+                                float* __restrict__ g0, float* __restrict__ g1, int words) {
+  const int r = blockIdx.x;
+  if (r >= Mpad || atom_of_row[r] >= 0) return;
+  for (int c = threadIdx.x; c < words; c += blockDim.x) {
+    g0[(size_t)r * words + c] = 0.f;
+    if (g1) g1[(size_t)r * words + c] = 0.f;
+  }
+}
+
+static int upload_layout(tm_system* s, SysLayout& L) {
+  tm_ctx* ctx = s->ctx;
+  const tm_model* m = s->model;
+  if (L.N > s->N_cap || L.nmol > s->nmol_cap || L.Mpad > s->Mpad_cap || L.nchunk > s->nchunk_cap ||
+      L.ncell_cap > s->ncell_alloc || L.ecell_cap > s->ecell_alloc)
+    return tm_fail(ctx, TM_E_CAPACITY, "layout exceeds the system's capacity");
+  s->N = L.N;
+  s->nmol = L.nmol;
+  s->Z = L.Z;
+  s->off = L.off;
+  s->elem_h = L.elem;
+  s->Mpad = L.Mpad;
+  s->ntiles = L.ntiles;
+  s->row_of_atom_h = L.row_of_atom;
+  s->tile_elem_h = L.tile_elem;
+  s->nchunk = L.nchunk;
+  s->ncell_cap = L.ncell_cap;
+  s->ecell_cap = L.ecell_cap;
+  s->nlist_valid = false;
+  cudaStream_t st = ctx->stream;
+  const int N = L.N, nmol = L.nmol;
+  cudaMemcpyAsync(s->row_of_atom, L.row_of_atom.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s->atom_of_row, L.atom_of_row.data(), sizeof(int32_t) * L.Mpad, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s->tile_elem, L.tile_elem.data(), sizeof(int32_t) * L.ntiles, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s->d_Z, L.Z.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s->d_elem, L.elem.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s->d_mol, L.mol.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s->d_off, L.off32.data(), sizeof(int32_t) * (nmol + 1), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s->d_chunk, L.chunks.data(), sizeof(int2) * L.nchunk, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(s->d_mol_chunk, L.mol_chunk.data(), sizeof(int32_t) * (nmol + 1),
+                  cudaMemcpyHostToDevice, st);
+  const bool split = m->desc.precision == TM_PREC_FP32;
+  const int words = (int)(m->k.Dp * m->elem_size / 4);
+  k_zero_pad_rows<<<L.Mpad, 128, 0, st>>>(s->atom_of_row, L.Mpad, m->k.Dp, (float*)s->G[0],
+                                          split ? (float*)s->G[1] : nullptr, words);
+  ctx->launches++;
+  // the host tables must outlive the copies
+  return tm_cuda_check(ctx, cudaStreamSynchronize(st), "system upload");
+}
+
+// Device buffers for up to N_cap atoms / nmol_cap molecules and the given
+// cell, chunk and row bounds; any layout within them can be uploaded later.
+static int system_alloc(tm_system* s, int N_cap, int nmol_cap, int Mpad_cap, int nchunk_cap,
+                        int ncell_alloc, int ecell_alloc) {
+  tm_ctx* ctx = s->ctx;
+  const tm_model* m = s->model;
+  s->N_cap = N_cap;
+  s->nmol_cap = nmol_cap;
+  s->Mpad_cap = Mpad_cap;
+  s->nchunk_cap = nchunk_cap;
+  s->ncell_alloc = ncell_alloc;
+  s->ecell_alloc = ecell_alloc;
+  const int N = N_cap, nmol = nmol_cap;
+  const int H = m->H, Dp = m->k.Dp;
   const size_t es = m->elem_size;
-  const size_t Mp = s->Mpad;
+  const size_t Mp = Mpad_cap;
   AllocList A{s};
   A.get(&s->row_of_atom, sizeof(int32_t) * N);
   A.get(&s->atom_of_row, sizeof(int32_t) * Mp);
-  A.get(&s->tile_elem, sizeof(int32_t) * s->ntiles);
+  A.get(&s->tile_elem, sizeof(int32_t) * (Mp / TM_BM));
   A.get(&s->d_Z, sizeof(int32_t) * N);
   A.get(&s->d_elem, sizeof(int32_t) * N);
   A.get(&s->d_mol, sizeof(int32_t) * N);
@@ -501,19 +546,19 @@ extern "C" int tm_system_create(tm_model* m, int N, int nmol, const int32_t* Z,
   A.get(&s->d_ncell, sizeof(int32_t));
   A.get(&s->d_ncell_m, sizeof(int32_t) * nmol);
   A.get(&s->d_need, sizeof(int32_t) * 2);
-  A.get(&s->d_cell_cnt, sizeof(int32_t) * (s->ncell_cap + 1));
-  A.get(&s->d_cell_start, sizeof(int32_t) * (s->ncell_cap + 1));
+  A.get(&s->d_cell_cnt, sizeof(int32_t) * (ncell_alloc + 1));
+  A.get(&s->d_cell_start, sizeof(int32_t) * (ncell_alloc + 1));
   A.get(&s->d_cell_atoms, sizeof(int32_t) * N);
   A.get(&s->d_cell_of_atom, sizeof(int32_t) * N);
-  A.get(&s->d_chunk, sizeof(int2) * s->nchunk);
+  A.get(&s->d_chunk, sizeof(int2) * nchunk_cap);
   A.get(&s->d_mol_chunk, sizeof(int32_t) * (nmol + 1));
-  A.get(&s->d_part, sizeof(double) * 8 * s->nchunk);
-  A.get(&s->d_cbox, sizeof(float) * 8 * s->nchunk);
+  A.get(&s->d_part, sizeof(double) * 8 * nchunk_cap);
+  A.get(&s->d_cbox, sizeof(float) * 8 * nchunk_cap);
   A.get(&s->d_egrid, sizeof(tm_grid) * nmol);
   A.get(&s->d_encell, sizeof(int32_t));
   A.get(&s->d_encell_m, sizeof(int32_t) * nmol);
-  A.get(&s->d_ecell_cnt, sizeof(int32_t) * (s->ecell_cap + 1));
-  A.get(&s->d_ecell_start, sizeof(int32_t) * (s->ecell_cap + 1));
+  A.get(&s->d_ecell_cnt, sizeof(int32_t) * (ecell_alloc + 1));
+  A.get(&s->d_ecell_start, sizeof(int32_t) * (ecell_alloc + 1));
   A.get(&s->d_ecell_atoms, sizeof(int32_t) * N);
   A.get(&s->d_ecell_of_atom, sizeof(int32_t) * N);
   A.get(&s->d_epos, sizeof(int32_t) * N);
@@ -550,43 +595,100 @@ extern "C" int tm_system_create(tm_model* m, int N, int nmol, const int32_t* Z,
   A.get(&s->d_F, sizeof(double) * 3 * N);
   A.get(&s->d_mol_E, sizeof(double) * 4 * nmol);
   A.get(&s->d_mol_aux, sizeof(double) * 8 * nmol);
-  if (A.rc) {
-    system_free(s);
-    return A.rc;
-  }
+  if (A.rc) return A.rc;
   cudaStream_t st = ctx->stream;
-  cudaMemcpyAsync(s->row_of_atom, s->row_of_atom_h.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(s->atom_of_row, atom_of_row.data(), sizeof(int32_t) * Mp, cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(s->tile_elem, s->tile_elem_h.data(), sizeof(int32_t) * s->ntiles, cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(s->d_Z, Z, sizeof(int32_t) * N, cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(s->d_elem, s->elem_h.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(s->d_mol, mol.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(s->d_off, off32.data(), sizeof(int32_t) * (nmol + 1), cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(s->d_chunk, chunks.data(), sizeof(int2) * s->nchunk, cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(s->d_mol_chunk, mol_chunk.data(), sizeof(int32_t) * (nmol + 1),
-                  cudaMemcpyHostToDevice, st);
   for (int h = 0; h < 2; ++h) {
     if (m->desc.precision == TM_PREC_BF16 && h == 1) break;
     cudaMemsetAsync(s->G[h], 0, Mp * Dp * es, st);
   }
   cudaMemsetAsync(s->d_x, 0, sizeof(double) * 3 * N, st);
   int rc;
-  if ((rc = tm_cuda_check(ctx, cudaStreamSynchronize(st), "system upload"))) {
-    system_free(s);
-    return rc;
-  }
+  if ((rc = tm_cuda_check(ctx, cudaStreamSynchronize(st), "system alloc"))) return rc;
   const int eb = (int)es;
   for (int h = 0; h < 2; ++h) {
     if ((rc = tm_make_tmap(ctx, &s->tm_G[h], s->G[h], eb, Mp, Dp, TM_BM)) ||
         (rc = tm_make_tmap(ctx, &s->tm_H1[h], s->H1[h], eb, 2 * Mp, H, TM_BM)) ||
         (rc = tm_make_tmap(ctx, &s->tm_H2[h], s->H2[h], eb, 2 * Mp, H, TM_BM)) ||
-        (rc = tm_make_tmap(ctx, &s->tm_G3[h], s->G3[h], eb, 2 * Mp, H, TM_BM))) {
-      system_free(s);
+        (rc = tm_make_tmap(ctx, &s->tm_G3[h], s->G3[h], eb, 2 * Mp, H, TM_BM)))
       return rc;
+  }
+  return TM_OK;
+}
+
+extern "C" int tm_system_create(tm_model* m, int N, int nmol, const int32_t* Z,
+                                const int64_t* off, const double* cell, tm_system** out) {
+  *out = nullptr;
+  if (!m || !Z || !off || N <= 0 || nmol <= 0) return tm_fail(m ? m->ctx : nullptr, TM_E_ARG, "system args");
+  tm_ctx* ctx = m->ctx;
+  if (!m->final_) return tm_fail(ctx, TM_E_STATE, "model weights are not finalized");
+  tm_system* s = new tm_system();
+  s->model = m;
+  s->ctx = ctx;
+  const tm_consts& k = m->k;
+  if (cell) {
+    for (int q = 0; q < 9; ++q) s->lat[q] = cell[q];
+    if (cell[1] != 0 || cell[2] != 0 || cell[3] != 0 || cell[5] != 0 || cell[6] != 0 || cell[7] != 0) {
+      delete s;
+      return tm_fail(ctx, TM_E_UNSUPPORTED, "only orthorhombic cells are supported");
     }
+    if (nmol != 1) { delete s; return tm_fail(ctx, TM_E_ARG, "a periodic system is one molecule"); }
+    const double Lmin = std::min(cell[0], std::min(cell[4], cell[8]));
+    const double rmax = std::max(k.r_rc_d, k.ree_d);
+    if (Lmin < 2.0 * rmax) {
+      delete s;
+      return tm_fail(ctx, TM_E_ARG, "cell edges must be at least twice the largest cutoff");
+    }
+    // With edges >= 2 * cutoff, a +-R cell search (R = ceil(cutoff / cell
+    // edge) <= ceil(n / 2) <= n) wraps at most once per axis and reaches each
+    // (cell, image) at most once; the exact distance test keeps the one image
+    // within the cutoff.
+    s->periodic = true;
+    // Coulomb grid: floor(L / size) cells per edge, about 24 atoms per cell
+    const double vol = cell[0] * cell[4] * cell[8];
+    const double cs = std::max(2.0, cbrt(24.0 * vol / N));
+    for (int d = 0; d < 3; ++d) s->ee_dims[d] = std::max(1, std::min(4096, (int)floor(cell[4 * d] / cs)));
+  }
+  SysLayout L;
+  int rc = build_layout(s, N, nmol, Z, off, L);
+  if (!rc) rc = system_alloc(s, N, nmol, L.Mpad, L.nchunk, L.ncell_cap, L.ecell_cap);
+  if (!rc) rc = upload_layout(s, L);
+  if (rc) {
+    system_free(s);
+    return rc;
   }
   *out = s;
   return TM_OK;
+}
+
+// Open-boundary system with room for up to N_cap atoms in nmol_cap molecules
+// and no atoms yet (serving batches; layouts come from tm_system_relayout).
+int tm_system_create_capacity(tm_model* m, int N_cap, int nmol_cap, tm_system** out) {
+  *out = nullptr;
+  tm_ctx* ctx = m->ctx;
+  if (!m->final_) return tm_fail(ctx, TM_E_STATE, "model weights are not finalized");
+  if (N_cap <= 0 || nmol_cap <= 0 || N_cap >= (1 << 27)) return tm_fail(ctx, TM_E_ARG, "capacity");
+  tm_system* s = new tm_system();
+  s->model = m;
+  s->ctx = ctx;
+  const int nele = m->k.nele;
+  const int Mpad_cap = ((N_cap + TM_BM - 1) / TM_BM + nele) * TM_BM;
+  const int nchunk_cap = N_cap / 1024 + nmol_cap;
+  const int rc = system_alloc(s, N_cap, nmol_cap, Mpad_cap, nchunk_cap, 2 * N_cap + 64 * nmol_cap,
+                              N_cap / 8 + 8 * nmol_cap);
+  if (rc) {
+    system_free(s);
+    return rc;
+  }
+  *out = s;
+  return TM_OK;
+}
+
+int tm_system_relayout(tm_system* s, int N, int nmol, const int32_t* Z, const int64_t* off) {
+  if (s->periodic) return tm_fail(s->ctx, TM_E_UNSUPPORTED, "relayout of a periodic system");
+  SysLayout L;
+  int rc = build_layout(s, N, nmol, Z, off, L);
+  if (!rc) rc = upload_layout(s, L);
+  return rc;
 }
 
 static void system_free(tm_system* s) {

@@ -90,7 +90,9 @@ struct tm_model {
 struct tm_system {
   tm_model* model = nullptr;
   tm_ctx* ctx = nullptr;
-  int N = 0, nmol = 0;
+  int N = 0, nmol = 0;                 // current layout
+  int N_cap = 0, nmol_cap = 0;         // allocated capacity (a layout may use less)
+  int Mpad_cap = 0, nchunk_cap = 0, ncell_alloc = 0, ecell_alloc = 0;
   bool periodic = false;
   double lat[9] = {0};
   std::vector<int32_t> Z;              // host
@@ -182,6 +184,9 @@ int tm_cuda_check(tm_ctx* ctx, cudaError_t e, const char* what);
 int tm_alloc(tm_ctx* ctx, void** p, size_t bytes);
 void tm_free(tm_ctx* ctx, void* p, size_t bytes);
 int tm_sync_status(tm_ctx* ctx, const char* what);
+int tm_system_create_capacity(tm_model* m, int N_cap, int nmol_cap, tm_system** out);
+int tm_system_relayout(tm_system* s, int N, int nmol, const int32_t* Z, const int64_t* off);
+int tm_energy_force_device(tm_system* s, unsigned flags);
 
 // ---- launchers ----
 // tm_nlist.cu

@@ -876,25 +876,25 @@ int tm_nlist_grow(tm_system* s, bool* grew) {
   if (h_need[0] <= s->KR && h_need[1] <= s->KA) return TM_OK;
   const int KR = h_need[0] > s->KR ? ((h_need[0] + 31) / 32) * 32 : s->KR;
   const int KA = h_need[1] > s->KA ? ((h_need[1] + 31) / 32) * 32 : s->KA;
-  tm_free(ctx, s->d_nbr_r, sizeof(uint32_t) * (size_t)s->N * s->KR);
-  tm_free(ctx, s->d_rev_r, sizeof(int32_t) * (size_t)s->N * s->KR);
-  tm_free(ctx, s->d_sr, sizeof(float) * (size_t)s->N * s->KR);
-  tm_free(ctx, s->d_nbr_a, sizeof(uint32_t) * (size_t)s->N * s->KA);
-  tm_free(ctx, s->d_rev_a, sizeof(int32_t) * (size_t)s->N * s->KA);
-  tm_free(ctx, s->d_va, sizeof(float4) * (size_t)s->N * s->KA);
-  s->bytes -= (sizeof(uint32_t) + sizeof(int32_t) + sizeof(float)) * (size_t)s->N * s->KR +
-              (sizeof(uint32_t) + sizeof(int32_t) + sizeof(float4)) * (size_t)s->N * s->KA;
+  tm_free(ctx, s->d_nbr_r, sizeof(uint32_t) * (size_t)s->N_cap * s->KR);
+  tm_free(ctx, s->d_rev_r, sizeof(int32_t) * (size_t)s->N_cap * s->KR);
+  tm_free(ctx, s->d_sr, sizeof(float) * (size_t)s->N_cap * s->KR);
+  tm_free(ctx, s->d_nbr_a, sizeof(uint32_t) * (size_t)s->N_cap * s->KA);
+  tm_free(ctx, s->d_rev_a, sizeof(int32_t) * (size_t)s->N_cap * s->KA);
+  tm_free(ctx, s->d_va, sizeof(float4) * (size_t)s->N_cap * s->KA);
+  s->bytes -= (sizeof(uint32_t) + sizeof(int32_t) + sizeof(float)) * (size_t)s->N_cap * s->KR +
+              (sizeof(uint32_t) + sizeof(int32_t) + sizeof(float4)) * (size_t)s->N_cap * s->KA;
   s->KR = KR;
   s->KA = KA;
-  if ((rc = tm_alloc(ctx, (void**)&s->d_nbr_r, sizeof(uint32_t) * (size_t)s->N * KR)) ||
-      (rc = tm_alloc(ctx, (void**)&s->d_rev_r, sizeof(int32_t) * (size_t)s->N * KR)) ||
-      (rc = tm_alloc(ctx, (void**)&s->d_sr, sizeof(float) * (size_t)s->N * KR)) ||
-      (rc = tm_alloc(ctx, (void**)&s->d_nbr_a, sizeof(uint32_t) * (size_t)s->N * KA)) ||
-      (rc = tm_alloc(ctx, (void**)&s->d_rev_a, sizeof(int32_t) * (size_t)s->N * KA)) ||
-      (rc = tm_alloc(ctx, (void**)&s->d_va, sizeof(float4) * (size_t)s->N * KA)))
+  if ((rc = tm_alloc(ctx, (void**)&s->d_nbr_r, sizeof(uint32_t) * (size_t)s->N_cap * KR)) ||
+      (rc = tm_alloc(ctx, (void**)&s->d_rev_r, sizeof(int32_t) * (size_t)s->N_cap * KR)) ||
+      (rc = tm_alloc(ctx, (void**)&s->d_sr, sizeof(float) * (size_t)s->N_cap * KR)) ||
+      (rc = tm_alloc(ctx, (void**)&s->d_nbr_a, sizeof(uint32_t) * (size_t)s->N_cap * KA)) ||
+      (rc = tm_alloc(ctx, (void**)&s->d_rev_a, sizeof(int32_t) * (size_t)s->N_cap * KA)) ||
+      (rc = tm_alloc(ctx, (void**)&s->d_va, sizeof(float4) * (size_t)s->N_cap * KA)))
     return rc;
-  s->bytes += (sizeof(uint32_t) + sizeof(int32_t) + sizeof(float)) * (size_t)s->N * KR +
-              (sizeof(uint32_t) + sizeof(int32_t) + sizeof(float4)) * (size_t)s->N * KA;
+  s->bytes += (sizeof(uint32_t) + sizeof(int32_t) + sizeof(float)) * (size_t)s->N_cap * KR +
+              (sizeof(uint32_t) + sizeof(int32_t) + sizeof(float4)) * (size_t)s->N_cap * KA;
   s->nlist_valid = false;
   *grew = true;
   return TM_OK;
