@@ -94,8 +94,8 @@ __global__ void k_neutralize(const int32_t* __restrict__ mol, const int32_t* __r
 
 struct CoulArgs {
   const double* x;
-  const float4* exhi;       // cell-ordered hi parts (w = element)
-  const float4* exlo;       // cell-ordered lo parts (w = charge)
+  const float4* exhi;       // cell order: position relative to the atom's cell origin (w = element)
+  const float4* exlo;       // cell order: w = charge
   const int32_t* eatom;     // cell-ordered atom index
   const int32_t* mol;
   const tm_grid* grid;      // Coulomb grid per molecule
@@ -110,7 +110,8 @@ struct CoulArgs {
   int ref_periodic;         // image pairs contribute half the force (reference gradient)
   int periodic;
   double ree;
-  float ree2, ree2_lo, ree2_hi, ree2_screen;
+  float ree2, ree2_lo, ree2_hi;
+  float inv_bohr, inv_b2, inv_vdw_width, c_lin;   // 1/bohr, 1/bohr^2, 1/width, zz/R_lr + yy
   double lat[9];
   float sh_hi[27][3];
   float sh_lo[27][3];
@@ -122,8 +123,9 @@ struct PairOut {
   float dedr;   // dE/dr (Angstrom) of the pair
 };
 
-__device__ __forceinline__ PairOut pair_terms(float r, float qi, float qj, int ei, int ej,
-                                              const tm_consts& k) {
+// r in Angstrom and ir = 1/r; s6 = sqrt(C6_i C6_j), R0 = R0_i + R0_j of the pair.
+__device__ __forceinline__ PairOut pair_terms(float r, float ir, float qi, float qj, float s6,
+                                              float R0, const CoulArgs& a, const tm_consts& k) {
   PairOut o{0.f, 0.f, 0.f};
   if (k.add_ecc) {
     const float rb = r * k.bohr;
@@ -135,10 +137,9 @@ __device__ __forceinline__ PairOut pair_terms(float r, float qi, float qj, int e
       } else {
         const float ar = k.alpha * rb;
         const float ec = erfcf(ar);
-        const float ir = 1.f / rb;
-        kc = ec * ir - k.zz + (rb - k.r_lr) * (k.zz / k.r_lr + k.yy);
-        dkc = -(ec * ir * ir + 1.1283791671f * k.alpha * expf(-ar * ar) * ir) +
-              (k.zz / k.r_lr + k.yy);
+        const float irb = ir * a.inv_bohr;
+        kc = ec * irb - k.zz + (rb - k.r_lr) * a.c_lin;
+        dkc = a.c_lin - irb * (ec * irb + 1.1283791671f * k.alpha * expf(-ar * ar));
       }
     } else {
       const float ex = expf(rb - k.r_sr);
@@ -151,19 +152,17 @@ __device__ __forceinline__ PairOut pair_terms(float r, float qi, float qj, int e
   if (k.has_vdw) {
     const float b2 = k.bohr * k.bohr;
     const float rp = r * b2;
-    const float t = (rp - k.vdw_begin) / k.vdw_width;
+    const float t = (rp - k.vdw_begin) * a.inv_vdw_width;
     float cut, dcut;
     if (t > 1.f) { cut = 1.f; dcut = 0.f; }
-    else if (t > 0.f) { cut = -t * t * (2.f * t - 3.f); dcut = -6.f * t * (t - 1.f) / k.vdw_width; }
+    else if (t > 0.f) { cut = -t * t * (2.f * t - 3.f); dcut = -6.f * t * (t - 1.f) * a.inv_vdw_width; }
     else { cut = 0.f; dcut = 0.f; }
-    const float s6 = sqrtf(k.c6[ei] * k.c6[ej]);
-    const float R0 = k.r0[ei] + k.r0[ej];
-    const float inv = 1.f / rp;
+    const float inv = ir * a.inv_b2;                  // 1 / rp
     const float inv2 = inv * inv;
     const float inv6 = inv2 * inv2 * inv2;
-    const float xr = R0 * inv;                       // (rp/R0)^-1
+    const float xr = R0 * inv;                        // (rp/R0)^-1
     const float x2 = xr * xr, x4 = x2 * x2, x12 = x4 * x4 * x4;
-    const float damp = 1.f / (1.f + 6.f * x12);
+    const float damp = __fdividef(1.f, 1.f + 6.f * x12);
     const float K = -cut * s6 * inv6 * damp;
     // d damp / d rp = 72 x12 / (rp (1 + 6 x12)^2)
     const float dK = -s6 * inv6 * damp * (dcut - 6.f * cut * inv + 72.f * cut * x12 * inv * damp);
@@ -173,11 +172,23 @@ __device__ __forceinline__ PairOut pair_terms(float r, float qi, float qj, int e
   return o;
 }
 
-// One warp per Coulomb-grid cell; lane = centre atom (cells with more than 32
-// atoms loop). Candidate cells are culled by box distance and staged 32 atoms
-// at a time in shared memory, read back as broadcasts by every lane.
+// One warp per (Coulomb-grid cell, stencil split); lane = centre atom (cells
+// with more than 32 atoms loop). Positions are stored relative to the origin
+// of each atom's cell, so a pair vector is (p_i - off) - p_j with off the
+// stencil offset times the cell edge (periodic images included): two FP32
+// subtractions of small numbers per axis, accurate to about 1e-6 A. The
+// candidate cells (culled by box distance) are staged 32 atoms at a time in
+// shared memory and read back as broadcasts by every lane.
 __global__ void __launch_bounds__(128) k_coulomb(const CoulArgs a, const tm_consts k) {
-  __shared__ float4 sh[4][2][32];
+  __shared__ float4 sp[4][32];
+  __shared__ float sq[4][32];
+  __shared__ float tab[2][TM_MAX_ELE * TM_MAX_ELE];   // sqrt(C6_i C6_j), R0_i + R0_j
+  if (threadIdx.x < k.nele * k.nele) {
+    const int ei = threadIdx.x / k.nele, ej = threadIdx.x % k.nele;
+    tab[0][threadIdx.x] = sqrtf(k.c6[ei] * k.c6[ej]);
+    tab[1][threadIdx.x] = k.r0[ei] + k.r0[ej];
+  }
+  __syncthreads();
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int wg = blockIdx.x * (blockDim.x >> 5) + wib;
   const int c = wg / TM_EE_SPLIT, split = wg % TM_EE_SPLIT;
@@ -192,88 +203,84 @@ __global__ void __launch_bounds__(128) k_coulomb(const CoulArgs a, const tm_cons
   const int Rx = a.periodic ? min((int)ceil(a.ree / g.cx), g.nx) : (int)ceil(a.ree / g.cx);
   const int Ry = a.periodic ? min((int)ceil(a.ree / g.cy), g.ny) : (int)ceil(a.ree / g.cy);
   const int Rz = a.periodic ? min((int)ceil(a.ree / g.cz), g.nz) : (int)ceil(a.ree / g.cz);
-  float4* sj_hi = sh[wib][0];
-  float4* sj_lo = sh[wib][1];
+  float4* sj_p = sp[wib];
+  float* sj_q = sq[wib];
   for (int ib = t0; ib < t1; ib += 32) {
     const int ti = ib + lane;
     const bool have = ti < t1;
-    const float4 hi = a.exhi[have ? ti : t0];
-    const float4 lo = a.exlo[have ? ti : t0];
-    const int ei = __float_as_int(hi.w);
-    const float qi = lo.w;
+    const float4 pi = a.exhi[have ? ti : t0];
+    const float qi = a.exlo[have ? ti : t0].w;
+    const int ei = __float_as_int(pi.w);
+    const float* s6row = tab[0] + ei * k.nele;
+    const float* r0row = tab[1] + ei * k.nele;
     float acc_cc = 0.f, acc_vdw = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
     // this warp's share of the stencil: every TM_EE_SPLIT-th (ox, oy) column
     const int ncol = (2 * Rx + 1) * (2 * Ry + 1);
     for (int col = split; col < ncol; col += TM_EE_SPLIT) {
       const int ox = col / (2 * Ry + 1) - Rx, oy = col % (2 * Ry + 1) - Ry;
       const float gapx = fmaxf(0.f, (float)(abs(ox) - 1)) * cx;
-      {
-        const float gapy = fmaxf(0.f, (float)(abs(oy) - 1)) * cy;
-        for (int oz = -Rz; oz <= Rz; ++oz) {
-          const float gapz = fmaxf(0.f, (float)(abs(oz) - 1)) * cz;
-          if (gapx * gapx + gapy * gapy + gapz * gapz > a.ree2_hi) continue;
-          int jx = ix + ox, jy = iy + oy, jz = iz + oz, sx = 0, sy = 0, sz = 0;
-          if (a.periodic) {
-            if (jx < 0) { jx += g.nx; sx = -1; } else if (jx >= g.nx) { jx -= g.nx; sx = 1; }
-            if (jy < 0) { jy += g.ny; sy = -1; } else if (jy >= g.ny) { jy -= g.ny; sy = 1; }
-            if (jz < 0) { jz += g.nz; sz = -1; } else if (jz >= g.nz) { jz -= g.nz; sz = 1; }
-          } else if (jx < 0 || jx >= g.nx || jy < 0 || jy >= g.ny || jz < 0 || jz >= g.nz) {
-            continue;
+      const float gapy = fmaxf(0.f, (float)(abs(oy) - 1)) * cy;
+      const float offx = (float)(ox * g.cx), offy = (float)(oy * g.cy);
+      const float cix = pi.x - offx, ciy = pi.y - offy;
+      for (int oz = -Rz; oz <= Rz; ++oz) {
+        const float gapz = fmaxf(0.f, (float)(abs(oz) - 1)) * cz;
+        if (gapx * gapx + gapy * gapy + gapz * gapz > a.ree2_hi) continue;
+        int jx = ix + ox, jy = iy + oy, jz = iz + oz, sx = 0, sy = 0, sz = 0;
+        if (a.periodic) {
+          if (jx < 0) { jx += g.nx; sx = -1; } else if (jx >= g.nx) { jx -= g.nx; sx = 1; }
+          if (jy < 0) { jy += g.ny; sy = -1; } else if (jy >= g.ny) { jy -= g.ny; sy = 1; }
+          if (jz < 0) { jz += g.nz; sz = -1; } else if (jz >= g.nz) { jz -= g.nz; sz = 1; }
+        } else if (jx < 0 || jx >= g.nx || jy < 0 || jy >= g.ny || jz < 0 || jz >= g.nz) {
+          continue;
+        }
+        const int cj = g.cell_off + (jx * g.ny + jy) * g.nz + jz;
+        const int r = 9 * (sx + 1) + 3 * (sy + 1) + (sz + 1);
+        const float ciz = pi.z - (float)(oz * g.cz);
+        const float fscale = (a.ref_periodic && r != TM_IMG_SELF) ? 0.5f : 1.f;
+        const int u0 = a.cell_start[cj], u1 = a.cell_start[cj + 1];
+        for (int jb = u0; jb < u1; jb += 32) {
+          const int nj = min(32, u1 - jb);
+          __syncwarp();
+          if (lane < nj) {
+            sj_p[lane] = a.exhi[jb + lane];
+            sj_q[lane] = a.exlo[jb + lane].w;
           }
-          const int cj = g.cell_off + (jx * g.ny + jy) * g.nz + jz;
-          const int r = 9 * (sx + 1) + 3 * (sy + 1) + (sz + 1);
-          const float shx = a.sh_hi[r][0], shy = a.sh_hi[r][1], shz = a.sh_hi[r][2];
-          const float slx = a.sh_lo[r][0], sly = a.sh_lo[r][1], slz = a.sh_lo[r][2];
-          const float fscale = (a.ref_periodic && r != TM_IMG_SELF) ? 0.5f : 1.f;
-          const int u0 = a.cell_start[cj], u1 = a.cell_start[cj + 1];
-          for (int jb = u0; jb < u1; jb += 32) {
-            const int nj = min(32, u1 - jb);
-            __syncwarp();
-            if (lane < nj) {
-              sj_hi[lane] = a.exhi[jb + lane];
-              sj_lo[lane] = a.exlo[jb + lane];
-            }
-            __syncwarp();
-            if (!have) continue;
-            // cheap screen on the FP32 hi parts (error well below the margin
-            // in ree2_screen); only candidates that pass take the accurate path
-            uint32_t mask = 0;
-            for (int q = 0; q < nj; ++q) {
-              const float4 hj = sj_hi[q];
-              const float ex = hi.x - hj.x - shx, ey = hi.y - hj.y - shy, ez = hi.z - hj.z - shz;
-              if (ex * ex + ey * ey + ez * ez <= a.ree2_screen) mask |= 1u << q;
-            }
-            if (cj == c && r == TM_IMG_SELF && ti >= jb && ti < jb + nj)
-              mask &= ~(1u << (ti - jb));                                   // the atom itself
-            while (mask) {
-              const int q = __ffs(mask) - 1;
-              mask &= mask - 1;
-              const float4 hj = sj_hi[q], lj = sj_lo[q];
-              const float dx = ds_sub_shift(hi.x, lo.x, hj.x, lj.x, shx, slx);
-              const float dy = ds_sub_shift(hi.y, lo.y, hj.y, lj.y, shy, sly);
-              const float dz = ds_sub_shift(hi.z, lo.z, hj.z, lj.z, shz, slz);
-              const float d2 = dx * dx + dy * dy + dz * dz;
-              if (d2 > a.ree2_hi) continue;
-              if (d2 >= a.ree2_lo) {   // within 1e-5 of the cutoff: the exact FP64 rule
-                const int i = a.eatom[ti], j = a.eatom[jb + q];
-                double xj = a.x[3 * j], yj = a.x[3 * j + 1], zj = a.x[3 * j + 2];
-                if (a.periodic) {
-                  xj = tm_image_coord(xj, sx, sy, sz, a.lat[0], a.lat[3], a.lat[6]);
-                  yj = tm_image_coord(yj, sx, sy, sz, a.lat[1], a.lat[4], a.lat[7]);
-                  zj = tm_image_coord(zj, sx, sy, sz, a.lat[2], a.lat[5], a.lat[8]);
-                }
-                if (!tm_exact_within(a.x[3 * i], a.x[3 * i + 1], a.x[3 * i + 2], xj, yj, zj, a.ree))
-                  continue;
+          __syncwarp();
+          if (!have) continue;
+          uint32_t mask = 0;
+          for (int q = 0; q < nj; ++q) {
+            const float4 pj = sj_p[q];
+            const float ex = cix - pj.x, ey = ciy - pj.y, ez = ciz - pj.z;
+            if (ex * ex + ey * ey + ez * ez <= a.ree2_hi) mask |= 1u << q;
+          }
+          if (cj == c && r == TM_IMG_SELF && ti >= jb && ti < jb + nj)
+            mask &= ~(1u << (ti - jb));                                   // the atom itself
+          while (mask) {
+            const int q = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const float4 pj = sj_p[q];
+            const float dx = cix - pj.x, dy = ciy - pj.y, dz = ciz - pj.z;
+            const float d2 = dx * dx + dy * dy + dz * dz;
+            if (d2 >= a.ree2_lo) {   // within 1e-5 of the cutoff: the exact FP64 rule
+              const int i = a.eatom[ti], j = a.eatom[jb + q];
+              double xj = a.x[3 * j], yj = a.x[3 * j + 1], zj = a.x[3 * j + 2];
+              if (a.periodic) {
+                xj = tm_image_coord(xj, sx, sy, sz, a.lat[0], a.lat[3], a.lat[6]);
+                yj = tm_image_coord(yj, sx, sy, sz, a.lat[1], a.lat[4], a.lat[7]);
+                zj = tm_image_coord(zj, sx, sy, sz, a.lat[2], a.lat[5], a.lat[8]);
               }
-              const float rr = sqrtf(d2);
-              const PairOut po = pair_terms(rr, qi, lj.w, ei, __float_as_int(hj.w), k);
-              acc_cc += po.e_cc;
-              acc_vdw += po.e_vdw;
-              const float sc = fscale * po.dedr / rr;
-              gx += sc * dx;
-              gy += sc * dy;
-              gz += sc * dz;
+              if (!tm_exact_within(a.x[3 * i], a.x[3 * i + 1], a.x[3 * i + 2], xj, yj, zj, a.ree))
+                continue;
             }
+            const float ir = rsqrtf(d2);
+            const int ej = __float_as_int(pj.w);
+            const PairOut po = pair_terms(d2 * ir, ir, qi, sj_q[q], s6row[ej], r0row[ej], a, k);
+            acc_cc += po.e_cc;
+            acc_vdw += po.e_vdw;
+            const float sc = fscale * po.dedr * ir;
+            gx += sc * dx;
+            gy += sc * dy;
+            gz += sc * dz;
           }
         }
       }
@@ -387,14 +394,15 @@ int tm_launch_coulomb(tm_system* s, unsigned flags) {
   a.ree2 = (float)(k.ree_d * k.ree_d);
   a.ree2_lo = a.ree2 * (1.f - kBand);
   a.ree2_hi = a.ree2 * (1.f + kBand);
-  // hi parts of coordinates below 1e4 A are within 5e-4 A of the truth, so a
-  // hi-part distance errs by under 2e-3 A, inside this margin
-  a.ree2_screen = (float)((k.ree_d * (1.0 + 1e-4) + 5e-3) * (k.ree_d * (1.0 + 1e-4) + 5e-3));
+  a.inv_bohr = (float)(1.0 / (double)k.bohr);
+  a.inv_b2 = (float)(1.0 / ((double)k.bohr * (double)k.bohr));
+  a.inv_vdw_width = (float)(1.0 / (double)k.vdw_width);
+  a.c_lin = (float)((double)k.zz / (double)k.r_lr + (double)k.yy);
   for (int q = 0; q < 9; ++q) a.lat[q] = s->lat[q];
   tm_fill_shifts(s, a.sh_hi, a.sh_lo);
   k_coulomb<<<tm_div_up(s->ecell_cap * TM_EE_SPLIT, 4), 128, 0, ctx->stream>>>(a, k);
   k_coulomb_finish<<<tm_div_up(s->N, 256), 256, 0, ctx->stream>>>(a);
-  ctx->launches++;
+  ctx->launches += 2;
   k_chunk_sum2<<<s->nchunk, 256, 0, ctx->stream>>>(s->d_chunk, s->d_ecv, s->d_dEdq, s->d_q,
                                                    s->d_x, 1.889725989, s->d_part);
   k_mol_final2<<<tm_div_up(s->nmol, 128), 128, 0, ctx->stream>>>(s->d_mol_chunk, s->d_part,

@@ -245,15 +245,22 @@ __global__ void k_cell_sort(const int32_t* __restrict__ start, int32_t* __restri
 
 // Cell-ordered copies of the double-single positions for the pair kernel;
 // the charge slot (lo.w) is filled after the charge network runs.
-__global__ void k_ee_pack(const int32_t* __restrict__ order, const float4* __restrict__ xhi,
-                          const float4* __restrict__ xlo, int32_t* __restrict__ pos,
-                          float4* __restrict__ ohi, float4* __restrict__ olo, int N) {
+// Coulomb-grid packing: atoms in cell order with their positions relative to
+// the origin of their own cell (FP64 difference rounded once to FP32; w =
+// element). The charge (olo.w) is written after the charge network.
+__global__ void k_ee_pack(const int32_t* __restrict__ order, const double* __restrict__ x,
+                          const int32_t* __restrict__ elem, const int32_t* __restrict__ mol,
+                          const tm_grid* __restrict__ grid, const int32_t* __restrict__ cell_of,
+                          int32_t* __restrict__ pos, float4* __restrict__ ohi, int N) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= N) return;
   const int a = order[p];
   pos[a] = p;
-  ohi[p] = xhi[a];
-  olo[p] = xlo[a];
+  const tm_grid g = grid[mol[a]];
+  const int lc = cell_of[a] - g.cell_off;
+  const int iz = lc % g.nz, iy = (lc / g.nz) % g.ny, ix = lc / (g.nz * g.ny);
+  ohi[p] = make_float4((float)(x[3 * a] - (g.ox + ix * g.cx)), (float)(x[3 * a + 1] - (g.oy + iy * g.cy)),
+                       (float)(x[3 * a + 2] - (g.oz + iz * g.cz)), __int_as_float(elem[a]));
 }
 
 __global__ void k_grid_offsets(tm_grid* __restrict__ grid, const int32_t* __restrict__ ncell_m,
@@ -855,8 +862,9 @@ int tm_launch_nlist(tm_system* s) {
                                                      s->d_ecell_cnt, s->d_ecell_atoms, s->N);
   k_cell_sort<<<tm_div_up(s->ecell_cap, 128), 128, 0, st>>>(s->d_ecell_start, s->d_ecell_atoms,
                                                               s->d_encell, s->ecell_cap);
-  k_ee_pack<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_ecell_atoms, s->d_xhi, s->d_xlo, s->d_epos,
-                                                  s->d_exhi, s->d_exlo, s->N);
+  k_ee_pack<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_ecell_atoms, s->d_x, s->d_elem, s->d_mol,
+                                                  s->d_egrid, s->d_ecell_of_atom, s->d_epos,
+                                                  s->d_exhi, s->N);
   ctx->launches += 3;
   cudaMemcpyAsync(s->d_x_at_build, s->d_x, sizeof(double) * 3 * s->N, cudaMemcpyDeviceToDevice, st);
   s->nlist_valid = true;
