@@ -174,14 +174,73 @@ __device__ __forceinline__ PairOut pair_terms(float r, float ir, float qi, float
 
 // One warp per (Coulomb-grid cell, stencil split); lane = centre atom (cells
 // with more than 32 atoms loop). Positions are stored relative to the origin
-// of each atom's cell, so a pair vector is (p_i - off) - p_j with off the
-// stencil offset times the cell edge (periodic images included): two FP32
-// subtractions of small numbers per axis, accurate to about 1e-6 A. The
-// candidate cells (culled by box distance) are staged 32 atoms at a time in
-// shared memory and read back as broadcasts by every lane.
-__global__ void __launch_bounds__(128) k_coulomb(const CoulArgs a, const tm_consts k) {
-  __shared__ float4 sp[4][32];
-  __shared__ float sq[4][32];
+// of each atom's cell; a staged candidate is moved into the centre cell's
+// frame once (p_j + stencil offset x cell edge, periodic images included), so
+// a pair vector is one FP32 subtraction per axis, accurate to about 1e-6 A.
+// The candidate cells of one stencil column (culled by box distance) are
+// staged up to kStage atoms at a time in shared memory and read back as
+// broadcasts; each lane then walks its own set bits over the whole stage, so
+// the warp's divergence is set by the spread of per-lane pair counts over
+// kStage candidates rather than over 32.
+constexpr int kStage = 128;
+
+struct StageSmem {
+  float4 p[kStage];        // candidate position in the centre cell's frame (w = element)
+  float q[kStage];         // candidate charge
+  uint32_t meta[kStage];   // image code << 27 | cell-order index
+};
+
+__device__ __forceinline__ void coulomb_flush(const CoulArgs& a, const tm_consts& k,
+                                              const StageSmem& st, int n, int ti, float4 pi,
+                                              float qi, const float* s6row, const float* r0row,
+                                              float& acc_cc, float& acc_vdw, float& gx, float& gy,
+                                              float& gz) {
+  uint64_t m0 = 0, m1 = 0;
+  for (int q = 0; q < n; ++q) {
+    const float4 pj = st.p[q];
+    const float ex = pi.x - pj.x, ey = pi.y - pj.y, ez = pi.z - pj.z;
+    if (ex * ex + ey * ey + ez * ez <= a.ree2_hi) {
+      if (q < 64) m0 |= 1ull << q;
+      else m1 |= 1ull << (q - 64);
+    }
+  }
+  while (m0 | m1) {
+    int q;
+    if (m0) { q = __ffsll((long long)m0) - 1; m0 &= m0 - 1; }
+    else { q = 64 + __ffsll((long long)m1) - 1; m1 &= m1 - 1; }
+    const uint32_t meta = st.meta[q];
+    const int jp = (int)(meta & ((1u << 27) - 1)), r = (int)(meta >> 27);
+    if (jp == ti && r == TM_IMG_SELF) continue;   // the atom itself
+    const float4 pj = st.p[q];
+    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    if (d2 >= a.ree2_lo) {   // within 1e-5 of the cutoff: the exact FP64 rule
+      const int i = a.eatom[ti], j = a.eatom[jp];
+      double xj = a.x[3 * j], yj = a.x[3 * j + 1], zj = a.x[3 * j + 2];
+      if (a.periodic) {
+        int sx, sy, sz;
+        tm_img_ijk(r, sx, sy, sz);
+        xj = tm_image_coord(xj, sx, sy, sz, a.lat[0], a.lat[3], a.lat[6]);
+        yj = tm_image_coord(yj, sx, sy, sz, a.lat[1], a.lat[4], a.lat[7]);
+        zj = tm_image_coord(zj, sx, sy, sz, a.lat[2], a.lat[5], a.lat[8]);
+      }
+      if (!tm_exact_within(a.x[3 * i], a.x[3 * i + 1], a.x[3 * i + 2], xj, yj, zj, a.ree)) continue;
+    }
+    const float ir = rsqrtf(d2);
+    const int ej = __float_as_int(pj.w);
+    const PairOut po = pair_terms(d2 * ir, ir, qi, st.q[q], s6row[ej], r0row[ej], a, k);
+    acc_cc += po.e_cc;
+    acc_vdw += po.e_vdw;
+    const float fscale = (a.ref_periodic && r != TM_IMG_SELF) ? 0.5f : 1.f;
+    const float sc = fscale * po.dedr * ir;
+    gx += sc * dx;
+    gy += sc * dy;
+    gz += sc * dz;
+  }
+}
+
+__global__ void __launch_bounds__(128, 4) k_coulomb(const CoulArgs a, const tm_consts k) {
+  __shared__ StageSmem stage[4];
   __shared__ float tab[2][TM_MAX_ELE * TM_MAX_ELE];   // sqrt(C6_i C6_j), R0_i + R0_j
   if (threadIdx.x < k.nele * k.nele) {
     const int ei = threadIdx.x / k.nele, ej = threadIdx.x % k.nele;
@@ -203,8 +262,7 @@ __global__ void __launch_bounds__(128) k_coulomb(const CoulArgs a, const tm_cons
   const int Rx = a.periodic ? min((int)ceil(a.ree / g.cx), g.nx) : (int)ceil(a.ree / g.cx);
   const int Ry = a.periodic ? min((int)ceil(a.ree / g.cy), g.ny) : (int)ceil(a.ree / g.cy);
   const int Rz = a.periodic ? min((int)ceil(a.ree / g.cz), g.nz) : (int)ceil(a.ree / g.cz);
-  float4* sj_p = sp[wib];
-  float* sj_q = sq[wib];
+  StageSmem& st = stage[wib];
   for (int ib = t0; ib < t1; ib += 32) {
     const int ti = ib + lane;
     const bool have = ti < t1;
@@ -221,7 +279,7 @@ __global__ void __launch_bounds__(128) k_coulomb(const CoulArgs a, const tm_cons
       const float gapx = fmaxf(0.f, (float)(abs(ox) - 1)) * cx;
       const float gapy = fmaxf(0.f, (float)(abs(oy) - 1)) * cy;
       const float offx = (float)(ox * g.cx), offy = (float)(oy * g.cy);
-      const float cix = pi.x - offx, ciy = pi.y - offy;
+      int n = 0;   // staged candidates
       for (int oz = -Rz; oz <= Rz; ++oz) {
         const float gapz = fmaxf(0.f, (float)(abs(oz) - 1)) * cz;
         if (gapx * gapx + gapy * gapy + gapz * gapz > a.ree2_hi) continue;
@@ -234,55 +292,31 @@ __global__ void __launch_bounds__(128) k_coulomb(const CoulArgs a, const tm_cons
           continue;
         }
         const int cj = g.cell_off + (jx * g.ny + jy) * g.nz + jz;
-        const int r = 9 * (sx + 1) + 3 * (sy + 1) + (sz + 1);
-        const float ciz = pi.z - (float)(oz * g.cz);
-        const float fscale = (a.ref_periodic && r != TM_IMG_SELF) ? 0.5f : 1.f;
-        const int u0 = a.cell_start[cj], u1 = a.cell_start[cj + 1];
-        for (int jb = u0; jb < u1; jb += 32) {
-          const int nj = min(32, u1 - jb);
+        const uint32_t rcode = (uint32_t)(9 * (sx + 1) + 3 * (sy + 1) + (sz + 1)) << 27;
+        const float offz = (float)(oz * g.cz);
+        int u0 = a.cell_start[cj];
+        const int u1 = a.cell_start[cj + 1];
+        while (u0 < u1) {
+          const int take = min(u1 - u0, kStage - n);
           __syncwarp();
-          if (lane < nj) {
-            sj_p[lane] = a.exhi[jb + lane];
-            sj_q[lane] = a.exlo[jb + lane].w;
+          for (int t = lane; t < take; t += 32) {
+            const float4 pj = a.exhi[u0 + t];
+            st.p[n + t] = make_float4(pj.x + offx, pj.y + offy, pj.z + offz, pj.w);
+            st.q[n + t] = a.exlo[u0 + t].w;
+            st.meta[n + t] = rcode | (uint32_t)(u0 + t);
           }
-          __syncwarp();
-          if (!have) continue;
-          uint32_t mask = 0;
-          for (int q = 0; q < nj; ++q) {
-            const float4 pj = sj_p[q];
-            const float ex = cix - pj.x, ey = ciy - pj.y, ez = ciz - pj.z;
-            if (ex * ex + ey * ey + ez * ez <= a.ree2_hi) mask |= 1u << q;
-          }
-          if (cj == c && r == TM_IMG_SELF && ti >= jb && ti < jb + nj)
-            mask &= ~(1u << (ti - jb));                                   // the atom itself
-          while (mask) {
-            const int q = __ffs(mask) - 1;
-            mask &= mask - 1;
-            const float4 pj = sj_p[q];
-            const float dx = cix - pj.x, dy = ciy - pj.y, dz = ciz - pj.z;
-            const float d2 = dx * dx + dy * dy + dz * dz;
-            if (d2 >= a.ree2_lo) {   // within 1e-5 of the cutoff: the exact FP64 rule
-              const int i = a.eatom[ti], j = a.eatom[jb + q];
-              double xj = a.x[3 * j], yj = a.x[3 * j + 1], zj = a.x[3 * j + 2];
-              if (a.periodic) {
-                xj = tm_image_coord(xj, sx, sy, sz, a.lat[0], a.lat[3], a.lat[6]);
-                yj = tm_image_coord(yj, sx, sy, sz, a.lat[1], a.lat[4], a.lat[7]);
-                zj = tm_image_coord(zj, sx, sy, sz, a.lat[2], a.lat[5], a.lat[8]);
-              }
-              if (!tm_exact_within(a.x[3 * i], a.x[3 * i + 1], a.x[3 * i + 2], xj, yj, zj, a.ree))
-                continue;
-            }
-            const float ir = rsqrtf(d2);
-            const int ej = __float_as_int(pj.w);
-            const PairOut po = pair_terms(d2 * ir, ir, qi, sj_q[q], s6row[ej], r0row[ej], a, k);
-            acc_cc += po.e_cc;
-            acc_vdw += po.e_vdw;
-            const float sc = fscale * po.dedr * ir;
-            gx += sc * dx;
-            gy += sc * dy;
-            gz += sc * dz;
+          n += take;
+          u0 += take;
+          if (n == kStage) {
+            __syncwarp();
+            if (have) coulomb_flush(a, k, st, n, ti, pi, qi, s6row, r0row, acc_cc, acc_vdw, gx, gy, gz);
+            n = 0;
           }
         }
+      }
+      if (n) {
+        __syncwarp();
+        if (have) coulomb_flush(a, k, st, n, ti, pi, qi, s6row, r0row, acc_cc, acc_vdw, gx, gy, gz);
       }
     }
     if (have) {
