@@ -38,6 +38,9 @@ import numpy as np  # noqa: E402
 
 METRIC = "atom-steps/s E+F, fused adjoint vs plain autograd, 1 GB300; serve p50/p99 ms"
 UNIT = "atom-steps/s"
+# DRAM bytes of the six k_gemm launches of one evaluation (one ncu capture; the
+# k_gemm summary under profiles/ gives the command and the per-launch figures)
+GEMM_DRAM_BYTES_PER_STEP = 2_250_700_000
 WORKLOAD = ("water cube: 8,000 H2O = 24,000 atoms, open boundary, O on a 3.1 A lattice "
             "+-0.2 A jitter, single energy+force")
 
@@ -61,8 +64,8 @@ class Clocks:
     """nvidia-smi sampling during the timed region."""
 
     def __init__(self, index=0):
-        self.f = os.path.join(HERE, "gpurun_out", f"clocks_{os.getpid()}.csv")
-        os.makedirs(os.path.dirname(self.f), exist_ok=True)
+        import tempfile
+        self.f = os.path.join(tempfile.gettempdir(), f"tm_clocks_{os.getpid()}.csv")
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -400,10 +403,16 @@ def main():
         return 0
     # stage breakdown (one profiled evaluation)
     import ctypes
-    st = np.zeros(7, dtype=np.float32)
-    model.ctx.check(model.lib.tm_energy_force_profile(s.h, 0, st.ctypes.data))
+    # stage breakdown: CUDA events on the library's stream between the stages,
+    # averaged over `steps` evaluations
+    acc = np.zeros(7)
+    for _ in range(args.steps):
+        st = np.zeros(7, dtype=np.float32)
+        model.ctx.check(model.lib.tm_energy_force_profile(s.h, 0, st.ctypes.data))
+        acc += st
     stages = dict(zip(["nlist", "descriptors", "mlp_forward", "mlp_backward", "pair_terms",
-                       "adjoint_gather", "total"], [float(v) for v in st]))
+                       "adjoint_gather", "total"], [float(v) / args.steps for v in acc]))
+    counts = s.nlist_counts()
     e2e_t, h2d, d2h = time_e2e(model, s, w, args.steps, args.warmup, torch)
     e2e_ms = sum(e2e_t) / len(e2e_t)
     s.close()
@@ -428,12 +437,30 @@ def main():
     gemm_ms = stages["mlp_forward"] + stages["mlp_backward"]
     achieved = alg_flop / (gemm_ms / 1000.0) / 1e12
     roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak, "traffic": None,
+            "frac": achieved / peak, "traffic": GEMM_DRAM_BYTES_PER_STEP,
+            "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of the 6 k_gemm launches "
+                            "of one evaluation, one ncu capture (k_gemm summary under profiles/); "
+                            "algorithmic operand + output bytes are about 1.2 GB",
             "kernel": "k_gemm: 6 launches per E+F (3 forward, 3 backward; both networks per launch)",
             "algorithmic_flop_per_step": alg_flop,
             "note": (f"peak = {src} BF16 dense burst from MEASURED_PEAKS.json; FP32 mode executes "
                      "3 TF32 MMA passes (hi*hi + hi*lo + lo*hi) at half the BF16 rate, i.e. 6x the "
                      "BF16 tensor time for the same algorithmic FLOPs")}
+    # the other stages against HBM (algorithmic bytes per evaluation from the
+    # built lists: N atoms, P ordered pairs <= 4.6 A, T triples <= 3.1 A)
+    N, P, T, Pee = natoms, counts["pairs"], counts["triples"], counts["ee_pairs"]
+    Dd = 256
+    stage_bytes = {"nlist": 24 * N + 4 * N + 4 * P + 8 * T + 4 * P + 4 * T,
+                   "descriptors": 16 * N + 4 * P + 8 * T + 4 * N * Dd,
+                   "adjoint_gather": 16 * N + 4 * P + 8 * T + 4 * N * Dd + 12 * N,
+                   "pair_terms": 16 * N + 12 * N + 4 * N}
+    stage_roof = {}
+    for k_, b_ in stage_bytes.items():
+        gbs = b_ / (stages[k_] * 1e-3) / 1e9
+        stage_roof[k_] = {"bound": "hbm", "algorithmic_bytes": int(b_), "achieved_gbs": gbs,
+                          "peak_gbs": hbm, "frac": gbs / hbm}
+    stage_roof["pair_terms"]["pair_evaluations_per_s"] = 2 * Pee / (stages["pair_terms"] * 1e-3)
+    stage_roof["counts"] = {"atoms": N, "pairs": P, "triples": T, "ee_pairs_i_lt_j": Pee}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
@@ -445,6 +472,7 @@ def main():
             "e2e": {"value": ws * natoms / (e2e_ms / 1000.0), "unit": UNIT, "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches), "clocks": clocks, "stages_ms": stages, "roofline": roof,
+            "stage_rooflines": stage_roof,
             "bf16": {"value": natoms / (ms16 / 1000.0), "ms_per_step": ms16},
             "plain_autograd": plain,
             "serve": serving,

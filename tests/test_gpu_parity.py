@@ -227,3 +227,23 @@ def test_energy_force_chno512_with_finite_differences(gpu):
         fd = -om1.fd_gradient(b.x[a0:a1], atoms, h=1e-4) * JOULEPERHARTREE
         dfd = np.abs(out["force"][a0 + atoms] - fd).max() / JOULEPERHARTREE * EV_PER_HARTREE
         assert dfd < 1e-3, (mol, dfd)
+
+
+def test_autograd_function_gradient(gpu):
+    """FusedEnergy (torch.autograd.Function over the fused adjoint): energies
+    and dE/dx against the oracle, with per-molecule weights on the outputs."""
+    import torch
+    from tensormol_gb300.autograd import energy
+    b = systems.chno_batch(nmol=6, seed=3)
+    m, om = _model(gpu, [1, 6, 7, 8], "sigmoid_with_param")
+    s = m.system(b.x, b.Z, b.offsets)
+    x = torch.tensor(b.x, dtype=torch.float64, device="cuda", requires_grad=True)
+    E = energy(s, x)
+    wts = torch.arange(1, len(E) + 1, dtype=torch.float64, device="cuda")
+    (E * wts).sum().backward()
+    ref = orc.OpenSystemOracle(om, b.x, b.Z, b.offsets).terms(b.x)
+    n_per = np.diff(b.offsets)
+    dE = np.max(np.abs(E.detach().cpu().numpy() - ref["Etotal"]) * EV_PER_HARTREE / n_per)
+    w_atom = np.repeat(np.arange(1, len(n_per) + 1), n_per)[:, None]
+    dG = np.abs(x.grad.cpu().numpy() - ref["gradient"] * w_atom).max() * EV_PER_HARTREE
+    assert dE < E_TOL and dG < F_TOL * len(n_per), (dE, dG)
