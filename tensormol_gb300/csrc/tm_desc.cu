@@ -10,9 +10,10 @@
 //                            exp(-eta ((r_ij + r_ik)/2 - Rs_n)^2) fc_a(r_ij) fc_a(r_ik)
 //   fc(r) = 0.5 (cos(3.14159265359 r / Rc) + 1)
 // cos(theta - theta_m) is formed as c cos(theta_m) + s sin(theta_m) with
-// c = u_ij . u_ik and s = sqrt(1 - c^2) >= 0, which is cos(acos(c) - theta_m)
-// without the acos; the reference's clamp of c to +-(1 - 1e-16) only protects
-// its acos and is a no-op in FP32.
+// c = u_ij . u_ik and s = |u_ij x u_ik| >= 0, which is cos(acos(c) - theta_m)
+// without the acos (and accurate for nearly collinear triples, where
+// sqrt(1 - c^2) is not); the reference's clamp of c to +-(1 - 1e-16) only
+// protects its acos and is a no-op in FP32.
 //
 // The adjoint takes dE/dG per atom (energy net + dE/dq * charge net), recomputes
 // the pair/triple geometry from the positions, and produces
@@ -116,26 +117,24 @@ __host__ __device__ __forceinline__ int smem_floats(int Dp, int KA) { return Dp 
 __device__ __forceinline__ void load_angular(const DescArgs& a, const tm_consts& k, int i,
                                              float4 hi, float4 lo, int ca, WarpSmem& w,
                                              int* seg, int lane) {
-  for (int s = lane; s < ca; s += 32) {
-    float dx, dy, dz;
-    int el;
-    nbr_vec(a, hi, lo, a.nbr_a[(size_t)i * a.KA + s], dx, dy, dz, el);
-    const float r = sqrtf(dx * dx + dy * dy + dz * dz);
-    const float inv = 1.0f / r;
-    w.ux[s] = dx * inv;
-    w.uy[s] = dy * inv;
-    w.uz[s] = dz * inv;
-    w.r[s] = r;
-    w.fc[s] = fcut(r, k.pi_tf, k.a_rc);
-    w.fcd[s] = fcut_d(r, k.pi_tf, k.a_rc);
-  }
-  for (int e = 0; e < k.nele; ++e) {
-    int c = 0;
-    for (int s = lane; s < ca; s += 32) {
-      const uint32_t ent = a.nbr_a[(size_t)i * a.KA + s];
-      c += __float_as_int(a.xhi[tm_atom(ent)].w) == e;
+  for (int e = 0; e <= k.nele; ++e) seg[e] = 0;
+  for (int base = 0; base < ca; base += 32) {
+    const int s = base + lane;
+    int el = -1;
+    if (s < ca) {
+      float dx, dy, dz;
+      nbr_vec(a, hi, lo, a.nbr_a[(size_t)i * a.KA + s], dx, dy, dz, el);
+      const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+      const float inv = 1.0f / r;
+      w.ux[s] = dx * inv;
+      w.uy[s] = dy * inv;
+      w.uz[s] = dz * inv;
+      w.r[s] = r;
+      w.fc[s] = fcut(r, k.pi_tf, k.a_rc);
+      w.fcd[s] = fcut_d(r, k.pi_tf, k.a_rc);
     }
-    seg[e] = __reduce_add_sync(TM_FULL, c);
+    // rows are sorted by element: count each element's neighbours by ballot
+    for (int e = 0; e < k.nele; ++e) seg[e] += __popc(__ballot_sync(TM_FULL, el == e));
   }
   int acc = 0;
   for (int e = 0; e < k.nele; ++e) { int c = seg[e]; seg[e] = acc; acc += c; }
@@ -176,6 +175,9 @@ __global__ void __launch_bounds__(128) k_desc_fwd(const DescArgs a, const tm_con
   const float4 hi = a.xhi[i], lo = a.xlo[i];
   // ---- radial ----
   const int cr = a.cnt_r[i];
+  const float rs_lane = k.rs_r[lane < k.nr ? lane : 0];
+  float racc = 0.f;
+  int rel = -1;
   for (int base = 0; base < cr; base += 32) {
     const int s = base + lane;
     float r = 0.f, f = 0.f;
@@ -186,17 +188,23 @@ __global__ void __launch_bounds__(128) k_desc_fwd(const DescArgs a, const tm_con
       r = sqrtf(dx * dx + dy * dy + dz * dz);
       f = fcut(r, k.pi_tf, k.r_rc);
     }
+    // rows are sorted by element: accumulate in a register, flush to the
+    // row when the element changes (at most nele flushes per centre)
     const int n = min(32, cr - base);
     for (int q = 0; q < n; ++q) {
       const float rq = __shfl_sync(TM_FULL, r, q);
       const float fq = __shfl_sync(TM_FULL, f, q);
       const int lq = __shfl_sync(TM_FULL, el, q);
-      if (lane < k.nr) {
-        const float t = rq - k.rs_r[lane];
-        w.row[lq * k.nr + lane] += expf(-k.eta * t * t) * fq;
+      if (lq != rel) {
+        if (rel >= 0 && lane < k.nr) w.row[rel * k.nr + lane] += racc;
+        racc = 0.f;
+        rel = lq;
       }
+      const float t = rq - rs_lane;
+      racc += expf(-k.eta * t * t) * fq;
     }
   }
+  if (rel >= 0 && lane < k.nr) w.row[rel * k.nr + lane] += racc;
   // ---- angular ----
   const int ca = a.cnt_a[i];
   int seg[TM_MAX_ELE + 1];
@@ -215,31 +223,37 @@ __global__ void __launch_bounds__(128) k_desc_fwd(const DescArgs a, const tm_con
       for (int n = 0; n < 8; ++n) acc[n] = 0.f;
       int pa, pb;
       pair_start(grp, pa, pb, na_, tri);
-      for (int tb = 0; tb < npair; tb += 4) {
-        const bool act = tb + grp < npair;
-        float AF = 0.f, B = 0.f;
-        if (act) {
-          const int sa = seg[ea] + pa, sb = seg[eb] + pb;
-          const float c = w.ux[sa] * w.ux[sb] + w.uy[sa] * w.uy[sb] + w.uz[sa] * w.uz[sb];
-          // sin(theta) = |u_a x u_b|: well conditioned for nearly collinear triples,
-          // where sqrt(1 - c^2) loses most of its digits in FP32
-          const float nx = w.uy[sa] * w.uz[sb] - w.uz[sa] * w.uy[sb];
-          const float ny = w.uz[sa] * w.ux[sb] - w.ux[sa] * w.uz[sb];
-          const float nz = w.ux[sa] * w.uy[sb] - w.uy[sa] * w.ux[sb];
-          const float sn = sqrtf(nx * nx + ny * ny + nz * nz);
-          const float T = c * cth + sn * sth;
-          float p, dp;
-          powz(fmaxf(0.f, 1.f + T), k, p, dp);
-          AF = k.two_1mz * p * w.fc[sa] * w.fc[sb];
-          const float u = 0.5f * (w.r[sa] + w.r[sb]) - rsq;
-          B = expf(-k.eta * u * u);
+      // two triples per group per iteration (independent chains for latency)
+      for (int tb = 0; tb < npair; tb += 8) {
+        float AF[2], B[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          AF[h] = 0.f;
+          B[h] = 0.f;
+          if (tb + 4 * h + grp < npair) {
+            const int sa = seg[ea] + pa, sb = seg[eb] + pb;
+            const float c = w.ux[sa] * w.ux[sb] + w.uy[sa] * w.uy[sb] + w.uz[sa] * w.uz[sb];
+            // sin(theta) = |u_a x u_b|: well conditioned for nearly collinear triples,
+            // where sqrt(1 - c^2) loses most of its digits in FP32
+            const float nx = w.uy[sa] * w.uz[sb] - w.uz[sa] * w.uy[sb];
+            const float ny = w.uz[sa] * w.ux[sb] - w.ux[sa] * w.uz[sb];
+            const float nz = w.ux[sa] * w.uy[sb] - w.uy[sa] * w.ux[sb];
+            const float sn = sqrtf(nx * nx + ny * ny + nz * nz);
+            const float T = c * cth + sn * sth;
+            float p, dp;
+            powz(fmaxf(0.f, 1.f + T), k, p, dp);
+            AF[h] = k.two_1mz * p * w.fc[sa] * w.fc[sb];
+            const float u = 0.5f * (w.r[sa] + w.r[sb]) - rsq;
+            B[h] = expf(-k.eta * u * u);
+          }
+          pair_advance(pa, pb, na_, tri);
         }
 #pragma unroll
         for (int n = 0; n < 8; ++n) {
-          const float Bn = __shfl_sync(TM_FULL, B, (lane & ~7) | n);
-          acc[n] += AF * Bn;
+          const float B0 = __shfl_sync(TM_FULL, B[0], (lane & ~7) | n);
+          const float B1 = __shfl_sync(TM_FULL, B[1], (lane & ~7) | n);
+          acc[n] += AF[0] * B0 + AF[1] * B1;
         }
-        pair_advance(pa, pb, na_, tri);
       }
 #pragma unroll
       for (int n = 0; n < 8; ++n) {
@@ -311,21 +325,16 @@ __global__ void __launch_bounds__(128) k_desc_adj(const DescArgs a, const tm_con
       f = fcut(r, k.pi_tf, k.r_rc);
       fd = fcut_d(r, k.pi_tf, k.r_rc);
     }
+    // lane = edge: S = sum_n dE/dG[l, n] d/dr (exp(-eta (r - Rs_n)^2) fc(r)),
+    // the row read from shared memory as broadcasts within each element
     float myS = 0.f;
-    const int n = min(32, cr - base);
-    for (int q = 0; q < n; ++q) {
-      const float rq = __shfl_sync(TM_FULL, r, q);
-      const float fq = __shfl_sync(TM_FULL, f, q);
-      const float fdq = __shfl_sync(TM_FULL, fd, q);
-      const int lq = __shfl_sync(TM_FULL, el, q);
-      float part = 0.f;
-      if (lane < k.nr) {
-        const float t = rq - k.rs_r[lane];
+    if (s < cr) {
+      const float* up = w.row + el * k.nr;
+      for (int n = 0; n < k.nr; ++n) {
+        const float t = r - k.rs_r[n];
         const float g = expf(-k.eta * t * t);
-        part = w.row[lq * k.nr + lane] * g * (-2.f * k.eta * t * fq + fdq);
+        myS += up[n] * g * (-2.f * k.eta * t * f + fd);
       }
-      const float S = warp_sum(part);
-      if (lane == q) myS = S;
     }
     if (s < cr) {
       a.sr[(size_t)i * a.KR + s] = myS;
@@ -343,6 +352,7 @@ __global__ void __launch_bounds__(128) k_desc_adj(const DescArgs a, const tm_con
   __syncwarp();
   const int grp = lane >> 3, q = lane & 7;
   const float cth = k.cos_th[q], sth = k.sin_th[q], rsq = k.rs_a[q];
+  float fown = 0.f;   // lanes q = 0..5: one component of the centre's angular dE/dx
   for (int ea = 0; ea < k.nele; ++ea) {
     for (int eb = ea; eb < k.nele; ++eb) {
       const int na_ = seg[ea + 1] - seg[ea], nb_ = seg[eb + 1] - seg[eb];
@@ -356,78 +366,101 @@ __global__ void __launch_bounds__(128) k_desc_adj(const DescArgs a, const tm_con
       for (int n = 0; n < 8; ++n) wl[n] = src[n];
       int pa, pb;
       pair_start(grp, pa, pb, na_, tri);
-      for (int tb = 0; tb < npair; tb += 4) {
-        const bool act = tb + grp < npair;
-        int sa = 0, sb = 0;
-        float c = 0.f, sn = 0.f, A = 0.f, dA = 0.f, B = 0.f, Bd = 0.f;
-        float nx = 0.f, ny = 0.f, nz = 0.f;
-        if (act) {
-          sa = seg[ea] + pa;
-          sb = seg[eb] + pb;
-          c = w.ux[sa] * w.ux[sb] + w.uy[sa] * w.uy[sb] + w.uz[sa] * w.uz[sb];
-          // n = u_a x u_b, sin(theta) = |n| (accurate near collinearity)
-          nx = w.uy[sa] * w.uz[sb] - w.uz[sa] * w.uy[sb];
-          ny = w.uz[sa] * w.ux[sb] - w.ux[sa] * w.uz[sb];
-          nz = w.ux[sa] * w.uy[sb] - w.uy[sa] * w.ux[sb];
-          sn = sqrtf(nx * nx + ny * ny + nz * nz);
-          const float T = c * cth + sn * sth;
-          const float dT = -(sn * cth - c * sth);   // d cos(theta - theta_m) / d theta
-          float p, dp;
-          powz(fmaxf(0.f, 1.f + T), k, p, dp);
-          A = k.two_1mz * p;
-          dA = k.two_1mz * dp * dT;
-          const float u = 0.5f * (w.r[sa] + w.r[sb]) - rsq;
-          B = expf(-k.eta * u * u);
-          Bd = B * (-2.f * k.eta * u);
+      // two triples per group per iteration; the six output components of a
+      // triple (a-side xyz, b-side xyz) go to lanes q = 0..5 of its group
+      for (int tb = 0; tb < npair; tb += 8) {
+        int sa[2], sb[2];
+        bool act[2];
+        float sn[2], A[2], dA[2], B[2], Bd[2], nx[2], ny[2], nz[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          act[h] = tb + 4 * h + grp < npair;
+          sa[h] = 0; sb[h] = 0;
+          sn[h] = 0.f; A[h] = 0.f; dA[h] = 0.f; B[h] = 0.f; Bd[h] = 0.f;
+          nx[h] = 0.f; ny[h] = 0.f; nz[h] = 0.f;
+          if (act[h]) {
+            const int ia = seg[ea] + pa, ib = seg[eb] + pb;
+            sa[h] = ia;
+            sb[h] = ib;
+            const float c = w.ux[ia] * w.ux[ib] + w.uy[ia] * w.uy[ib] + w.uz[ia] * w.uz[ib];
+            // n = u_a x u_b, sin(theta) = |n| (accurate near collinearity)
+            nx[h] = w.uy[ia] * w.uz[ib] - w.uz[ia] * w.uy[ib];
+            ny[h] = w.uz[ia] * w.ux[ib] - w.ux[ia] * w.uz[ib];
+            nz[h] = w.ux[ia] * w.uy[ib] - w.uy[ia] * w.ux[ib];
+            sn[h] = sqrtf(nx[h] * nx[h] + ny[h] * ny[h] + nz[h] * nz[h]);
+            const float T = c * cth + sn[h] * sth;
+            const float dT = -(sn[h] * cth - c * sth);   // d cos(theta - theta_m) / d theta
+            float p, dp;
+            powz(fmaxf(0.f, 1.f + T), k, p, dp);
+            A[h] = k.two_1mz * p;
+            dA[h] = k.two_1mz * dp * dT;
+            const float u = 0.5f * (w.r[ia] + w.r[ib]) - rsq;
+            B[h] = expf(-k.eta * u * u);
+            Bd[h] = B[h] * (-2.f * k.eta * u);
+          }
+          pair_advance(pa, pb, na_, tri);
         }
-        float P = 0.f, Q = 0.f;
+        float P[2] = {0.f, 0.f}, Q[2] = {0.f, 0.f};
 #pragma unroll
         for (int n = 0; n < 8; ++n) {
           const int src_lane = (lane & ~7) | n;
-          P += wl[n] * __shfl_sync(TM_FULL, B, src_lane);
-          Q += wl[n] * __shfl_sync(TM_FULL, Bd, src_lane);
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            P[h] += wl[n] * __shfl_sync(TM_FULL, B[h], src_lane);
+            Q[h] += wl[n] * __shfl_sync(TM_FULL, Bd[h], src_lane);
+          }
         }
-        float S1 = A * P, S2 = A * Q, S3 = dA * P;
+        float S1[2], S2[2], S3[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          S1[h] = A[h] * P[h];
+          S2[h] = A[h] * Q[h];
+          S3[h] = dA[h] * P[h];
+        }
 #pragma unroll
         for (int o = 1; o < 8; o <<= 1) {
-          S1 += __shfl_xor_sync(TM_FULL, S1, o);
-          S2 += __shfl_xor_sync(TM_FULL, S2, o);
-          S3 += __shfl_xor_sync(TM_FULL, S3, o);
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            S1[h] += __shfl_xor_sync(TM_FULL, S1[h], o);
+            S2[h] += __shfl_xor_sync(TM_FULL, S2[h], o);
+            S3[h] += __shfl_xor_sync(TM_FULL, S3[h], o);
+          }
         }
-        if (act && q == 0) {
-          const float fa = w.fc[sa], fb = w.fc[sb];
-          const float fcc = fa * fb;
-          const float dra = 0.5f * S2 * fcc + S1 * w.fcd[sa] * fb;
-          const float drb = 0.5f * S2 * fcc + S1 * fa * w.fcd[sb];
-          const float dth = S3 * fcc;
-          // d theta / d d_a = -(u_b - c u_a) / (r_a sin theta); the in-plane
-          // directions are formed as n x u_a and u_b x n, whose length is sin theta
-          const float kc = -dth / fmaxf(sn, 1e-30f);
-          const float ra = w.r[sa], rb = w.r[sb];
-          const float uax = w.ux[sa], uay = w.uy[sa], uaz = w.uz[sa];
-          const float ubx = w.ux[sb], uby = w.uy[sb], ubz = w.uz[sb];
-          const float pax = ny * uaz - nz * uay, pay = nz * uax - nx * uaz, paz = nx * uay - ny * uax;
-          const float pbx = uby * nz - ubz * ny, pby = ubz * nx - ubx * nz, pbz = ubx * ny - uby * nx;
-          const float ka = kc / ra, kb = kc / rb;
-          const float gax = dra * uax + ka * pax;
-          const float gay = dra * uay + ka * pay;
-          const float gaz = dra * uaz + ka * paz;
-          const float gbx = drb * ubx + kb * pbx;
-          const float gby = drb * uby + kb * pby;
-          const float gbz = drb * ubz + kb * pbz;
-          fx += gax + gbx;
-          fy += gay + gby;
-          fz += gaz + gbz;
-          atomicAdd(&w.vx[sa], -gax); atomicAdd(&w.vy[sa], -gay); atomicAdd(&w.vz[sa], -gaz);
-          atomicAdd(&w.vx[sb], -gbx); atomicAdd(&w.vy[sb], -gby); atomicAdd(&w.vz[sb], -gbz);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          if (act[h] && q < 6) {
+            const int ia = sa[h], ib = sb[h];
+            const float fa = w.fc[ia], fb = w.fc[ib];
+            const float fcc = fa * fb;
+            const bool bside = q >= 3;
+            const int d = bside ? q - 3 : q;
+            // dE/dr along the edge, and d theta / d d = -(u_o - c u) / (r sin theta):
+            // the in-plane directions are n x u_a and u_b x n, of length sin theta
+            const float dr = 0.5f * S2[h] * fcc + S1[h] * (bside ? fa * w.fcd[ib] : w.fcd[ia] * fb);
+            const float kc = -(S3[h] * fcc) / fmaxf(sn[h], 1e-30f);
+            const int e = bside ? ib : ia;
+            const float* U0 = d == 0 ? w.ux : (d == 1 ? w.uy : w.uz);
+            const float* U1 = d == 0 ? w.uy : (d == 1 ? w.uz : w.ux);
+            const float* U2 = d == 0 ? w.uz : (d == 1 ? w.ux : w.uy);
+            const float n1 = d == 0 ? ny[h] : (d == 1 ? nz[h] : nx[h]);
+            const float n2 = d == 0 ? nz[h] : (d == 1 ? nx[h] : ny[h]);
+            // a side: (n x u_a)_d = n1 u2 - n2 u1; b side: (u_b x n)_d = u1 n2 - u2 n1
+            const float perp = bside ? (U1[e] * n2 - U2[e] * n1) : (n1 * U2[e] - n2 * U1[e]);
+            const float g = dr * U0[e] + (kc / w.r[e]) * perp;
+            fown += g;
+            float* V = d == 0 ? w.vx : (d == 1 ? w.vy : w.vz);
+            atomicAdd(&V[e], -g);
+          }
         }
-        pair_advance(pa, pb, na_, tri);
       }
     }
   }
   __syncwarp();
   for (int s = lane; s < ca; s += 32)
     a.va[(size_t)i * a.KA + s] = make_float4(w.vx[s], w.vy[s], w.vz[s], 0.f);
+  fx += (q == 0 || q == 3) ? fown : 0.f;
+  fy += (q == 1 || q == 4) ? fown : 0.f;
+  fz += (q == 2 || q == 5) ? fown : 0.f;
   fx = warp_sum(fx);
   fy = warp_sum(fy);
   fz = warp_sum(fz);
