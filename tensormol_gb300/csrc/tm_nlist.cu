@@ -180,17 +180,25 @@ __global__ void k_grid_from_chunks(const float* __restrict__ cbox, const int32_t
                                    int32_t* __restrict__ ncell_m, int nmol, double rc, int periodic,
                                    double Lx, double Ly, double Lz, double occ, double cap_a,
                                    double cap_c, int pnx, int pny, int pnz) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  // one warp per molecule: lanes reduce the chunk boxes, lane 0 sizes the grid
+  const int m = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (m >= nmol) return;
-  double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
-  for (int c = mol_chunk[m]; c < mol_chunk[m + 1]; ++c)
+  float mnf[3] = {3e38f, 3e38f, 3e38f}, mxf[3] = {-3e38f, -3e38f, -3e38f};
+  for (int c = mol_chunk[m] + lane; c < mol_chunk[m + 1]; c += 32)
     for (int d = 0; d < 3; ++d) {
-      mn[d] = fmin(mn[d], (double)cbox[8 * c + d]);
-      mx[d] = fmax(mx[d], (double)cbox[8 * c + 3 + d]);
+      mnf[d] = fminf(mnf[d], cbox[8 * c + d]);
+      mxf[d] = fmaxf(mxf[d], cbox[8 * c + 3 + d]);
     }
+  for (int o = 16; o > 0; o >>= 1)
+    for (int d = 0; d < 3; ++d) {
+      mnf[d] = fminf(mnf[d], __shfl_xor_sync(TM_FULL, mnf[d], o));
+      mxf[d] = fmaxf(mxf[d], __shfl_xor_sync(TM_FULL, mxf[d], o));
+    }
+  if (lane != 0) return;
+  double mn[3], mx[3];
   for (int d = 0; d < 3; ++d) {
-    mn[d] -= 1e-5 + 1e-6 * fabs(mn[d]);
-    mx[d] += 1e-5 + 1e-6 * fabs(mx[d]);
+    mn[d] = (double)mnf[d] - (1e-5 + 1e-6 * fabs((double)mnf[d]));
+    mx[d] = (double)mxf[d] + (1e-5 + 1e-6 * fabs((double)mxf[d]));
   }
   const tm_grid g = grid_from_bbox(mn, mx, off[m], off[m + 1], rc, periodic, Lx, Ly, Lz, occ,
                                    cap_a, cap_c, pnx, pny, pnz);
@@ -230,16 +238,37 @@ __global__ void k_cell_fill(const int32_t* __restrict__ cell_of, const int32_t* 
 }
 
 // Atom order inside a cell is made deterministic (ascending index).
-__global__ void k_cell_sort(const int32_t* __restrict__ start, int32_t* __restrict__ atoms,
-                            const int32_t* __restrict__ ncell, int cap) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
+// Atoms of each cell in ascending index order (the fill used atomics), one
+// warp per cell: every atom's rank is the number of smaller indices in the
+// cell, counted from a shared-memory copy; cells above kSortMax atoms (not
+// expected) fall back to an insertion sort by one lane.
+constexpr int kSortMax = 128;
+__global__ void __launch_bounds__(128) k_cell_sort(const int32_t* __restrict__ start,
+                                                   int32_t* __restrict__ atoms,
+                                                   const int32_t* __restrict__ ncell, int cap) {
+  __shared__ int32_t buf[4][kSortMax];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * 4 + wib;
   if (c >= cap || c >= *ncell) return;
-  int a = start[c], b = start[c + 1];
-  for (int p = a + 1; p < b; ++p) {
-    int v = atoms[p];
-    int q = p - 1;
-    while (q >= a && atoms[q] > v) { atoms[q + 1] = atoms[q]; --q; }
-    atoms[q + 1] = v;
+  const int a = start[c], b = start[c + 1], n = b - a;
+  if (n <= 1) return;
+  if (n <= kSortMax) {
+    int32_t* v = buf[wib];
+    for (int t = lane; t < n; t += 32) v[t] = atoms[a + t];
+    __syncwarp();
+    for (int t = lane; t < n; t += 32) {
+      const int x = v[t];
+      int rank = 0;
+      for (int q = 0; q < n; ++q) rank += v[q] < x;
+      atoms[a + rank] = x;
+    }
+  } else if (lane == 0) {
+    for (int p = a + 1; p < b; ++p) {
+      const int v = atoms[p];
+      int q = p - 1;
+      while (q >= a && atoms[q] > v) { atoms[q + 1] = atoms[q]; --q; }
+      atoms[q + 1] = v;
+    }
   }
 }
 
@@ -805,7 +834,7 @@ int tm_launch_nlist(tm_system* s) {
   int rc;
   if ((rc = tm_launch_positions(s))) return rc;
   k_cbox_chunks<<<s->nchunk, 256, 0, st>>>(s->d_chunk, s->d_xhi, s->d_cbox);
-  k_grid_from_chunks<<<tm_div_up(s->nmol, 128), 128, 0, st>>>(
+  k_grid_from_chunks<<<tm_div_up(s->nmol, 4), 128, 0, st>>>(
       s->d_cbox, s->d_mol_chunk, s->d_off, s->d_grid, s->d_ncell_m, s->nmol, k.r_rc_d,
       s->periodic ? 1 : 0, s->lat[0], s->lat[4], s->lat[8], 0.0, 2.0, 64.0, 0, 0, 0);
   ctx->launches++;
@@ -823,8 +852,8 @@ int tm_launch_nlist(tm_system* s) {
   cudaMemsetAsync(s->d_cell_cnt, 0, sizeof(int32_t) * (s->ncell_cap + 1), st);
   k_cell_fill<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_cell_of_atom, s->d_cell_start,
                                                      s->d_cell_cnt, s->d_cell_atoms, s->N);
-  k_cell_sort<<<tm_div_up(s->ncell_cap, 128), 128, 0, st>>>(s->d_cell_start, s->d_cell_atoms,
-                                                             s->d_ncell, s->ncell_cap);
+  k_cell_sort<<<tm_div_up(s->ncell_cap, 4), 128, 0, st>>>(s->d_cell_start, s->d_cell_atoms,
+                                                           s->d_ncell, s->ncell_cap);
   ctx->launches += 2;
   cudaMemsetAsync(s->d_need, 0, sizeof(int32_t) * 2, st);
   NbrArgs a = make_nbr_args(s, s->d_need);
@@ -843,7 +872,7 @@ int tm_launch_nlist(tm_system* s) {
                                                     s->d_mol, s->d_off, s->N, s->KA);
   ctx->launches += 3;
   // Coulomb grid: about 24 atoms per cell, atoms packed in cell order
-  k_grid_from_chunks<<<tm_div_up(s->nmol, 128), 128, 0, st>>>(
+  k_grid_from_chunks<<<tm_div_up(s->nmol, 4), 128, 0, st>>>(
       s->d_cbox, s->d_mol_chunk, s->d_off, s->d_egrid, s->d_encell_m, s->nmol, 2.0,
       s->periodic ? 1 : 0, s->lat[0], s->lat[4], s->lat[8], 24.0, 0.125, 8.0, s->ee_dims[0],
       s->ee_dims[1], s->ee_dims[2]);
@@ -860,8 +889,8 @@ int tm_launch_nlist(tm_system* s) {
   cudaMemsetAsync(s->d_ecell_cnt, 0, sizeof(int32_t) * (s->ecell_cap + 1), st);
   k_cell_fill<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_ecell_of_atom, s->d_ecell_start,
                                                      s->d_ecell_cnt, s->d_ecell_atoms, s->N);
-  k_cell_sort<<<tm_div_up(s->ecell_cap, 128), 128, 0, st>>>(s->d_ecell_start, s->d_ecell_atoms,
-                                                              s->d_encell, s->ecell_cap);
+  k_cell_sort<<<tm_div_up(s->ecell_cap, 4), 128, 0, st>>>(s->d_ecell_start, s->d_ecell_atoms,
+                                                            s->d_encell, s->ecell_cap);
   k_ee_pack<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_ecell_atoms, s->d_x, s->d_elem, s->d_mol,
                                                   s->d_egrid, s->d_ecell_of_atom, s->d_epos,
                                                   s->d_exhi, s->N);
@@ -1134,7 +1163,7 @@ extern "C" int tm_nlist_build_static(const double* x, const int32_t* elem, int n
   cudaMemsetAsync(S->cell_cnt, 0, sizeof(int32_t) * (cap + 1), st);
   k_cell_fill<<<tm_div_up(N, 256), 256, 0, st>>>(S->cell_of_atom, S->cell_start, S->cell_cnt,
                                                   S->cell_atoms, N);
-  k_cell_sort<<<tm_div_up(cap, 128), 128, 0, st>>>(S->cell_start, S->cell_atoms, &S->ncell, cap);
+  k_cell_sort<<<tm_div_up(cap, 4), 128, 0, st>>>(S->cell_start, S->cell_atoms, &S->ncell, cap);
   NbrArgs a;
   a.x = x; a.xhi = S->xhi; a.xlo = S->xlo; a.mol = S->mol; a.elem = elem; a.grid = &S->grid;
   a.cell_of = S->cell_of_atom; a.cell_start = S->cell_start; a.cell_atoms = S->cell_atoms;
