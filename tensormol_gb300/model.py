@@ -358,6 +358,7 @@ def EnergyAndForce(manager, atoms, Rr_cut=None, Ra_cut=None, Ree_cut=None):
         return sysm
 
     EnAndForce.system_for = system_for
+    EnAndForce.model = manager.Instances   # lets drivers batch structures (tensormol_gb300.opt)
     return EnAndForce
 
 

@@ -82,7 +82,16 @@ PARAMS = {
     "OptMaxCycles": 50,
     "OptThresh": 0.0001,
     "OptMaxStep": 0.1,
+    "OptStepSize": 0.1,
+    "OptMomentum": 0.5,
+    "OptMomentumDecay": 0.8,
     "GSSearchAlpha": 0.05,
+    "SDStep": 0.05,
+    "NebSolver": "Verlet",
+    "NebNumBeads": 18,
+    "NebK": 0.07,
+    "NebClimbingImage": True,
+    "RemoveInvariant": True,
 }
 
 ACTIVATIONS = {"relu": 0, "sigmoid_with_param": 1, "softplus": 2, "tanh": 3,
