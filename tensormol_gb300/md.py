@@ -16,6 +16,7 @@ package; any other routine raises (there is no host integrator here).
 from __future__ import annotations
 
 import ctypes
+import os
 
 import numpy as np
 
@@ -108,9 +109,38 @@ class VelocityVerlet:
         self.md.set_velocities(self.v)
         self.md_log = None
 
+    def WriteTrajectory(self):
+        """Append the current frame to ./results/MDTrajectory<name>.xyz with
+        Time, KineticEnergy and PotEnergy (SimpleMD.py:383-389)."""
+        from .model import Mol
+        m = Mol(self.atoms, self.x)
+        m.properties["Time"] = self.t
+        m.properties["KineticEnergy"] = self.KE
+        m.properties["PotEnergy"] = self.EPot
+        m.WriteXYZfile("./results/", "MDTrajectory" + self.name)
+
     def Prop(self):
-        """Propagate maxstep steps on the device (SimpleMD.py:391-424)."""
-        log = self.md.run(self.maxstep)
+        """Propagate maxstep steps on the device (SimpleMD.py:391-424). With
+        PARAMS["MDLogTrajectory"] the run pauses every third step to append a
+        frame (positions come back only then); md_log is saved to
+        ./results/MDLog<name>.txt every 500 steps and at the end."""
+        if PARAMS.get("MDLogTrajectory"):
+            logs = []
+            done = 0
+            while done < self.maxstep:
+                n = min(3 if done else 1, self.maxstep - done)
+                part = self.md.run(n)
+                logs.append(part)
+                done += n
+                self.x = self.system.positions()
+                self.t = (done - 1) * self.dt
+                self.EPot = float(part[-1, 0])
+                self.KE = float(part[-1, 1])
+                if (done - 1) % 3 == 0:
+                    self.WriteTrajectory()
+            log = np.concatenate(logs)
+        else:
+            log = self.md.run(self.maxstep)
         self.md_log = np.zeros((self.maxstep, 7))
         self.md_log[:, 0] = np.arange(self.maxstep) * self.dt
         ke_prev = np.concatenate([[0.0], log[:-1, 1]])
@@ -122,4 +152,7 @@ class VelocityVerlet:
         self.t = (self.maxstep - 1) * self.dt
         self.EPot = float(log[-1, 0]) if self.maxstep else self.EPot0
         self.KE = float(log[-1, 1]) if self.maxstep else 0.0
+        if PARAMS.get("MDLogTrajectory") or os.path.isdir("./results"):
+            os.makedirs("./results", exist_ok=True)
+            np.savetxt("./results/" + "MDLog" + self.name + ".txt", self.md_log)
         return self.md_log

@@ -17,6 +17,8 @@ from . import _lib
 from .params import JOULEPERHARTREE, PARAMS, ACTIVATIONS, descriptor_width, element_pairs
 
 _F64 = np.float64
+# element symbols by atomic number (PhysicalData.py:17-18), Z = 1..10 here
+_SYMBOLS = ["X", "H", "He", "Li", "Be", "B", "C", "N", "O", "F", "Ne"]
 
 
 def _ptr(a):
@@ -366,13 +368,58 @@ class Mol:
     """Minimal molecule container with the reference's fields
     (Containers/Mol.py:7-23: atoms, coords, properties)."""
 
-    def __init__(self, atoms, coords):
-        self.atoms = np.asarray(atoms)
-        self.coords = np.asarray(coords, dtype=_F64)
+    def __init__(self, atoms=None, coords=None):
+        self.atoms = np.asarray([] if atoms is None else atoms, dtype=np.int64)
+        self.coords = np.asarray(np.zeros((0, 3)) if coords is None else coords, dtype=_F64)
         self.properties = {}
 
     def NAtoms(self):
         return int(self.atoms.shape[0])
+
+    # -- XYZ text, the reference's format (Containers/Mol.py:268-360) -------
+    def PropertyString(self):
+        out = ""
+        for prop, val in self.properties.items():
+            out += ";;;" + prop + " " + str(val)
+        return out
+
+    def __str__(self, wprop=False):
+        n = self.NAtoms()
+        lines = str(n) + "\nComment: " + (self.PropertyString() if wprop else "") + "\n"
+        rows = [_SYMBOLS[int(z)] + "   " + str(c[0]) + "  " + str(c[1]) + "  " + str(c[2])
+                for z, c in zip(self.atoms, self.coords)]
+        return lines + "\n".join(rows)
+
+    def WriteXYZfile(self, fpath=".", fname="mol", mode="a", wprop=False):
+        import os
+        path = os.path.join(fpath, fname + ".xyz")
+        os.makedirs(os.path.dirname(path) or ".", exist_ok=True)
+        with open(path, mode) as f:
+            for line in self.__str__(wprop).split("\n"):
+                f.write(line + "\n")
+
+    def FromXYZString(self, string):
+        lines = string.split("\n")
+        n = int(lines[0])
+        if "Comment:" in lines[1]:
+            for prop in lines[1].split("Comment:")[1].split(";;;"):
+                s = prop.split()
+                if len(s) >= 2:
+                    try:
+                        self.properties[s[0]] = float(s[1])
+                    except ValueError:
+                        self.properties[s[0]] = " ".join(s[1:])
+        atoms, coords = [], []
+        for i in range(n):
+            t = lines[i + 2].split()
+            atoms.append(_SYMBOLS.index(t[0]))
+            coords.append([float(t[1]), float(t[2]), float(t[3])])
+        self.atoms = np.array(atoms, dtype=np.int64)
+        self.coords = np.array(coords, dtype=_F64)
+
+    def ReadAtomsFromXYZFile(self, path):
+        with open(path) as f:
+            self.FromXYZString(f.read())
 
 
 class MSet:

@@ -227,3 +227,33 @@ def test_velocity_verlet_driver_mirror(gpu):
     assert np.abs(vv.x - x).max() < X_TOL
     assert mdlog.shape == (10, 7) and mdlog[0, 4] == 0.0
     assert abs(mdlog[-1, 5] - e) * EV_PER_HARTREE / w.natoms < E_TOL
+
+
+def test_velocity_verlet_trajectory_files(gpu, tmp_path, monkeypatch):
+    """MDLogTrajectory: frames at steps 0, 3, 6, ... in ./results, positions equal
+    to an uninterrupted device run of the same steps; md_log saved."""
+    model, md = gpu
+    from tensormol_gb300.model import EnergyAndForce, Mol, TFMolManage
+    w = systems.water_cluster_60(seed=0)
+    m, _ = _models(model, [1, 8])
+    monkeypatch.chdir(tmp_path)
+    saved = {k: PARAMS.get(k) for k in ("MDMaxStep", "MDdt", "MDThermostat", "MDV0", "MDLogTrajectory")}
+    try:
+        PARAMS.update(MDMaxStep=8, MDdt=0.5, MDThermostat=None, MDV0="Thermal", MDLogTrajectory=True)
+        vv = md.VelocityVerlet(None, Mol(w.Z, w.x), "w60", EnergyAndForce(TFMolManage(m), w.Z),
+                               seed=5)
+        v0 = vv.v.copy()
+        vv.Prop()
+    finally:
+        PARAMS.update(saved)
+    text = (tmp_path / "results" / "MDTrajectoryw60.xyz").read_text()
+    frames = [f for f in text.split("60\nComment:") if f.strip()]
+    assert len(frames) == 3                                   # steps 0, 3, 6
+    assert (tmp_path / "results" / "MDLogw60.txt").exists()
+    s = m.system(w.x, w.Z, w.offsets)
+    dyn = md.DeviceMD(s, "nve", dt=0.5)
+    dyn.set_velocities(v0)
+    dyn.run(7)
+    last = Mol()
+    last.FromXYZString("60\nComment:" + frames[-1])
+    np.testing.assert_allclose(last.coords, s.positions(), rtol=0, atol=1e-12)
