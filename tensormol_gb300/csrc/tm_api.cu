@@ -550,6 +550,8 @@ static int system_alloc(tm_system* s, int N_cap, int nmol_cap, int Mpad_cap, int
   A.get(&s->d_cell_start, sizeof(int32_t) * (ncell_alloc + 1));
   A.get(&s->d_cell_atoms, sizeof(int32_t) * N);
   A.get(&s->d_cell_of_atom, sizeof(int32_t) * N);
+  A.get(&s->d_sort_tmp, sizeof(int32_t) * N);
+  A.get(&s->d_scan_tmp, sizeof(int32_t) * 4096);
   A.get(&s->d_chunk, sizeof(int2) * nchunk_cap);
   A.get(&s->d_mol_chunk, sizeof(int32_t) * (nmol + 1));
   A.get(&s->d_part, sizeof(double) * 8 * nchunk_cap);
@@ -698,7 +700,7 @@ static void system_free(tm_system* s) {
                   s->d_off, s->d_x, s->d_xhi, s->d_xlo, s->d_x_at_build, s->d_grid, s->d_ncell, s->d_ncell_m, s->d_need,
                   s->d_chunk, s->d_mol_chunk, s->d_part, s->d_cbox,
                   s->d_egrid, s->d_encell, s->d_encell_m, s->d_ecell_cnt, s->d_ecell_start,
-                  s->d_ecell_atoms, s->d_ecell_of_atom, s->d_epos, s->d_exhi, s->d_exlo,
+                  s->d_ecell_atoms, s->d_ecell_of_atom, s->d_epos, s->d_exhi, s->d_exlo, s->d_sort_tmp, s->d_scan_tmp,
                   s->d_cpart,
                   s->d_cell_cnt, s->d_cell_start, s->d_cell_atoms, s->d_cell_of_atom, s->d_cnt_r,
                   s->d_cnt_a, s->d_nbr_r, s->d_nbr_a, s->d_rev_r, s->d_rev_a, s->d_sr, s->d_va,

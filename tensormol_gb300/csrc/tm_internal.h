@@ -123,6 +123,8 @@ struct tm_system {
   int32_t* d_cell_start = nullptr;     // [ncell_cap+1]
   int32_t* d_cell_atoms = nullptr;     // [N]
   int32_t* d_cell_of_atom = nullptr;   // [N]
+  int32_t* d_sort_tmp = nullptr;       // [N] scratch of the cell sort (crowded cells)
+  int32_t* d_scan_tmp = nullptr;       // [4096] block sums of the cell-count scans
   // coarser grid for the Coulomb/vdW pair terms (about 24 atoms per cell)
   int ee_dims[3] = {0, 0, 0};          // periodic: host-chosen cells per edge
   int ecell_cap = 0;
@@ -146,6 +148,7 @@ struct tm_system {
   int32_t* d_rev_r = nullptr;          // [N*KR] j*KR + position of i in j's list
   int32_t* d_rev_a = nullptr;
   bool nlist_valid = false;
+  bool need_sticky = false;            // keep the overflow counters across builds (MD chunks)
   // descriptors + networks
   void* G[2] = {};                     // [Mpad][Dp] hi/lo (tf32) or bf16 (G[0])
   void* H1[2] = {};                    // [2*Mpad][H] per net stacked

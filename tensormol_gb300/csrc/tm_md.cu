@@ -184,9 +184,14 @@ __global__ void k_accel(double* __restrict__ a, const double* __restrict__ F,
 
 // log row: potential (Hartree, summed over molecules), KE per atom (J/mol),
 // conserved (J/mol), T_eff (K)
-__global__ void k_log(double* __restrict__ row, const double* __restrict__ molE, int nmol,
+// The row is log + 4 * (*step); the step counter lives on the device so that
+// one captured step can be replayed.
+__global__ void k_log(double* __restrict__ log, int* __restrict__ step,
+                      const double* __restrict__ molE, int nmol,
                       const double* __restrict__ sc, int kind, int M, double kT, double gnkt,
                       double Qnose, double N) {
+  double* row = log + 4 * (size_t)(*step);
+  *step += 1;
   double pe = 0.0;
   for (int m = 0; m < nmol; ++m) pe += molE[4 * m];
   const double ke = 0.5 * sc[S_KE2] * 1e10;   // J/mol total
@@ -221,6 +226,10 @@ struct tm_md {
   double* vh = nullptr;
   double* sc = nullptr;
   double* part = nullptr;
+  double* ck_x = nullptr;    // chunk-start copies (overflow replay)
+  double* ck_v = nullptr;
+  double* ck_a = nullptr;
+  double* ck_sc = nullptr;
   size_t bytes = 0;
 };
 
@@ -248,7 +257,9 @@ extern "C" int tm_md_create(tm_system* s, int kind, double dt, double T, int cha
   int rc;
   if ((rc = tm_alloc(ctx, (void**)&md->v, n3 * 8)) || (rc = tm_alloc(ctx, (void**)&md->a, n3 * 8)) ||
       (rc = tm_alloc(ctx, (void**)&md->vh, n3 * 8)) || (rc = tm_alloc(ctx, (void**)&md->m, (size_t)N * 8)) ||
-      (rc = tm_alloc(ctx, (void**)&md->sc, nsc * 8)) || (rc = tm_alloc(ctx, (void**)&md->part, RB * 8))) {
+      (rc = tm_alloc(ctx, (void**)&md->sc, nsc * 8)) || (rc = tm_alloc(ctx, (void**)&md->part, RB * 8)) ||
+      (rc = tm_alloc(ctx, (void**)&md->ck_x, n3 * 8)) || (rc = tm_alloc(ctx, (void**)&md->ck_v, n3 * 8)) ||
+      (rc = tm_alloc(ctx, (void**)&md->ck_a, n3 * 8)) || (rc = tm_alloc(ctx, (void**)&md->ck_sc, nsc * 8))) {
     delete md;
     return rc;
   }
@@ -285,6 +296,10 @@ extern "C" int tm_md_destroy(tm_md* md) {
   tm_free(ctx, md->m, (size_t)md->s->N * 8);
   tm_free(ctx, md->sc, (S_CHAIN + 40) * 8);
   tm_free(ctx, md->part, RB * 8);
+  tm_free(ctx, md->ck_x, n3 * 8);
+  tm_free(ctx, md->ck_v, n3 * 8);
+  tm_free(ctx, md->ck_a, n3 * 8);
+  tm_free(ctx, md->ck_sc, (S_CHAIN + 40) * 8);
   cudaStreamSynchronize(ctx->stream);
   delete md;
   return TM_OK;
@@ -317,67 +332,141 @@ static void ke_into(tm_md* md, const double* v, int slot) {
   ctx->launches += 2;
 }
 
-extern "C" int tm_md_run(tm_md* md, int nsteps, double skin, double* log) {
-  if (!md || nsteps < 0) return TM_E_ARG;
-  (void)skin;   // lists are rebuilt every step (exact membership each step)
+// One integrator step (all kernels enqueued, no host synchronisation).
+static int md_step(tm_md* md, double* dlog, int* dstep) {
   tm_system* s = md->s;
   tm_ctx* ctx = s->ctx;
   cudaStream_t st = ctx->stream;
   const int N = s->N, n3 = 3 * N;
   const int gb = tm_div_up(n3, 256);
   const double dt = md->dt;
-  double* dlog = nullptr;
-  int rc;
-  if (nsteps > 0 && (rc = tm_alloc(ctx, (void**)&dlog, sizeof(double) * 4 * nsteps))) return rc;
   const unsigned flags = 0;
-  for (int step = 0; step < nsteps; ++step) {
-    if (md->kind == TM_MD_NVE) {
-      k_vv_pos<<<gb, 256, 0, st>>>(s->d_x, md->v, md->a, dt, n3);
-      ctx->launches++;
-      if (s->periodic) { k_wrap<<<tm_div_up(N, 256), 256, 0, st>>>(s->d_x, s->lat[0], s->lat[4], s->lat[8], N); ctx->launches++; }
-      if ((rc = tm_energy_force_device(s, flags))) break;
-      k_vv_vel<<<gb, 256, 0, st>>>(md->v, md->a, s->d_F, md->m, dt, n3);
-      ctx->launches++;
-      ke_into(md, md->v, S_KE2);
-    } else if (md->kind == TM_MD_NOSE) {
-      ke_into(md, md->v, S_KE2);
-      k_nose_pos<<<gb, 256, 0, st>>>(s->d_x, md->v, md->a, md->vh, md->sc, dt, n3);
-      ctx->launches++;
-      if (s->periodic) { k_wrap<<<tm_div_up(N, 256), 256, 0, st>>>(s->d_x, s->lat[0], s->lat[4], s->lat[8], N); ctx->launches++; }
-      ke_into(md, md->vh, S_KE2B);
-      if ((rc = tm_energy_force_device(s, flags))) break;
-      k_nose_eta<<<1, 1, 0, st>>>(md->sc, md->Qnose, md->kT, (double)N, dt);
-      k_nose_vel<<<gb, 256, 0, st>>>(md->v, md->a, md->vh, s->d_F, md->m, md->sc, dt, n3);
-      ctx->launches += 2;
-      ke_into(md, md->v, S_KE2);
-    } else {
-      ke_into(md, md->v, S_KE2);
-      k_nhc_chain<<<1, 1, 0, st>>>(md->sc, md->M, md->kT, md->gnkt, dt);
-      k_scale<<<gb, 256, 0, st>>>(md->v, md->sc, n3);
-      k_kick<<<gb, 256, 0, st>>>(md->v, md->a, 0.5 * dt, n3);
-      k_drift<<<gb, 256, 0, st>>>(s->d_x, md->v, dt, n3);
-      ctx->launches += 4;
-      if (s->periodic) { k_wrap<<<tm_div_up(N, 256), 256, 0, st>>>(s->d_x, s->lat[0], s->lat[4], s->lat[8], N); ctx->launches++; }
-      if ((rc = tm_energy_force_device(s, flags))) break;
-      k_accel<<<gb, 256, 0, st>>>(md->a, s->d_F, md->m, n3);
-      k_kick<<<gb, 256, 0, st>>>(md->v, md->a, 0.5 * dt, n3);
-      ctx->launches += 2;
-      ke_into(md, md->v, S_KE2);
-      k_nhc_chain<<<1, 1, 0, st>>>(md->sc, md->M, md->kT, md->gnkt, dt);
-      k_scale<<<gb, 256, 0, st>>>(md->v, md->sc, n3);
-      ctx->launches += 2;
-      ke_into(md, md->v, S_KE2);
-    }
-    k_log<<<1, 1, 0, st>>>(dlog + 4 * step, s->d_mol_E, s->nmol, md->sc, md->kind, md->M, md->kT,
-                           md->gnkt, md->Qnose, (double)N);
+  int rc;
+  if (md->kind == TM_MD_NVE) {
+    k_vv_pos<<<gb, 256, 0, st>>>(s->d_x, md->v, md->a, dt, n3);
     ctx->launches++;
+    if (s->periodic) { k_wrap<<<tm_div_up(N, 256), 256, 0, st>>>(s->d_x, s->lat[0], s->lat[4], s->lat[8], N); ctx->launches++; }
+    if ((rc = tm_energy_force_device(s, flags))) return rc;
+    k_vv_vel<<<gb, 256, 0, st>>>(md->v, md->a, s->d_F, md->m, dt, n3);
+    ctx->launches++;
+    ke_into(md, md->v, S_KE2);
+  } else if (md->kind == TM_MD_NOSE) {
+    ke_into(md, md->v, S_KE2);
+    k_nose_pos<<<gb, 256, 0, st>>>(s->d_x, md->v, md->a, md->vh, md->sc, dt, n3);
+    ctx->launches++;
+    if (s->periodic) { k_wrap<<<tm_div_up(N, 256), 256, 0, st>>>(s->d_x, s->lat[0], s->lat[4], s->lat[8], N); ctx->launches++; }
+    ke_into(md, md->vh, S_KE2B);
+    if ((rc = tm_energy_force_device(s, flags))) return rc;
+    k_nose_eta<<<1, 1, 0, st>>>(md->sc, md->Qnose, md->kT, (double)N, dt);
+    k_nose_vel<<<gb, 256, 0, st>>>(md->v, md->a, md->vh, s->d_F, md->m, md->sc, dt, n3);
+    ctx->launches += 2;
+    ke_into(md, md->v, S_KE2);
+  } else {
+    ke_into(md, md->v, S_KE2);
+    k_nhc_chain<<<1, 1, 0, st>>>(md->sc, md->M, md->kT, md->gnkt, dt);
+    k_scale<<<gb, 256, 0, st>>>(md->v, md->sc, n3);
+    k_kick<<<gb, 256, 0, st>>>(md->v, md->a, 0.5 * dt, n3);
+    k_drift<<<gb, 256, 0, st>>>(s->d_x, md->v, dt, n3);
+    ctx->launches += 4;
+    if (s->periodic) { k_wrap<<<tm_div_up(N, 256), 256, 0, st>>>(s->d_x, s->lat[0], s->lat[4], s->lat[8], N); ctx->launches++; }
+    if ((rc = tm_energy_force_device(s, flags))) return rc;
+    k_accel<<<gb, 256, 0, st>>>(md->a, s->d_F, md->m, n3);
+    k_kick<<<gb, 256, 0, st>>>(md->v, md->a, 0.5 * dt, n3);
+    ctx->launches += 2;
+    ke_into(md, md->v, S_KE2);
+    k_nhc_chain<<<1, 1, 0, st>>>(md->sc, md->M, md->kT, md->gnkt, dt);
+    k_scale<<<gb, 256, 0, st>>>(md->v, md->sc, n3);
+    ctx->launches += 2;
+    ke_into(md, md->v, S_KE2);
   }
-  if (!rc && log && nsteps > 0)
+  k_log<<<1, 1, 0, st>>>(dlog, dstep, s->d_mol_E, s->nmol, md->sc, md->kind, md->M, md->kT,
+                         md->gnkt, md->Qnose, (double)N);
+  ctx->launches++;
+  return TM_OK;
+}
+
+// Steps run in chunks of kChunk. Each chunk starts from a device-side copy of
+// the state (positions, velocities, accelerations, thermostat scalars); the
+// neighbour-row overflow counters stay armed across the chunk's list builds.
+// If any build of the chunk overflowed its rows, the rows are grown and the
+// chunk is run again from the copy, so a run never keeps a force computed
+// from a truncated row. One host synchronisation per chunk. Within a chunk the
+// launch sequence of one step (about 45 kernels) is captured once into a CUDA
+// graph and replayed; it is captured again after the rows grow (new buffers).
+extern "C" int tm_md_run(tm_md* md, int nsteps, double skin, double* log) {
+  if (!md || nsteps < 0 || skin < 0) return TM_E_ARG;
+  tm_system* s = md->s;
+  tm_ctx* ctx = s->ctx;
+  cudaStream_t st = ctx->stream;
+  const size_t n3b = sizeof(double) * 3 * (size_t)s->N;
+  const size_t nsc = sizeof(double) * (S_CHAIN + 40);
+  constexpr int kChunk = 64;
+  double* dlog = nullptr;
+  int* dstep = nullptr;
+  int rc = TM_OK;
+  if (nsteps == 0) return TM_OK;
+  if ((rc = tm_alloc(ctx, (void**)&dlog, sizeof(double) * 4 * nsteps)) ||
+      (rc = tm_alloc(ctx, (void**)&dstep, sizeof(int))))
+    return rc;
+  s->need_sticky = true;
+  // the first step runs uncaptured: it builds what later steps reuse (lists
+  // grown to fit, one-time function attributes) and checks that a step works
+  cudaGraphExec_t exec = nullptr;
+  int64_t launches_per_step = 0;
+  int start = 0, retries = 0;
+  while (!rc && start < nsteps) {
+    const int n = nsteps - start < kChunk ? nsteps - start : kChunk;
+    cudaMemcpyAsync(md->ck_x, s->d_x, n3b, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(md->ck_v, md->v, n3b, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(md->ck_a, md->a, n3b, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(md->ck_sc, md->sc, nsc, cudaMemcpyDeviceToDevice, st);
+    cudaMemsetAsync(s->d_need, 0, sizeof(int32_t) * 2, st);
+    cudaMemcpyAsync(dstep, &start, sizeof(int), cudaMemcpyHostToDevice, st);
+    int q = 0;
+    if (!exec) {                                   // plain first step of the chunk
+      const int64_t l0 = ctx->launches;
+      rc = md_step(md, dlog, dstep);
+      launches_per_step = ctx->launches - l0;
+      q = 1;
+      if (!rc && q < n) {
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+          const int64_t l1 = ctx->launches;
+          rc = md_step(md, dlog, dstep);
+          ctx->launches = l1;
+          e = cudaStreamEndCapture(st, &graph);
+          if (!rc && e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+          if (graph) cudaGraphDestroy(graph);
+        }
+        if (!rc && e != cudaSuccess) rc = tm_cuda_check(ctx, e, "md step graph");
+      }
+    }
+    for (; q < n && !rc; ++q) {
+      rc = tm_cuda_check(ctx, cudaGraphLaunch(exec, st), "md step replay");
+      ctx->launches += launches_per_step;
+    }
+    if (rc) break;
+    bool grew = false;
+    if ((rc = tm_nlist_grow(s, &grew))) break;          // synchronises the stream
+    if ((rc = tm_sync_status(ctx, "md chunk"))) break;  // a device error ends the run
+    if (grew) {
+      if (++retries > 8) { rc = tm_fail(ctx, TM_E_CAPACITY, "neighbour rows keep overflowing"); break; }
+      cudaMemcpyAsync(s->d_x, md->ck_x, n3b, cudaMemcpyDeviceToDevice, st);
+      cudaMemcpyAsync(md->v, md->ck_v, n3b, cudaMemcpyDeviceToDevice, st);
+      cudaMemcpyAsync(md->a, md->ck_a, n3b, cudaMemcpyDeviceToDevice, st);
+      cudaMemcpyAsync(md->sc, md->ck_sc, nsc, cudaMemcpyDeviceToDevice, st);
+      if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }   // buffers were replaced
+      continue;                                          // the same chunk again
+    }
+    start += n;
+  }
+  if (exec) cudaGraphExecDestroy(exec);
+  s->need_sticky = false;
+  if (!rc && log)
     rc = tm_cuda_check(ctx, cudaMemcpyAsync(log, dlog, sizeof(double) * 4 * nsteps, cudaMemcpyDeviceToHost, st), "md log");
-  bool grew = false;
-  if (!rc) rc = tm_nlist_grow(s, &grew);
-  if (!rc && grew) rc = tm_fail(ctx, TM_E_CAPACITY, "neighbour rows overflowed during MD; rerun");
-  if (dlog) tm_free(ctx, dlog, sizeof(double) * 4 * nsteps);
+  tm_free(ctx, dlog, sizeof(double) * 4 * nsteps);
+  tm_free(ctx, dstep, sizeof(int));
   if (!rc) rc = tm_sync_status(ctx, "md_run");
   return rc;
 }

@@ -240,11 +240,12 @@ __global__ void k_cell_fill(const int32_t* __restrict__ cell_of, const int32_t* 
 // Atom order inside a cell is made deterministic (ascending index).
 // Atoms of each cell in ascending index order (the fill used atomics), one
 // warp per cell: every atom's rank is the number of smaller indices in the
-// cell, counted from a shared-memory copy; cells above kSortMax atoms (not
-// expected) fall back to an insertion sort by one lane.
+// cell, counted from a copy (shared memory up to kSortMax atoms, else the
+// cell's range of tmp[], for cells that crowding has made very large).
 constexpr int kSortMax = 128;
 __global__ void __launch_bounds__(128) k_cell_sort(const int32_t* __restrict__ start,
                                                    int32_t* __restrict__ atoms,
+                                                   int32_t* __restrict__ tmp,
                                                    const int32_t* __restrict__ ncell, int cap) {
   __shared__ int32_t buf[4][kSortMax];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -262,12 +263,14 @@ __global__ void __launch_bounds__(128) k_cell_sort(const int32_t* __restrict__ s
       for (int q = 0; q < n; ++q) rank += v[q] < x;
       atoms[a + rank] = x;
     }
-  } else if (lane == 0) {
-    for (int p = a + 1; p < b; ++p) {
-      const int v = atoms[p];
-      int q = p - 1;
-      while (q >= a && atoms[q] > v) { atoms[q + 1] = atoms[q]; --q; }
-      atoms[q + 1] = v;
+  } else {
+    for (int t = lane; t < n; t += 32) tmp[a + t] = atoms[a + t];
+    __syncwarp();
+    for (int t = lane; t < n; t += 32) {
+      const int x = tmp[a + t];
+      int rank = 0;
+      for (int q = 0; q < n; ++q) rank += tmp[a + q] < x;
+      atoms[a + rank] = x;
     }
   }
 }
@@ -780,11 +783,13 @@ __global__ void __launch_bounds__(128) k_ee_pairs(const EEArgs a) {
 }
 
 template <typename T>
-int scan_exclusive(tm_ctx* ctx, const T* in, T* out, int64_t n, T* total_dev) {
+int scan_exclusive(tm_ctx* ctx, const T* in, T* out, int64_t n, T* total_dev,
+                   T* scratch = nullptr) {
   const int64_t nb = (n + 4095) / 4096;
   if (nb > 4096) return tm_fail(ctx, TM_E_ARG, "scan too large");
-  T* bsum = nullptr;
-  if (tm_alloc(ctx, (void**)&bsum, sizeof(T) * (size_t)(nb > 0 ? nb : 1))) return TM_E_CUDA;
+  // scratch (4096 entries) keeps the per-step scans free of allocations
+  T* bsum = scratch;
+  if (!bsum && tm_alloc(ctx, (void**)&bsum, sizeof(T) * (size_t)(nb > 0 ? nb : 1))) return TM_E_CUDA;
   if (n > 0) {
     k_scan_blocks<T><<<(unsigned)nb, 1024, 0, ctx->stream>>>(in, out, bsum, n);
     k_scan_top<T><<<1, 1024, 0, ctx->stream>>>(bsum, (int)nb, total_dev);
@@ -792,7 +797,7 @@ int scan_exclusive(tm_ctx* ctx, const T* in, T* out, int64_t n, T* total_dev) {
     ctx->launches += 3;
   }
   int rc = tm_cuda_check(ctx, cudaGetLastError(), "scan");
-  tm_free(ctx, bsum, sizeof(T) * (size_t)(nb > 0 ? nb : 1));
+  if (!scratch) tm_free(ctx, bsum, sizeof(T) * (size_t)(nb > 0 ? nb : 1));
   return rc;
 }
 
@@ -847,15 +852,15 @@ int tm_launch_nlist(tm_system* s) {
                                                       ctx->d_status);
   ctx->launches++;
   if ((rc = scan_exclusive<int32_t>(ctx, s->d_cell_cnt, s->d_cell_start, s->ncell_cap + 1,
-                                    nullptr)))
+                                    nullptr, s->d_scan_tmp)))
     return rc;
   cudaMemsetAsync(s->d_cell_cnt, 0, sizeof(int32_t) * (s->ncell_cap + 1), st);
   k_cell_fill<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_cell_of_atom, s->d_cell_start,
                                                      s->d_cell_cnt, s->d_cell_atoms, s->N);
   k_cell_sort<<<tm_div_up(s->ncell_cap, 4), 128, 0, st>>>(s->d_cell_start, s->d_cell_atoms,
-                                                           s->d_ncell, s->ncell_cap);
+                                                           s->d_sort_tmp, s->d_ncell, s->ncell_cap);
   ctx->launches += 2;
-  cudaMemsetAsync(s->d_need, 0, sizeof(int32_t) * 2, st);
+  if (!s->need_sticky) cudaMemsetAsync(s->d_need, 0, sizeof(int32_t) * 2, st);
   NbrArgs a = make_nbr_args(s, s->d_need);
   const size_t shm = (size_t)4 * (s->KR + s->KA) * sizeof(uint64_t);
   if (shm > 48 * 1024) {
@@ -884,13 +889,13 @@ int tm_launch_nlist(tm_system* s) {
                                                       ctx->d_status);
   ctx->launches += 3;
   if ((rc = scan_exclusive<int32_t>(ctx, s->d_ecell_cnt, s->d_ecell_start, s->ecell_cap + 1,
-                                    nullptr)))
+                                    nullptr, s->d_scan_tmp)))
     return rc;
   cudaMemsetAsync(s->d_ecell_cnt, 0, sizeof(int32_t) * (s->ecell_cap + 1), st);
   k_cell_fill<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_ecell_of_atom, s->d_ecell_start,
                                                      s->d_ecell_cnt, s->d_ecell_atoms, s->N);
   k_cell_sort<<<tm_div_up(s->ecell_cap, 4), 128, 0, st>>>(s->d_ecell_start, s->d_ecell_atoms,
-                                                            s->d_encell, s->ecell_cap);
+                                                            s->d_sort_tmp, s->d_encell, s->ecell_cap);
   k_ee_pack<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_ecell_atoms, s->d_x, s->d_elem, s->d_mol,
                                                   s->d_egrid, s->d_ecell_of_atom, s->d_epos,
                                                   s->d_exhi, s->N);
@@ -1073,6 +1078,7 @@ struct StaticScratch {
   int32_t mol[TM_STATIC_MAX_ATOMS];
   int32_t cell_atoms[TM_STATIC_MAX_ATOMS];
   int32_t cell_of_atom[TM_STATIC_MAX_ATOMS];
+  int32_t sort_tmp[TM_STATIC_MAX_ATOMS];
   int32_t cell_cnt[TM_STATIC_MAX_CELLS + 1];
   int32_t cell_start[TM_STATIC_MAX_CELLS + 1];
   tm_grid grid;
@@ -1163,7 +1169,8 @@ extern "C" int tm_nlist_build_static(const double* x, const int32_t* elem, int n
   cudaMemsetAsync(S->cell_cnt, 0, sizeof(int32_t) * (cap + 1), st);
   k_cell_fill<<<tm_div_up(N, 256), 256, 0, st>>>(S->cell_of_atom, S->cell_start, S->cell_cnt,
                                                   S->cell_atoms, N);
-  k_cell_sort<<<tm_div_up(cap, 4), 128, 0, st>>>(S->cell_start, S->cell_atoms, &S->ncell, cap);
+  k_cell_sort<<<tm_div_up(cap, 4), 128, 0, st>>>(S->cell_start, S->cell_atoms, S->sort_tmp, &S->ncell,
+                                                 cap);
   NbrArgs a;
   a.x = x; a.xhi = S->xhi; a.xlo = S->xlo; a.mol = S->mol; a.elem = elem; a.grid = &S->grid;
   a.cell_of = S->cell_of_atom; a.cell_start = S->cell_start; a.cell_atoms = S->cell_atoms;
