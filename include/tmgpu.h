@@ -203,6 +203,7 @@ int tm_md_run(tm_md *md, int nsteps, double skin, double *log);
  */
 #define TM_SERVE_EF 0   /* energy + force at fixed positions          */
 #define TM_SERVE_MD 1   /* velocity-Verlet step (SimpleMD.py:14-38)   */
+#define TM_SERVE_OPT 2  /* one FIRE relaxation step (Bitzek et al. 2006) */
 int tm_serve_create(tm_model *m, int max_atoms, int max_mols, double dt_fs, tm_serve **out);
 int tm_serve_destroy(tm_serve *sv);
 int tm_serve_info(const tm_serve *sv, int *max_atoms, int *max_mols, int *natoms, int *nmol,
@@ -219,8 +220,13 @@ int tm_serve_info(const tm_serve *sv, int *max_atoms, int *max_mols, int *natoms
 int tm_serve_layout(tm_serve *sv, int nmol, const int32_t *Z, const int64_t *offsets,
                     const int32_t *mode, const int32_t *src, const double *x_new,
                     const double *v_new);
-/* One step of every molecule; E_out[nmol][4] (host, may be NULL) as tm_energy_force. */
-int tm_serve_step(tm_serve *sv, double *E_out);
+/*
+ * One step of every molecule; E_out[nmol][4] (host, may be NULL) as
+ * tm_energy_force; fmax_out[nmol] (host, may be NULL): the largest atomic
+ * force (J/mol/A) of each TM_SERVE_OPT molecule (0 for the others), for the
+ * caller's convergence test.
+ */
+int tm_serve_step(tm_serve *sv, double *E_out, double *fmax_out);
 /* Positions, velocities, forces (J/mol/A) of molecule mol to host (each may be NULL). */
 int tm_serve_read(tm_serve *sv, int mol, double *x, double *v, double *F);
 

@@ -22,7 +22,7 @@ TM_F_DEVICE_IO = 2
 TM_F_REUSE_NLIST = 4
 TM_F_REFERENCE_PERIODIC_FORCE = 8
 TM_MD = {"nve": 0, "nose": 1, "nhc": 2}
-TM_SERVE = {"ef": 0, "md": 1}
+TM_SERVE = {"ef": 0, "md": 1, "opt": 2}
 
 # every symbol include/tmgpu.h declares
 EXPORTS = [
@@ -105,7 +105,7 @@ def _declare(lib):
         "tm_serve_destroy": (I, [P]),
         "tm_serve_info": (I, [P, P, P, P, P, P]),
         "tm_serve_layout": (I, [P, I, P, P, P, P, P, P]),
-        "tm_serve_step": (I, [P, P]),
+        "tm_serve_step": (I, [P, P, P]),
         "tm_serve_read": (I, [P, I, P, P, P]),
     }
     for name, (res, args) in sig.items():

@@ -1,7 +1,9 @@
 """Continuous-batching serving loop over ``tm_serve`` (libtmgpu).
 
-Requests are energy+force evaluations ("ef", one step) or NVE molecular
-dynamics runs ("md", ``nsteps`` velocity-Verlet steps of SimpleMD.py:14-38).
+Requests are energy+force evaluations ("ef", one step), NVE molecular
+dynamics runs ("md", ``nsteps`` velocity-Verlet steps of SimpleMD.py:14-38) or
+geometry optimisations ("opt": FIRE steps until the largest atomic force is
+below ``fmax`` eV/A, at most ``nsteps``).
 Every request in flight is one molecule of a single device-resident batch, and
 one ``Server.step()`` advances all of them with one fused energy+force
 evaluation. Between steps, finished requests leave and waiting requests are
@@ -19,6 +21,7 @@ import time
 import numpy as np
 
 from . import _lib
+from .params import EV_PER_HARTREE, JOULEPERHARTREE
 
 _F64 = np.float64
 
@@ -33,15 +36,18 @@ class Request:
 
     _next = 0
 
-    def __init__(self, Z, x, kind="md", nsteps=50, v=None, arrival=0.0):
+    def __init__(self, Z, x, kind="md", nsteps=50, v=None, arrival=0.0, fmax=0.05):
         if kind not in _lib.TM_SERVE:
-            raise ValueError("kind must be 'ef' or 'md'")
+            raise ValueError("kind must be 'ef', 'md' or 'opt'")
         self.Z = np.ascontiguousarray(Z, dtype=np.int32)
         self.x0 = np.ascontiguousarray(x, dtype=_F64).reshape(-1, 3)
         self.v0 = (np.zeros_like(self.x0) if v is None
                    else np.ascontiguousarray(v, dtype=_F64).reshape(-1, 3))
         self.kind = kind
         self.nsteps = 1 if kind == "ef" else int(nsteps)
+        self.fmax = float(fmax)          # eV/A, optimisation requests
+        self.fmax_last = None
+        self.converged = False
         self.arrival = float(arrival)
         self.rid = Request._next
         Request._next += 1
@@ -56,7 +62,7 @@ class Request:
 
     @property
     def done(self):
-        return self.steps_done >= self.nsteps
+        return self.steps_done >= self.nsteps or self.converged
 
 
 class Server:
@@ -166,12 +172,17 @@ class Server:
         if not self.active:
             return 0
         E = np.zeros((len(self.active), 4))
-        self.ctx.check(self.lib.tm_serve_step(self.h, _p(E)))
+        fmax = np.zeros(len(self.active))
+        self.ctx.check(self.lib.tm_serve_step(self.h, _p(E), _p(fmax)))
         natoms = 0
         for q, r in enumerate(self.active):
             r.steps_done += 1
             r.energies.append(E[q].copy())
             natoms += r.natoms
+            if r.kind == "opt":
+                # the force of the positions just evaluated (the step's x)
+                r.fmax_last = fmax[q] / JOULEPERHARTREE * EV_PER_HARTREE
+                r.converged = r.fmax_last <= r.fmax
         for q, r in enumerate(self.active):
             if r.done:
                 r.x = np.empty((r.natoms, 3))

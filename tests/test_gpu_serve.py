@@ -115,3 +115,32 @@ def test_capacity_for_budget(env):
     srv = serve.Server(m, max_atoms=n, max_mols=64)
     assert srv.bytes <= (2 << 30) * 1.01
     srv.close()
+
+
+def test_optimisation_requests_relax_and_match_alone(env):
+    """FIRE optimisation requests next to MD and E+F requests: each reaches
+    fmax <= 0.05 eV/A (or its step limit) with a non-increasing trend of the
+    energy, and gives the same positions alone and in the mix."""
+    m, serve, _ = env
+    from tensormol_gb300 import systems as sy
+    rng = np.random.default_rng(5)
+    xo, Zo = sy.chno_molecule(rng, 12)
+    Zo = np.where(np.isin(Zo, [1, 8]), Zo, 8).astype(np.int32)   # the water model's H and O
+    O = serve.Request(Zo, xo, kind="opt", nsteps=400, fmax=0.05)
+    A = _req(serve, 10, 1, "md", 30)
+    C = _req(serve, 20, 3, "ef")
+    srv = serve.Server(m, max_atoms=2048, max_mols=8)
+    for r in (A, O, C):
+        srv.submit(r)
+    srv.drain()
+    srv.close()
+    assert O.done and (O.converged or O.steps_done == O.nsteps)
+    e = np.array([x[0] for x in O.energies])
+    assert e[-1] < e[0]
+    alone = serve.Request(Zo, xo, kind="opt", nsteps=400, fmax=0.05)
+    s1 = serve.Server(m, max_atoms=1024, max_mols=2)
+    s1.submit(alone)
+    s1.drain()
+    s1.close()
+    assert alone.steps_done == O.steps_done
+    assert np.array_equal(alone.x, O.x)

@@ -55,7 +55,7 @@ class _FakeLib:
         self.mode = _arr(mode, ctypes.c_int32, nmol).copy()
         return 0
 
-    def tm_serve_step(self, h, E):
+    def tm_serve_step(self, h, E, fmax=None):
         E = _arr(E, ctypes.c_double, 4 * len(self.mode)).reshape(-1, 4)
         for q, md in enumerate(self.mode):
             a, b = self.offs[q], self.offs[q + 1]
