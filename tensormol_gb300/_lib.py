@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(HERE, "libtmgpu.so")
 TM_OK = 0
 ERRORS = {1: "TM_E_ARG", 2: "TM_E_CUDA", 3: "TM_E_CAPACITY", 4: "TM_E_NONFINITE",
           5: "TM_E_BUDGET", 6: "TM_E_TIMEOUT", 7: "TM_E_STATE", 8: "TM_E_UNSUPPORTED"}
+ERROR_CODES = {name: code for code, name in ERRORS.items()}
 
 TM_ACT = {"relu": 0, "sigmoid_with_param": 1, "softplus": 2, "tanh": 3, "elu": 4}
 TM_PREC = {"fp32": 0, "bf16": 1}

@@ -12,8 +12,8 @@
 // Gumbsch, Phys. Rev. Lett. 97, 170201 (2006)): semi-implicit Euler steps with
 // the mixing v <- (1 - alpha) v + alpha |v| F/|F|, the step growing (x1.1, up
 // to 8 dt) and alpha shrinking (x0.99) after 5 downhill steps, and v = 0,
-// step x0.5, alpha = 0.1 when F.v < 0; per-molecule sums are two-level and
-// deterministic.
+// step x0.5, alpha = 0.1 when F.v < 0; no atom moves more than 0.2 A in a
+// step; per-molecule sums are two-level and deterministic.
 // Molecules are independent in every kernel (per-molecule cell grids, element
 // rows that never mix atoms within a row, per-molecule chunked reductions), so
 // a request's results do not depend on what else is in the batch.
@@ -53,6 +53,7 @@ namespace {
 constexpr double kFireAlpha0 = 0.1;
 constexpr int kFireNmin = 5;
 constexpr double kFireDtMax = 8.0;   // largest FIRE step, in units of the serving dt
+constexpr double kFireMaxMove = 0.2; // A per atom and step
 
 __constant__ double c_mass_amu[11] = {0, 1.00794, 4.002602, 6.941, 9.012182, 10.811, 12.0107,
                                       14.0067, 15.9994, 18.9984032, 20.1791};
@@ -217,7 +218,16 @@ __global__ void k_fire_move(double* __restrict__ x, const double* __restrict__ v
   const int q = mol[i];
   if (mode[q] != TM_SERVE_OPT) return;
   const double dt = f[2 * q];
-  for (int d = 0; d < 3; ++d) x[3 * i + d] += dt * v[3 * i + d];
+  double st[3], n2 = 0.0;
+  for (int d = 0; d < 3; ++d) {
+    st[d] = dt * v[3 * i + d];
+    n2 += st[d] * st[d];
+  }
+  // no atom moves more than kFireMaxMove per step (the usual FIRE safeguard)
+  const double c = !isfinite(n2) ? 0.0
+                   : (n2 > kFireMaxMove * kFireMaxMove ? kFireMaxMove / sqrt(n2) : 1.0);
+  if (c == 0.0) return;   // a non-finite step leaves the atom where it is
+  for (int d = 0; d < 3; ++d) x[3 * i + d] += c * st[d];
 }
 
 }  // namespace

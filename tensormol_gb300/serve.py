@@ -48,6 +48,7 @@ class Request:
         self.fmax = float(fmax)          # eV/A, optimisation requests
         self.fmax_last = None
         self.converged = False
+        self.error = None                # set when the request had to be dropped
         self.arrival = float(arrival)
         self.rid = Request._next
         Request._next += 1
@@ -62,7 +63,7 @@ class Request:
 
     @property
     def done(self):
-        return self.steps_done >= self.nsteps or self.converged
+        return self.steps_done >= self.nsteps or self.converged or self.error is not None
 
 
 class Server:
@@ -87,6 +88,7 @@ class Server:
         self.finished = []
         self.step_ms = []         # wall time of each step (admission + layout + step)
         self.step_atoms = []
+        self.step_info = []       # (relayout?, layout ms, step ms, atoms) per step
         self.atom_steps = 0
 
     @staticmethod
@@ -165,15 +167,28 @@ class Server:
         t0 = time.perf_counter()
         keep = [r for r in self.active if not r.done]
         admit = self._admit(keep)
-        if admit or len(keep) != len(self.active):
+        relayout = bool(admit or len(keep) != len(self.active))
+        if relayout:
             self._relayout(keep, admit)
             for r in admit:
                 r.t_admit = t0
+        t1 = time.perf_counter()
         if not self.active:
             return 0
         E = np.zeros((len(self.active), 4))
         fmax = np.zeros(len(self.active))
-        self.ctx.check(self.lib.tm_serve_step(self.h, _p(E), _p(fmax)))
+        try:
+            self.ctx.check(self.lib.tm_serve_step(self.h, _p(E), _p(fmax)))
+        except _lib.TmError as exc:
+            # non-finite positions belong to one request (molecules never
+            # interact): drop those requests, the others' step is valid
+            if exc.code != _lib.ERROR_CODES["TM_E_NONFINITE"]:
+                raise
+            for q, r in enumerate(self.active):
+                x = np.empty((r.natoms, 3))
+                self.ctx.check(self.lib.tm_serve_read(self.h, q, _p(x), None, None))
+                if not np.all(np.isfinite(x)):
+                    r.error = "non-finite positions"
         natoms = 0
         for q, r in enumerate(self.active):
             r.steps_done += 1
@@ -191,7 +206,9 @@ class Server:
                 self.ctx.check(self.lib.tm_serve_read(self.h, q, _p(r.x), _p(r.v), _p(r.F)))
                 r.t_done = time.perf_counter()
                 self.finished.append(r)
-        self.step_ms.append((time.perf_counter() - t0) * 1e3)
+        t2 = time.perf_counter()
+        self.step_ms.append((t2 - t0) * 1e3)
+        self.step_info.append((relayout, (t1 - t0) * 1e3, (t2 - t1) * 1e3, natoms))
         self.step_atoms.append(natoms)
         self.atom_steps += natoms
         return len(self.active)
