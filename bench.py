@@ -281,8 +281,8 @@ def serve_requests(specs):
 def time_md(model_fp32, torch):
     """The MD workloads: (1) the 60-atom cluster, one E+F then 100 NVE steps of
     0.5 fs; (2) the 12,288-atom periodic box (49.7 A), 1,000 Nose-Hoover-chain
-    (length 3) steps at 300 K, dt 0.5 fs, BF16 networks, with an FP32-network
-    run of the same steps beside it. Device-resident integrators (FP64 state);
+    (length 3) steps at 300 K, dt 0.5 fs, BF16 networks, 1.0 A neighbour skin,
+    with an FP32-network run of the same steps beside it. Device-resident integrators (FP64 state);
     time from CUDA events on the library stream; drift = slope of the
     conserved quantity (least squares over the run)."""
     from tensormol_gb300 import md, systems
@@ -334,8 +334,8 @@ def time_md(model_fp32, torch):
         s = m.system(x0, box.Z, None, lat)
         dyn = md.DeviceMD(s, "nhc", dt=0.5, T=300.0, chain=3)
         dyn.set_velocities(v0)
-        dyn.run(3)
-        log, ms = timed(lambda: dyn.run(1000))
+        dyn.run(3, skin=1.0)
+        log, ms = timed(lambda: dyn.run(1000, skin=1.0))
         t_ns = 0.5e-6 * np.arange(1000)
         slope = np.polyfit(t_ns, log[:, 2], 1)[0]                 # J/mol per ns
         res[prec] = {"ms_per_step": ms / 1000, "atom_steps_per_s": box.natoms * 1000 / (ms * 1e-3),
@@ -346,7 +346,8 @@ def time_md(model_fp32, torch):
         s.close()
         m.close()
     out["waterbox12288_nhc3_1000"] = res
-    out["note"] = ("neighbour lists are rebuilt exactly every step (no skin); drift is the "
+    out["note"] = ("periodic box: 1.0 A skin lists (candidates rebuilt on displacement, exact "
+                   "rows filtered every step); 60-atom cluster: a full build every step; drift is the "
                    "least-squares slope of the extended-system conserved energy over the run; "
                    "the periodic-box networks have their output layers scaled by 0.01 so that "
                    "the random-init potential does not collapse the box")

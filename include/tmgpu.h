@@ -184,10 +184,13 @@ int tm_md_destroy(tm_md *md);
 int tm_md_set_velocities(tm_md *md, const double *v, int on_device);
 int tm_md_get_velocities(tm_md *md, double *v, int on_device);
 /*
- * nsteps integrator steps, each with one energy+force evaluation and a fresh
- * neighbour-list build (the reference builds its lists on every call,
- * TFMolManage.py:1418-1431). skin is reserved and must be 0 or positive; it is
- * not used. log[nsteps][4] (host, may be NULL) =
+ * nsteps integrator steps, each with one energy+force evaluation on exact
+ * neighbour rows (the reference builds its lists on every call,
+ * TFMolManage.py:1418-1431). skin = 0: a full build every step. skin > 0 (A):
+ * candidates within the cutoffs + skin are built when atoms may have moved
+ * skin/2 (checked on the device, chunks replayed if exceeded) and filtered to
+ * the exact rows every step; periodic positions are wrapped into the cell at
+ * candidate builds and at the end. log[nsteps][4] (host, may be NULL) =
  * (potential Hartree, kinetic J/mol per atom, conserved J/mol, T_eff K).
  */
 int tm_md_run(tm_md *md, int nsteps, double skin, double *log);

@@ -552,6 +552,10 @@ static int system_alloc(tm_system* s, int N_cap, int nmol_cap, int Mpad_cap, int
   A.get(&s->d_cell_of_atom, sizeof(int32_t) * N);
   A.get(&s->d_sort_tmp, sizeof(int32_t) * N);
   A.get(&s->d_scan_tmp, sizeof(int32_t) * 4096);
+  A.get(&s->d_ccnt, sizeof(int32_t) * N);
+  A.get(&s->d_cand, sizeof(uint32_t) * (size_t)N * s->KC);
+  A.get(&s->d_need_c, sizeof(int32_t) * 2);
+  A.get(&s->d_disp, sizeof(unsigned long long));
   A.get(&s->d_chunk, sizeof(int2) * nchunk_cap);
   A.get(&s->d_mol_chunk, sizeof(int32_t) * (nmol + 1));
   A.get(&s->d_part, sizeof(double) * 8 * nchunk_cap);
@@ -700,7 +704,7 @@ static void system_free(tm_system* s) {
                   s->d_off, s->d_x, s->d_xhi, s->d_xlo, s->d_x_at_build, s->d_grid, s->d_ncell, s->d_ncell_m, s->d_need,
                   s->d_chunk, s->d_mol_chunk, s->d_part, s->d_cbox,
                   s->d_egrid, s->d_encell, s->d_encell_m, s->d_ecell_cnt, s->d_ecell_start,
-                  s->d_ecell_atoms, s->d_ecell_of_atom, s->d_epos, s->d_exhi, s->d_exlo, s->d_sort_tmp, s->d_scan_tmp,
+                  s->d_ecell_atoms, s->d_ecell_of_atom, s->d_epos, s->d_exhi, s->d_exlo, s->d_sort_tmp, s->d_scan_tmp, s->d_ccnt, s->d_cand, s->d_need_c, s->d_disp,
                   s->d_cpart,
                   s->d_cell_cnt, s->d_cell_start, s->d_cell_atoms, s->d_cell_of_atom, s->d_cnt_r,
                   s->d_cnt_a, s->d_nbr_r, s->d_nbr_a, s->d_rev_r, s->d_rev_a, s->d_sr, s->d_va,
@@ -824,7 +828,9 @@ static int energy_force_pipeline(tm_system* s, unsigned flags, cudaEvent_t* ev) 
   cudaStream_t st = s->ctx->stream;
   const bool force = !(flags & TM_F_ENERGY_ONLY);
   if (ev) cudaEventRecord(ev[0], st);
-  if (!(flags & TM_F_REUSE_NLIST) || !s->nlist_valid) {
+  if (s->skin > 0.0 && s->cand_valid && !s->cand_rebuild) {
+    if ((rc = tm_launch_nlist_filter(s))) return rc;      // exact rows from the candidates
+  } else if (!(flags & TM_F_REUSE_NLIST) || !s->nlist_valid) {
     if ((rc = tm_launch_nlist(s))) return rc;
   } else {
     if ((rc = tm_launch_positions(s))) return rc;

@@ -111,6 +111,8 @@ struct CoulArgs {
   int periodic;
   double ree;
   float ree2, ree2_lo, ree2_hi;
+  double reach;             // cell search radius: cutoff + skin (cells from an earlier build)
+  float reach2;
   float inv_bohr, inv_b2, inv_vdw_width, c_lin;   // 1/bohr, 1/bohr^2, 1/width, zz/R_lr + yy
   double lat[9];
   float sh_hi[27][3];
@@ -261,9 +263,9 @@ __global__ void __launch_bounds__(128, 4) k_coulomb(const CoulArgs a, const tm_c
   const int iz = lc % g.nz, iy = (lc / g.nz) % g.ny, ix = lc / (g.nz * g.ny);
   const float cx = (float)g.cx, cy = (float)g.cy, cz = (float)g.cz;
   // periodic: at most one wrap per axis (R <= n; edges are >= 2 * cutoff)
-  const int Rx = a.periodic ? min((int)ceil(a.ree / g.cx), g.nx) : (int)ceil(a.ree / g.cx);
-  const int Ry = a.periodic ? min((int)ceil(a.ree / g.cy), g.ny) : (int)ceil(a.ree / g.cy);
-  const int Rz = a.periodic ? min((int)ceil(a.ree / g.cz), g.nz) : (int)ceil(a.ree / g.cz);
+  const int Rx = a.periodic ? min((int)ceil(a.reach / g.cx), g.nx) : (int)ceil(a.reach / g.cx);
+  const int Ry = a.periodic ? min((int)ceil(a.reach / g.cy), g.ny) : (int)ceil(a.reach / g.cy);
+  const int Rz = a.periodic ? min((int)ceil(a.reach / g.cz), g.nz) : (int)ceil(a.reach / g.cz);
   StageSmem& st = stage[wib];
   for (int ib = t0; ib < t1; ib += 32) {
     const int ti = ib + lane;
@@ -284,7 +286,7 @@ __global__ void __launch_bounds__(128, 4) k_coulomb(const CoulArgs a, const tm_c
       int n = 0;   // staged candidates
       for (int oz = -Rz; oz <= Rz; ++oz) {
         const float gapz = fmaxf(0.f, (float)(abs(oz) - 1)) * cz;
-        if (gapx * gapx + gapy * gapy + gapz * gapz > a.ree2_hi) continue;
+        if (gapx * gapx + gapy * gapy + gapz * gapz > a.reach2) continue;
         int jx = ix + ox, jy = iy + oy, jz = iz + oz, sx = 0, sy = 0, sz = 0;
         if (a.periodic) {
           if (jx < 0) { jx += g.nx; sx = -1; } else if (jx >= g.nx) { jx -= g.nx; sx = 1; }
@@ -430,6 +432,8 @@ int tm_launch_coulomb(tm_system* s, unsigned flags) {
   a.ree2 = (float)(k.ree_d * k.ree_d);
   a.ree2_lo = a.ree2 * (1.f - kBand);
   a.ree2_hi = a.ree2 * (1.f + kBand);
+  a.reach = k.ree_d + s->skin;
+  a.reach2 = (float)(a.reach * a.reach) * (1.f + kBand);
   a.inv_bohr = (float)(1.0 / (double)k.bohr);
   a.inv_b2 = (float)(1.0 / ((double)k.bohr * (double)k.bohr));
   a.inv_vdw_width = (float)(1.0 / (double)k.vdw_width);

@@ -149,6 +149,16 @@ struct tm_system {
   int32_t* d_rev_a = nullptr;
   bool nlist_valid = false;
   bool need_sticky = false;            // keep the overflow counters across builds (MD chunks)
+  // skin lists (MD): candidates within cutoff + skin, rebuilt when asked;
+  // every step filters them with the exact membership rule
+  double skin = 0.0;                   // 0: a full build every step
+  bool cand_valid = false;
+  bool cand_rebuild = true;            // the next build rebuilds the candidates
+  int KC = 128;                        // candidate row capacity
+  int32_t* d_ccnt = nullptr;           // [N] candidates per centre
+  uint32_t* d_cand = nullptr;          // [N*KC] packed (img << 27 | atom), sorted like the rows
+  int32_t* d_need_c = nullptr;         // [2] largest candidate count seen (on overflow)
+  unsigned long long* d_disp = nullptr;  // squared displacement since the candidate build (bits)
   // descriptors + networks
   void* G[2] = {};                     // [Mpad][Dp] hi/lo (tf32) or bf16 (G[0])
   void* H1[2] = {};                    // [2*Mpad][H] per net stacked
@@ -195,6 +205,7 @@ int tm_energy_force_device(tm_system* s, unsigned flags);
 // tm_nlist.cu
 int tm_launch_positions(tm_system* s);
 int tm_launch_nlist(tm_system* s);
+int tm_launch_nlist_filter(tm_system* s);   // skin lists: filter the candidates
 int tm_nlist_grow(tm_system* s, bool* grew);
 int tm_launch_export_nlist(tm_system* s, int64_t* radp, int64_t* angt, int64_t* mil_j,
                            int64_t* mil_jk, int64_t P, int64_t T);

@@ -14,6 +14,7 @@
 // two-level and deterministic, thermostat scalars live in device memory.
 #include <cuda_runtime.h>
 #include <math.h>
+#include <string.h>
 
 #include <vector>
 
@@ -341,11 +342,15 @@ static int md_step(tm_md* md, double* dlog, int* dstep) {
   const int gb = tm_div_up(n3, 256);
   const double dt = md->dt;
   const unsigned flags = 0;
+  // periodic positions go back into the cell at every full list build; with
+  // skin lists they stay continuous between candidate builds (a candidate's
+  // image code refers to the positions it was built from)
+  const bool wrap = s->periodic && !(s->skin > 0.0 && s->cand_valid && !s->cand_rebuild);
   int rc;
   if (md->kind == TM_MD_NVE) {
     k_vv_pos<<<gb, 256, 0, st>>>(s->d_x, md->v, md->a, dt, n3);
     ctx->launches++;
-    if (s->periodic) { k_wrap<<<tm_div_up(N, 256), 256, 0, st>>>(s->d_x, s->lat[0], s->lat[4], s->lat[8], N); ctx->launches++; }
+    if (wrap) { k_wrap<<<tm_div_up(N, 256), 256, 0, st>>>(s->d_x, s->lat[0], s->lat[4], s->lat[8], N); ctx->launches++; }
     if ((rc = tm_energy_force_device(s, flags))) return rc;
     k_vv_vel<<<gb, 256, 0, st>>>(md->v, md->a, s->d_F, md->m, dt, n3);
     ctx->launches++;
@@ -354,7 +359,7 @@ static int md_step(tm_md* md, double* dlog, int* dstep) {
     ke_into(md, md->v, S_KE2);
     k_nose_pos<<<gb, 256, 0, st>>>(s->d_x, md->v, md->a, md->vh, md->sc, dt, n3);
     ctx->launches++;
-    if (s->periodic) { k_wrap<<<tm_div_up(N, 256), 256, 0, st>>>(s->d_x, s->lat[0], s->lat[4], s->lat[8], N); ctx->launches++; }
+    if (wrap) { k_wrap<<<tm_div_up(N, 256), 256, 0, st>>>(s->d_x, s->lat[0], s->lat[4], s->lat[8], N); ctx->launches++; }
     ke_into(md, md->vh, S_KE2B);
     if ((rc = tm_energy_force_device(s, flags))) return rc;
     k_nose_eta<<<1, 1, 0, st>>>(md->sc, md->Qnose, md->kT, (double)N, dt);
@@ -368,7 +373,7 @@ static int md_step(tm_md* md, double* dlog, int* dstep) {
     k_kick<<<gb, 256, 0, st>>>(md->v, md->a, 0.5 * dt, n3);
     k_drift<<<gb, 256, 0, st>>>(s->d_x, md->v, dt, n3);
     ctx->launches += 4;
-    if (s->periodic) { k_wrap<<<tm_div_up(N, 256), 256, 0, st>>>(s->d_x, s->lat[0], s->lat[4], s->lat[8], N); ctx->launches++; }
+    if (wrap) { k_wrap<<<tm_div_up(N, 256), 256, 0, st>>>(s->d_x, s->lat[0], s->lat[4], s->lat[8], N); ctx->launches++; }
     if ((rc = tm_energy_force_device(s, flags))) return rc;
     k_accel<<<gb, 256, 0, st>>>(md->a, s->d_F, md->m, n3);
     k_kick<<<gb, 256, 0, st>>>(md->v, md->a, 0.5 * dt, n3);
@@ -385,16 +390,21 @@ static int md_step(tm_md* md, double* dlog, int* dstep) {
   return TM_OK;
 }
 
-// Steps run in chunks of kChunk. Each chunk starts from a device-side copy of
-// the state (positions, velocities, accelerations, thermostat scalars); the
+// Steps run in chunks. Each chunk starts from a device-side copy of the state
+// (positions, velocities, accelerations, thermostat scalars); the
 // neighbour-row overflow counters stay armed across the chunk's list builds.
 // If any build of the chunk overflowed its rows, the rows are grown and the
 // chunk is run again from the copy, so a run never keeps a force computed
 // from a truncated row. One host synchronisation per chunk. Within a chunk the
-// launch sequence of one step (about 45 kernels) is captured once into a CUDA
-// graph and replayed; it is captured again after the rows grow (new buffers).
+// launch sequence of one step is captured once into a CUDA graph and replayed;
+// it is captured again after buffers are replaced.
+// skin > 0: the first step of every chunk builds candidate lists within the
+// cutoffs + skin and the other steps filter them (exact rows every step). The
+// chunk length adapts so that no atom moves more than skin/2 within a chunk
+// (judged from the largest displacement seen in the previous chunk); a chunk
+// that exceeded it anyway is run again from its copy, shorter.
 extern "C" int tm_md_run(tm_md* md, int nsteps, double skin, double* log) {
-  if (!md || nsteps < 0 || skin < 0) return TM_E_ARG;
+  if (!md || nsteps < 0 || !(skin >= 0)) return TM_E_ARG;
   tm_system* s = md->s;
   tm_ctx* ctx = s->ctx;
   cudaStream_t st = ctx->stream;
@@ -409,60 +419,100 @@ extern "C" int tm_md_run(tm_md* md, int nsteps, double skin, double* log) {
       (rc = tm_alloc(ctx, (void**)&dstep, sizeof(int))))
     return rc;
   s->need_sticky = true;
-  // the first step runs uncaptured: it builds what later steps reuse (lists
-  // grown to fit, one-time function attributes) and checks that a step works
+  s->skin = skin;
+  s->cand_valid = false;
   cudaGraphExec_t exec = nullptr;
   int64_t launches_per_step = 0;
   int start = 0, retries = 0;
+  int chunk = skin > 0.0 ? 8 : kChunk;
   while (!rc && start < nsteps) {
-    const int n = nsteps - start < kChunk ? nsteps - start : kChunk;
+    const int n = nsteps - start < chunk ? nsteps - start : chunk;
     cudaMemcpyAsync(md->ck_x, s->d_x, n3b, cudaMemcpyDeviceToDevice, st);
     cudaMemcpyAsync(md->ck_v, md->v, n3b, cudaMemcpyDeviceToDevice, st);
     cudaMemcpyAsync(md->ck_a, md->a, n3b, cudaMemcpyDeviceToDevice, st);
     cudaMemcpyAsync(md->ck_sc, md->sc, nsc, cudaMemcpyDeviceToDevice, st);
     cudaMemsetAsync(s->d_need, 0, sizeof(int32_t) * 2, st);
+    cudaMemsetAsync(s->d_need_c, 0, sizeof(int32_t) * 2, st);
     cudaMemcpyAsync(dstep, &start, sizeof(int), cudaMemcpyHostToDevice, st);
-    int q = 0;
-    if (!exec) {                                   // plain first step of the chunk
-      const int64_t l0 = ctx->launches;
-      rc = md_step(md, dlog, dstep);
-      launches_per_step = ctx->launches - l0;
-      q = 1;
-      if (!rc && q < n) {
-        cudaGraph_t graph = nullptr;
-        cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
-        if (e == cudaSuccess) {
-          const int64_t l1 = ctx->launches;
-          rc = md_step(md, dlog, dstep);
-          ctx->launches = l1;
-          e = cudaStreamEndCapture(st, &graph);
-          if (!rc && e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
-          if (graph) cudaGraphDestroy(graph);
-        }
-        if (!rc && e != cudaSuccess) rc = tm_cuda_check(ctx, e, "md step graph");
+    // first step of the chunk, uncaptured: a full build (candidates when skin > 0)
+    s->cand_rebuild = true;
+    const int64_t l0 = ctx->launches;
+    rc = md_step(md, dlog, dstep);
+    const int64_t first_launches = ctx->launches - l0;
+    int q = 1;
+    if (!rc && !exec && q < n) {
+      cudaGraph_t graph = nullptr;
+      cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) {
+        const int64_t l1 = ctx->launches;
+        rc = md_step(md, dlog, dstep);
+        launches_per_step = ctx->launches - l1;
+        ctx->launches = l1;
+        e = cudaStreamEndCapture(st, &graph);
+        if (!rc && e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
       }
+      if (!rc && e != cudaSuccess) rc = tm_cuda_check(ctx, e, "md step graph");
     }
+    (void)first_launches;
     for (; q < n && !rc; ++q) {
       rc = tm_cuda_check(ctx, cudaGraphLaunch(exec, st), "md step replay");
       ctx->launches += launches_per_step;
     }
     if (rc) break;
+    unsigned long long disp_bits = 0;
+    int32_t need_c[2] = {0, 0};
+    if (skin > 0.0) {
+      cudaMemcpyAsync(&disp_bits, s->d_disp, sizeof(disp_bits), cudaMemcpyDeviceToHost, st);
+      cudaMemcpyAsync(need_c, s->d_need_c, sizeof(need_c), cudaMemcpyDeviceToHost, st);
+    }
     bool grew = false;
     if ((rc = tm_nlist_grow(s, &grew))) break;          // synchronises the stream
     if ((rc = tm_sync_status(ctx, "md chunk"))) break;  // a device error ends the run
-    if (grew) {
-      if (++retries > 8) { rc = tm_fail(ctx, TM_E_CAPACITY, "neighbour rows keep overflowing"); break; }
+    double disp = 0.0;
+    memcpy(&disp, &disp_bits, sizeof(disp));
+    disp = sqrt(disp);
+    bool replay = grew;
+    if (skin > 0.0 && need_c[0] > s->KC) {              // candidate rows too short
+      const int KC = ((need_c[0] + 31) / 32) * 32;
+      tm_free(ctx, s->d_cand, sizeof(uint32_t) * (size_t)s->N_cap * s->KC);
+      s->bytes -= sizeof(uint32_t) * (size_t)s->N_cap * s->KC;
+      s->KC = KC;
+      if ((rc = tm_alloc(ctx, (void**)&s->d_cand, sizeof(uint32_t) * (size_t)s->N_cap * KC))) break;
+      s->bytes += sizeof(uint32_t) * (size_t)s->N_cap * KC;
+      replay = true;
+    }
+    if (skin > 0.0 && disp > 0.5 * skin) {               // moved too far for the candidates
+      chunk = chunk > 1 ? chunk / 2 : 1;
+      replay = true;
+    }
+    if (replay) {
+      if (++retries > 16) { rc = tm_fail(ctx, TM_E_CAPACITY, "MD chunk cannot be completed"); break; }
       cudaMemcpyAsync(s->d_x, md->ck_x, n3b, cudaMemcpyDeviceToDevice, st);
       cudaMemcpyAsync(md->v, md->ck_v, n3b, cudaMemcpyDeviceToDevice, st);
       cudaMemcpyAsync(md->a, md->ck_a, n3b, cudaMemcpyDeviceToDevice, st);
       cudaMemcpyAsync(md->sc, md->ck_sc, nsc, cudaMemcpyDeviceToDevice, st);
-      if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }   // buffers were replaced
+      if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }   // buffers may be new
       continue;                                          // the same chunk again
+    }
+    if (skin > 0.0) {
+      // the next chunk: as long as the last one's displacement, scaled, allows
+      const double per_step = disp / (n > 1 ? n - 1 : 1);
+      int next = per_step > 0 ? (int)floor(0.5 * skin / (1.3 * per_step)) + 1 : kChunk;
+      chunk = next < 1 ? 1 : (next > kChunk ? kChunk : next);
     }
     start += n;
   }
   if (exec) cudaGraphExecDestroy(exec);
+  if (!rc && s->periodic && skin > 0.0) {   // hand back positions inside the cell
+    k_wrap<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_x, s->lat[0], s->lat[4], s->lat[8], s->N);
+    ctx->launches++;
+  }
   s->need_sticky = false;
+  s->skin = 0.0;
+  s->cand_valid = false;
+  s->cand_rebuild = true;
+  s->nlist_valid = false;
   if (!rc && log)
     rc = tm_cuda_check(ctx, cudaMemcpyAsync(log, dlog, sizeof(double) * 4 * nsteps, cudaMemcpyDeviceToHost, st), "md log");
   tm_free(ctx, dlog, sizeof(double) * 4 * nsteps);

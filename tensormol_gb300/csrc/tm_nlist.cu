@@ -18,6 +18,8 @@
 
 #include "tm_internal.h"
 
+void tm_fill_shifts(const tm_system* s, float hi[27][3], float lo[27][3]);   // tm_desc.cu
+
 namespace {
 
 constexpr float kBand = 1e-5f;   // relative band on d^2 settled in FP64
@@ -818,6 +820,118 @@ NbrArgs make_nbr_args(tm_system* s, int32_t* need) {
   return a;
 }
 
+// Exact rows from the candidate rows: the same FP32 screen + FP64 membership
+// rule as k_nbr_build, applied to each candidate in its (sorted) order, so
+// the rows equal a fresh build as long as no atom has moved more than half the
+// skin since the candidates were built. Also records the largest squared
+// displacement since then (as the bits of a non-negative double).
+struct FiltArgs {
+  const double* x;
+  const double* x0;         // positions at the candidate build
+  const float4* xhi;
+  const float4* xlo;
+  const uint32_t* cand;
+  const int32_t* ccnt;
+  int32_t* cnt_r;
+  int32_t* cnt_a;
+  uint32_t* nbr_r;
+  uint32_t* nbr_a;
+  int32_t* need;
+  unsigned long long* disp;
+  int N, KC, KR, KA, periodic;
+  double rr, ra;
+  float rr2_lo, rr2_hi, ra2_lo, ra2_hi;
+  double lat[9];
+  float sh_hi[27][3], sh_lo[27][3];
+};
+
+__global__ void __launch_bounds__(128) k_nbr_filter(const FiltArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (i >= a.N) return;
+  const float4 hi = a.xhi[i], lo = a.xlo[i];
+  const double xi = a.x[3 * i], yi = a.x[3 * i + 1], zi = a.x[3 * i + 2];
+  const int cc = a.ccnt[i];
+  int nr = 0, na = 0;
+  for (int base = 0; base < cc; base += 32) {
+    const int t = base + lane;
+    bool in_r = false, in_a = false;
+    uint32_t e = 0;
+    if (t < cc) {
+      e = a.cand[(size_t)i * a.KC + t];
+      const int j = (int)tm_atom(e), r = tm_img(e);
+      const float4 hj = a.xhi[j], lj = a.xlo[j];
+      const float dx = ds_sub_shift(hi.x, lo.x, hj.x, lj.x, a.sh_hi[r][0], a.sh_lo[r][0]);
+      const float dy = ds_sub_shift(hi.y, lo.y, hj.y, lj.y, a.sh_hi[r][1], a.sh_lo[r][1]);
+      const float dz = ds_sub_shift(hi.z, lo.z, hj.z, lj.z, a.sh_hi[r][2], a.sh_lo[r][2]);
+      const float d2 = dx * dx + dy * dy + dz * dz;
+      if (d2 <= a.rr2_hi) {
+        double xj = a.x[3 * j], yj = a.x[3 * j + 1], zj = a.x[3 * j + 2];
+        if (a.periodic) {
+          int sx, sy, sz;
+          tm_img_ijk(r, sx, sy, sz);
+          xj = tm_image_coord(xj, sx, sy, sz, a.lat[0], a.lat[3], a.lat[6]);
+          yj = tm_image_coord(yj, sx, sy, sz, a.lat[1], a.lat[4], a.lat[7]);
+          zj = tm_image_coord(zj, sx, sy, sz, a.lat[2], a.lat[5], a.lat[8]);
+        }
+        in_r = d2 < a.rr2_lo ? true : tm_exact_within(xi, yi, zi, xj, yj, zj, a.rr);
+        if (in_r) in_a = d2 < a.ra2_lo ? true
+                         : (d2 <= a.ra2_hi ? tm_exact_within(xi, yi, zi, xj, yj, zj, a.ra) : false);
+      }
+    }
+    const unsigned mr = __ballot_sync(TM_FULL, in_r);
+    const unsigned ma = __ballot_sync(TM_FULL, in_a);
+    if (in_r) {
+      const int p = nr + __popc(mr & lanemask_lt());
+      if (p < a.KR) a.nbr_r[(size_t)i * a.KR + p] = e;
+    }
+    if (in_a) {
+      const int p = na + __popc(ma & lanemask_lt());
+      if (p < a.KA) a.nbr_a[(size_t)i * a.KA + p] = e;
+    }
+    nr += __popc(mr);
+    na += __popc(ma);
+  }
+  if (lane == 0) {
+    if (nr > a.KR || na > a.KA) {
+      atomicMax(&a.need[0], nr);
+      atomicMax(&a.need[1], na);
+    }
+    a.cnt_r[i] = min(nr, a.KR);
+    a.cnt_a[i] = min(na, a.KA);
+    double d2 = 0.0;
+    for (int d = 0; d < 3; ++d) {
+      double u = a.x[3 * i + d] - a.x0[3 * i + d];
+      if (a.periodic) {   // wrapped into the cell since the build: nearest image
+        const double L = a.lat[4 * d];
+        u -= L * rint(u / L);
+      }
+      d2 += u * u;
+    }
+    atomicMax(a.disp, (unsigned long long)__double_as_longlong(d2));
+  }
+}
+
+int launch_filter(tm_system* s) {
+  tm_ctx* ctx = s->ctx;
+  const tm_consts& k = s->model->k;
+  FiltArgs a;
+  a.x = s->d_x; a.x0 = s->d_x_at_build; a.xhi = s->d_xhi; a.xlo = s->d_xlo;
+  a.cand = s->d_cand; a.ccnt = s->d_ccnt; a.cnt_r = s->d_cnt_r; a.cnt_a = s->d_cnt_a;
+  a.nbr_r = s->d_nbr_r; a.nbr_a = s->d_nbr_a; a.need = s->d_need; a.disp = s->d_disp;
+  a.N = s->N; a.KC = s->KC; a.KR = s->KR; a.KA = s->KA; a.periodic = s->periodic ? 1 : 0;
+  a.rr = k.r_rc_d; a.ra = k.a_rc_d;
+  a.rr2_lo = (float)(k.r_rc_d * k.r_rc_d) * (1.f - kBand);
+  a.rr2_hi = (float)(k.r_rc_d * k.r_rc_d) * (1.f + kBand);
+  a.ra2_lo = (float)(k.a_rc_d * k.a_rc_d) * (1.f - kBand);
+  a.ra2_hi = (float)(k.a_rc_d * k.a_rc_d) * (1.f + kBand);
+  for (int q = 0; q < 9; ++q) a.lat[q] = s->lat[q];
+  tm_fill_shifts(s, a.sh_hi, a.sh_lo);
+  k_nbr_filter<<<tm_div_up(s->N, 4), 128, 0, ctx->stream>>>(a);
+  ctx->launches++;
+  return tm_cuda_check(ctx, cudaGetLastError(), "filter");
+}
+
 }  // namespace
 
 int tm_launch_positions(tm_system* s) {
@@ -840,7 +954,7 @@ int tm_launch_nlist(tm_system* s) {
   if ((rc = tm_launch_positions(s))) return rc;
   k_cbox_chunks<<<s->nchunk, 256, 0, st>>>(s->d_chunk, s->d_xhi, s->d_cbox);
   k_grid_from_chunks<<<tm_div_up(s->nmol, 4), 128, 0, st>>>(
-      s->d_cbox, s->d_mol_chunk, s->d_off, s->d_grid, s->d_ncell_m, s->nmol, k.r_rc_d,
+      s->d_cbox, s->d_mol_chunk, s->d_off, s->d_grid, s->d_ncell_m, s->nmol, k.r_rc_d + s->skin,
       s->periodic ? 1 : 0, s->lat[0], s->lat[4], s->lat[8], 0.0, 2.0, 64.0, 0, 0, 0);
   ctx->launches++;
   k_grid_offsets<<<1, 32, 0, st>>>(s->d_grid, s->d_ncell_m, s->nmol, s->d_ncell, s->ncell_cap,
@@ -862,7 +976,23 @@ int tm_launch_nlist(tm_system* s) {
   ctx->launches += 2;
   if (!s->need_sticky) cudaMemsetAsync(s->d_need, 0, sizeof(int32_t) * 2, st);
   NbrArgs a = make_nbr_args(s, s->d_need);
-  const size_t shm = (size_t)4 * (s->KR + s->KA) * sizeof(uint64_t);
+  if (s->skin > 0.0) {
+    // candidates: every neighbour within AN1_r_Rc + skin (FP64 test at that
+    // radius), sorted as the rows are; the rows themselves come from the filter
+    if (!s->need_sticky) cudaMemsetAsync(s->d_need_c, 0, sizeof(int32_t) * 2, st);
+    a.need = s->d_need_c;
+    a.nbr_r = s->d_cand;
+    a.cnt_r = s->d_ccnt;
+    a.KR = s->KC;
+    a.KA = 1;              // no angular entries (ra = 0); the angular counts
+                           // written here are replaced by the filter
+    a.rr = k.r_rc_d + s->skin;
+    a.rr2_lo = (float)(a.rr * a.rr) * (1.f - kBand);
+    a.rr2_hi = (float)(a.rr * a.rr) * (1.f + kBand);
+    a.ra = 0.0;
+    a.ra2_lo = a.ra2_hi = -1.f;
+  }
+  const size_t shm = (size_t)4 * (a.KR + a.KA) * sizeof(uint64_t);
   if (shm > 48 * 1024) {
     cudaFuncSetAttribute(k_nbr_build<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
     cudaFuncSetAttribute(k_nbr_build<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
@@ -871,11 +1001,19 @@ int tm_launch_nlist(tm_system* s) {
     k_nbr_build<true><<<tm_div_up(s->N, 4), 128, shm, st>>>(a);
   else
     k_nbr_build<false><<<tm_div_up(s->N, 4), 128, shm, st>>>(a);
+  ctx->launches++;
+  if (s->skin > 0.0) {
+    cudaMemsetAsync(s->d_disp, 0, sizeof(unsigned long long), st);
+    cudaMemcpyAsync(s->d_x_at_build, s->d_x, sizeof(double) * 3 * s->N, cudaMemcpyDeviceToDevice, st);
+    if ((rc = launch_filter(s))) return rc;
+    s->cand_valid = true;
+    s->cand_rebuild = false;
+  }
   k_nbr_reverse<<<tm_div_up(s->N, 4), 128, 0, st>>>(s->d_nbr_r, s->d_cnt_r, s->d_rev_r, s->d_elem,
                                                     s->d_mol, s->d_off, s->N, s->KR);
   k_nbr_reverse<<<tm_div_up(s->N, 4), 128, 0, st>>>(s->d_nbr_a, s->d_cnt_a, s->d_rev_a, s->d_elem,
                                                     s->d_mol, s->d_off, s->N, s->KA);
-  ctx->launches += 3;
+  ctx->launches += 2;
   // Coulomb grid: about 24 atoms per cell, atoms packed in cell order
   k_grid_from_chunks<<<tm_div_up(s->nmol, 4), 128, 0, st>>>(
       s->d_cbox, s->d_mol_chunk, s->d_off, s->d_egrid, s->d_encell_m, s->nmol, 2.0,
@@ -900,9 +1038,32 @@ int tm_launch_nlist(tm_system* s) {
                                                   s->d_egrid, s->d_ecell_of_atom, s->d_epos,
                                                   s->d_exhi, s->N);
   ctx->launches += 3;
-  cudaMemcpyAsync(s->d_x_at_build, s->d_x, sizeof(double) * 3 * s->N, cudaMemcpyDeviceToDevice, st);
+  if (s->skin <= 0.0)
+    cudaMemcpyAsync(s->d_x_at_build, s->d_x, sizeof(double) * 3 * s->N, cudaMemcpyDeviceToDevice, st);
   s->nlist_valid = true;
   return tm_cuda_check(ctx, cudaGetLastError(), "nlist");
+}
+
+// Skin lists between candidate builds: positions, exact rows filtered from
+// the candidates, reverse edges, and the Coulomb-grid packing of the current
+// positions into the cells of the last build.
+int tm_launch_nlist_filter(tm_system* s) {
+  tm_ctx* ctx = s->ctx;
+  cudaStream_t st = ctx->stream;
+  int rc;
+  if ((rc = tm_launch_positions(s))) return rc;
+  if (!s->need_sticky) cudaMemsetAsync(s->d_need, 0, sizeof(int32_t) * 2, st);
+  if ((rc = launch_filter(s))) return rc;
+  k_nbr_reverse<<<tm_div_up(s->N, 4), 128, 0, st>>>(s->d_nbr_r, s->d_cnt_r, s->d_rev_r, s->d_elem,
+                                                    s->d_mol, s->d_off, s->N, s->KR);
+  k_nbr_reverse<<<tm_div_up(s->N, 4), 128, 0, st>>>(s->d_nbr_a, s->d_cnt_a, s->d_rev_a, s->d_elem,
+                                                    s->d_mol, s->d_off, s->N, s->KA);
+  k_ee_pack<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_ecell_atoms, s->d_x, s->d_elem, s->d_mol,
+                                                  s->d_egrid, s->d_ecell_of_atom, s->d_epos,
+                                                  s->d_exhi, s->N);
+  ctx->launches += 3;
+  s->nlist_valid = true;
+  return tm_cuda_check(ctx, cudaGetLastError(), "nlist filter");
 }
 
 // After a stream sync: if the last build overflowed a row, enlarge the rows

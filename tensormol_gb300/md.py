@@ -51,11 +51,13 @@ class DeviceMD:
         self.ctx.check(self.lib.tm_md_get_velocities(self.h, ctypes.c_void_p(v.ctypes.data), 0))
         return v
 
-    def run(self, nsteps):
+    def run(self, nsteps, skin=0.0):
         """Integrate nsteps; returns the log [nsteps, 4] = (potential Hartree,
-        KE J/mol per atom, conserved J/mol, T_eff K)."""
+        KE J/mol per atom, conserved J/mol, T_eff K). skin > 0 (A): neighbour
+        candidates within the cutoffs + skin are rebuilt only when atoms may
+        have moved skin/2; the rows used by every step are still exact."""
         log = np.zeros((max(nsteps, 1), 4))
-        self.ctx.check(self.lib.tm_md_run(self.h, int(nsteps), 0.0,
+        self.ctx.check(self.lib.tm_md_run(self.h, int(nsteps), float(skin),
                                           ctypes.c_void_p(log.ctypes.data)))
         return log[:nsteps]
 
