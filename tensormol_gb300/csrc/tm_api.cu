@@ -46,6 +46,7 @@ static const char* status_where(int w) {
   switch (w) {
     case 1: return "positions";
     case 2: return "cell grid";
+    case 3: return "pair terms (sums out of range)";
     case 100: case 101: case 102: return "tensor-core GEMM";
     default: return "kernel";
   }
@@ -570,7 +571,7 @@ static int system_alloc(tm_system* s, int N_cap, int nmol_cap, int Mpad_cap, int
   A.get(&s->d_epos, sizeof(int32_t) * N);
   A.get(&s->d_exhi, sizeof(float4) * N);
   A.get(&s->d_exlo, sizeof(float4) * N);
-  A.get(&s->d_cpart, sizeof(float4) * 2 * (size_t)TM_EE_SPLIT * N);
+  A.get(&s->d_cacc, sizeof(unsigned long long) * 5 * (size_t)N);
   A.get(&s->d_cnt_r, sizeof(int32_t) * N);
   A.get(&s->d_cnt_a, sizeof(int32_t) * N);
   A.get(&s->d_nbr_r, sizeof(uint32_t) * (size_t)N * s->KR);
@@ -705,7 +706,7 @@ static void system_free(tm_system* s) {
                   s->d_chunk, s->d_mol_chunk, s->d_part, s->d_cbox,
                   s->d_egrid, s->d_encell, s->d_encell_m, s->d_ecell_cnt, s->d_ecell_start,
                   s->d_ecell_atoms, s->d_ecell_of_atom, s->d_epos, s->d_exhi, s->d_exlo, s->d_sort_tmp, s->d_scan_tmp, s->d_ccnt, s->d_cand, s->d_need_c, s->d_disp,
-                  s->d_cpart,
+                  s->d_cacc,
                   s->d_cell_cnt, s->d_cell_start, s->d_cell_atoms, s->d_cell_of_atom, s->d_cnt_r,
                   s->d_cnt_a, s->d_nbr_r, s->d_nbr_a, s->d_rev_r, s->d_rev_a, s->d_sr, s->d_va,
                   s->dEdG, s->epart, s->d_Eatom, s->d_qraw, s->d_q, s->d_dEdq, s->d_fself,

@@ -8,12 +8,19 @@
 //
 // Pair terms are evaluated without a stored pair list, on a second cell grid
 // sized for about 24 atoms per cell with the atoms packed in cell order: one
-// warp per cell, lane = centre atom; the cells whose boxes come within the
-// Coulomb cutoff are staged 32 atoms at a time in shared memory and read by
-// all lanes as broadcasts. Every pair is evaluated from both ends (a gather),
-// so per-atom sums need no atomics and are deterministic. Membership uses the
-// same FP32 screen + exact FP64 rule as the neighbour lists. Energies are
-// returned as half-pair sums per atom and reduced per molecule in FP64.
+// warp per (cell, share of the stencil), lane = centre atom; the cells of the
+// upper half of the stencil (offsets after (0,0,0) in x-major order, plus
+// the centre cell's own later atoms) are staged in shared memory and read by
+// all lanes as broadcasts, so every pair is evaluated once (Newton's third
+// law). The centre's sums stay in registers; the reaction on the staged
+// atom (its dE/dq~ share and gradient) is added into per-candidate
+// fixed-point sums in shared memory (32-bit integer atomics, each term split
+// into a coarse and a fine part) and then into per-atom 64-bit fixed-point
+// totals in global memory. Integer addition is associative, so the totals are
+// bit-identical whatever order the warps and lanes add them in. The vdW
+// energy of a pair is booked whole at the centre. Membership uses the same FP32 screen +
+// exact FP64 rule as the neighbour lists. Energies are returned as half-pair
+// sums per atom and reduced per molecule in FP64.
 #include <cuda_runtime.h>
 
 #include "tm_internal.h"
@@ -105,7 +112,8 @@ struct CoulArgs {
   double* ecv;              // [N][2]
   float* dEdqt;             // [N]  dE/d q~_i
   float4* fcv;              // [N]  dE/dx_i of the pair terms
-  float4* part;             // [TM_EE_SPLIT][N][2] partial sums per stencil split
+  unsigned long long* acc;  // [5][N] fixed-point sums (cell order): cc, vdw, dE/dx xyz
+  tm_dev_status* st;
   int natoms;
   int ref_periodic;         // image pairs contribute half the force (reference gradient)
   int periodic;
@@ -120,10 +128,42 @@ struct CoulArgs {
 };
 
 struct PairOut {
-  float e_cc;   // q_j * k(r)           (energy = 0.5 * q_i * sum)
-  float e_vdw;  // K_vdw                (energy = 0.5 * sum)
+  float kc;     // k(r): the centre's sum takes q_j * k, the candidate's q_i * k
+  float e_vdw;  // K_vdw                (the pair's energy, booked at the centre)
   float dedr;   // dE/dr (Angstrom) of the pair
 };
+
+// 2^32 fixed-point units per Hartree (per Hartree/A for the gradient):
+// resolution 2.3e-10, range +-2.1e9.
+constexpr float kFixScale = 4294967296.f;
+constexpr double kFixInv = 1.0 / 4294967296.0;
+
+// Adds v to a 2^-32 fixed-point total in global memory; |v| >= 2^31 (only
+// non-finite or absurd charges reach it) flags the status word instead.
+__device__ __forceinline__ void add_fix(unsigned long long* dst, float v, tm_dev_status* st) {
+  if (!(fabsf(v) < 2.0e9f)) {
+    tm_flag(st, TM_E_NONFINITE, 0, 3);
+    return;
+  }
+  const long long t = __float2ll_rn(v * kFixScale);
+  if (t) atomicAdd(dst, (unsigned long long)t);
+}
+
+// Adds v to a staged candidate's split sum: hi counts 2^-8, lo 2^-32 (the
+// rounding remainder of hi, |lo| <= 2^23). A stage adds at most 32 terms per
+// candidate (one per centre lane), so |v| < 2^17 keeps both int32 sums
+// exact; larger terms go straight to the global total.
+__device__ __forceinline__ void add_split(int* hi, int* lo, unsigned long long* glob, float v,
+                                          tm_dev_status* st) {
+  const float s = v * 256.f;
+  if (fabsf(s) < 33554432.f) {
+    const float h = rintf(s);
+    atomicAdd(hi, (int)h);
+    atomicAdd(lo, __float2int_rn((s - h) * 16777216.f));   // s - h is exact
+  } else {
+    add_fix(glob, v, st);
+  }
+}
 
 // r in Angstrom and ir = 1/r; s6 = sqrt(C6_i C6_j), R0 = R0_i + R0_j of the pair.
 __device__ __forceinline__ PairOut pair_terms(float r, float ir, float qi, float qj, float s6,
@@ -148,7 +188,7 @@ __device__ __forceinline__ PairOut pair_terms(float r, float ir, float qi, float
       kc = k.elu_a * (ex - 1.f) + k.elu_shift;
       dkc = k.elu_a * ex;
     }
-    o.e_cc = qj * kc;
+    o.kc = kc;
     o.dedr = qi * qj * dkc * k.bohr;
   }
   if (k.has_vdw) {
@@ -176,7 +216,7 @@ __device__ __forceinline__ PairOut pair_terms(float r, float ir, float qi, float
   return o;
 }
 
-// One warp per (Coulomb-grid cell, stencil split); lane = centre atom (cells
+// One warp per (Coulomb-grid cell, stencil share); lane = centre atom (cells
 // with more than 32 atoms loop). Positions are stored relative to the origin
 // of each atom's cell; a staged candidate is moved into the centre cell's
 // frame once (p_j + stencil offset x cell edge, periodic images included), so
@@ -189,13 +229,15 @@ __device__ __forceinline__ PairOut pair_terms(float r, float ir, float qi, float
 constexpr int kStage = 128;
 
 struct StageSmem {
-  float4 p[kStage];        // candidate position in the centre cell's frame (w = element)
-  float q[kStage];         // candidate charge
-  uint32_t meta[kStage];   // image code << 27 | cell-order index
+  float4 p[kStage];                  // candidate position in the centre cell's frame (w = element)
+  float q[kStage];                   // candidate charge
+  uint32_t meta[kStage];             // image code << 27 | cell-order index
+  int hi[4][kStage];                 // reaction sums on the candidates: dE/dq~, dE/dx xyz
+  int lo[4][kStage];
 };
 
 __device__ __forceinline__ void coulomb_flush(const CoulArgs& a, const tm_consts& k,
-                                              const StageSmem& st, int n, int ti, float4 pi,
+                                              StageSmem& st, int n, int ti, int t0, float4 pi,
                                               float qi, const float* s6row, const float* r0row,
                                               float& acc_cc, float& acc_vdw, float& gx, float& gy,
                                               float& gz) {
@@ -214,7 +256,9 @@ __device__ __forceinline__ void coulomb_flush(const CoulArgs& a, const tm_consts
     else { q = 64 + __ffsll((long long)m1) - 1; m1 &= m1 - 1; }
     const uint32_t meta = st.meta[q];
     const int jp = (int)(meta & ((1u << 27) - 1)), r = (int)(meta >> 27);
-    if (jp == ti && r == TM_IMG_SELF) continue;   // the atom itself
+    // the centre cell itself (the only same-image candidates of this cell):
+    // each pair once, from its lower cell-order index
+    if (r == TM_IMG_SELF && jp >= t0 && jp <= ti) continue;
     const float4 pj = st.p[q];
     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
     const float d2 = dx * dx + dy * dy + dz * dz;
@@ -233,13 +277,31 @@ __device__ __forceinline__ void coulomb_flush(const CoulArgs& a, const tm_consts
     const float ir = rsqrtf(d2);
     const int ej = __float_as_int(pj.w);
     const PairOut po = pair_terms(d2 * ir, ir, qi, st.q[q], s6row[ej], r0row[ej], a, k);
-    acc_cc += po.e_cc;
+    acc_cc += st.q[q] * po.kc;
     acc_vdw += po.e_vdw;
     const float fscale = (a.ref_periodic && r != TM_IMG_SELF) ? 0.5f : 1.f;
     const float sc = fscale * po.dedr * ir;
     gx += sc * dx;
     gy += sc * dy;
     gz += sc * dz;
+    const size_t nat = (size_t)a.natoms;
+    add_split(&st.hi[0][q], &st.lo[0][q], a.acc + jp, qi * po.kc, a.st);
+    add_split(&st.hi[1][q], &st.lo[1][q], a.acc + 2 * nat + jp, -sc * dx, a.st);
+    add_split(&st.hi[2][q], &st.lo[2][q], a.acc + 3 * nat + jp, -sc * dy, a.st);
+    add_split(&st.hi[3][q], &st.lo[3][q], a.acc + 4 * nat + jp, -sc * dz, a.st);
+  }
+}
+
+// Adds the staged candidates' reaction sums into their atoms' totals.
+__device__ __forceinline__ void coulomb_drain(const CoulArgs& a, const StageSmem& st, int n,
+                                              int lane) {
+  for (int t = lane; t < n; t += 32) {
+    const int jp = (int)(st.meta[t] & ((1u << 27) - 1));
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const long long v = (long long)st.hi[c][t] * 16777216ll + (long long)st.lo[c][t];
+      if (v) atomicAdd(a.acc + (size_t)(c == 0 ? 0 : c + 1) * a.natoms + jp, (unsigned long long)v);
+    }
   }
 }
 
@@ -267,6 +329,12 @@ __global__ void __launch_bounds__(128, 4) k_coulomb(const CoulArgs a, const tm_c
   const int Ry = a.periodic ? min((int)ceil(a.reach / g.cy), g.ny) : (int)ceil(a.reach / g.cy);
   const int Rz = a.periodic ? min((int)ceil(a.reach / g.cz), g.nz) : (int)ceil(a.reach / g.cz);
   StageSmem& st = stage[wib];
+  // upper half of the (ox, oy) columns: (0, 0) (oz >= 0 only), then the
+  // columns after it in x-major order (all oz); the box-distance cull is
+  // symmetric in the offset, so every pair is met exactly once
+  const int ny2 = 2 * Ry + 1;
+  const int col0 = Rx * ny2 + Ry;
+  const int nhalf = (2 * Rx + 1) * ny2 - col0;
   for (int ib = t0; ib < t1; ib += 32) {
     const int ti = ib + lane;
     const bool have = ti < t1;
@@ -276,15 +344,14 @@ __global__ void __launch_bounds__(128, 4) k_coulomb(const CoulArgs a, const tm_c
     const float* s6row = tab[0] + ei * k.nele;
     const float* r0row = tab[1] + ei * k.nele;
     float acc_cc = 0.f, acc_vdw = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
-    // this warp's share of the stencil: every TM_EE_SPLIT-th (ox, oy) column
-    const int ncol = (2 * Rx + 1) * (2 * Ry + 1);
-    for (int col = split; col < ncol; col += TM_EE_SPLIT) {
-      const int ox = col / (2 * Ry + 1) - Rx, oy = col % (2 * Ry + 1) - Ry;
+    for (int col = split; col < nhalf; col += TM_EE_SPLIT) {
+      const int cf = col0 + col;
+      const int ox = cf / ny2 - Rx, oy = cf % ny2 - Ry;
       const float gapx = fmaxf(0.f, (float)(abs(ox) - 1)) * cx;
       const float gapy = fmaxf(0.f, (float)(abs(oy) - 1)) * cy;
       const float offx = (float)(ox * g.cx), offy = (float)(oy * g.cy);
       int n = 0;   // staged candidates
-      for (int oz = -Rz; oz <= Rz; ++oz) {
+      for (int oz = (col == 0 ? 0 : -Rz); oz <= Rz; ++oz) {
         const float gapz = fmaxf(0.f, (float)(abs(oz) - 1)) * cz;
         if (gapx * gapx + gapy * gapy + gapz * gapz > a.reach2) continue;
         int jx = ix + ox, jy = iy + oy, jz = iz + oz, sx = 0, sy = 0, sz = 0;
@@ -308,48 +375,57 @@ __global__ void __launch_bounds__(128, 4) k_coulomb(const CoulArgs a, const tm_c
             st.p[n + t] = make_float4(pj.x + offx, pj.y + offy, pj.z + offz, pj.w);
             st.q[n + t] = a.exlo[u0 + t].w;
             st.meta[n + t] = rcode | (uint32_t)(u0 + t);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              st.hi[e][n + t] = 0;
+              st.lo[e][n + t] = 0;
+            }
           }
           n += take;
           u0 += take;
           if (n == kStage) {
             __syncwarp();
-            if (have) coulomb_flush(a, k, st, n, ti, pi, qi, s6row, r0row, acc_cc, acc_vdw, gx, gy, gz);
+            if (have) coulomb_flush(a, k, st, n, ti, t0, pi, qi, s6row, r0row, acc_cc, acc_vdw, gx, gy, gz);
+            __syncwarp();
+            coulomb_drain(a, st, n, lane);
             n = 0;
           }
         }
       }
       if (n) {
         __syncwarp();
-        if (have) coulomb_flush(a, k, st, n, ti, pi, qi, s6row, r0row, acc_cc, acc_vdw, gx, gy, gz);
+        if (have) coulomb_flush(a, k, st, n, ti, t0, pi, qi, s6row, r0row, acc_cc, acc_vdw, gx, gy, gz);
+        __syncwarp();
+        coulomb_drain(a, st, n, lane);
       }
     }
     if (have) {
-      float4* dst = a.part + 2 * ((size_t)split * a.natoms + ti);
-      dst[0] = make_float4(acc_cc, acc_vdw, gx, gy);
-      dst[1] = make_float4(gz, 0.f, 0.f, 0.f);
+      const size_t nn = (size_t)a.natoms;
+      add_fix(a.acc + ti, acc_cc, a.st);
+      add_fix(a.acc + nn + ti, acc_vdw, a.st);
+      add_fix(a.acc + 2 * nn + ti, gx, a.st);
+      add_fix(a.acc + 3 * nn + ti, gy, a.st);
+      add_fix(a.acc + 4 * nn + ti, gz, a.st);
     }
   }
 }
 
-// Per atom (cell order): the stencil splits' partial sums added in split order.
+// Per atom (cell order): the fixed-point totals to the per-atom outputs.
 __global__ void k_coulomb_finish(const CoulArgs a) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= a.natoms) return;
-  float cc = 0.f, vdw = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
-  for (int s = 0; s < TM_EE_SPLIT; ++s) {
-    const float4* src = a.part + 2 * ((size_t)s * a.natoms + p);
-    const float4 u = src[0], v = src[1];
-    cc += u.x;
-    vdw += u.y;
-    gx += u.z;
-    gy += u.w;
-    gz += v.x;
-  }
+  const long long* acc = (const long long*)a.acc;
+  const size_t n = (size_t)a.natoms;
+  const double cc = (double)acc[p] * kFixInv;
+  const double vdw = (double)acc[n + p] * kFixInv;
+  const float gx = (float)((double)acc[2 * n + p] * kFixInv);
+  const float gy = (float)((double)acc[3 * n + p] * kFixInv);
+  const float gz = (float)((double)acc[4 * n + p] * kFixInv);
   const int i = a.eatom[p];
   const float qi = a.exlo[p].w;
-  a.ecv[2 * i + 0] = 0.5 * (double)qi * (double)cc;
-  a.ecv[2 * i + 1] = 0.5 * (double)vdw;
-  a.dEdqt[i] = cc;
+  a.ecv[2 * i + 0] = 0.5 * (double)qi * cc;
+  a.ecv[2 * i + 1] = vdw;   // whole pair energies of the pairs this atom is centre of
+  a.dEdqt[i] = (float)cc;
   a.fcv[i] = make_float4(gx, gy, gz, 0.f);
 }
 
@@ -425,7 +501,7 @@ int tm_launch_coulomb(tm_system* s, unsigned flags) {
   a.x = s->d_x; a.exhi = s->d_exhi; a.exlo = s->d_exlo; a.eatom = s->d_ecell_atoms;
   a.mol = s->d_mol; a.grid = s->d_egrid; a.cell_start = s->d_ecell_start; a.ncell = s->d_encell;
   a.ncell_cap = s->ecell_cap; a.ecv = s->d_ecv; a.dEdqt = s->d_dEdq; a.fcv = s->d_fcv;
-  a.part = s->d_cpart; a.natoms = s->N;
+  a.acc = s->d_cacc; a.natoms = s->N; a.st = ctx->d_status;
   a.ref_periodic = (s->periodic && (flags & TM_F_REFERENCE_PERIODIC_FORCE)) ? 1 : 0;
   a.periodic = s->periodic ? 1 : 0;
   a.ree = k.ree_d;
@@ -440,6 +516,7 @@ int tm_launch_coulomb(tm_system* s, unsigned flags) {
   a.c_lin = (float)((double)k.zz / (double)k.r_lr + (double)k.yy);
   for (int q = 0; q < 9; ++q) a.lat[q] = s->lat[q];
   tm_fill_shifts(s, a.sh_hi, a.sh_lo);
+  cudaMemsetAsync(s->d_cacc, 0, sizeof(unsigned long long) * 5 * (size_t)s->N, ctx->stream);
   k_coulomb<<<tm_div_up(s->ecell_cap * TM_EE_SPLIT, 4), 128, 0, ctx->stream>>>(a, k);
   k_coulomb_finish<<<tm_div_up(s->N, 256), 256, 0, ctx->stream>>>(a);
   ctx->launches += 2;

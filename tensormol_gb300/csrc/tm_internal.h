@@ -15,7 +15,7 @@
 #define TM_MAX_HIDDEN 4
 #define TM_BN 256          // padding of the hidden width H and descriptor width Dp
 #define TM_BM 128          // GEMM M tile (rows per element are padded to this)
-#define TM_EE_SPLIT 16     // warps sharing one Coulomb cell's candidate stencil
+#define TM_EE_SPLIT 8      // warps sharing one Coulomb cell's half stencil
 
 // Constants of the model read by the device kernels (passed by value).
 struct tm_consts {
@@ -138,7 +138,7 @@ struct tm_system {
   int32_t* d_epos = nullptr;           // [N] position of an atom in cell order
   float4* d_exhi = nullptr;            // [N] cell-ordered hi parts (w = element)
   float4* d_exlo = nullptr;            // [N] cell-ordered lo parts (w = charge)
-  float4* d_cpart = nullptr;           // [TM_EE_SPLIT][N][2] pair-term partial sums
+  unsigned long long* d_cacc = nullptr; // [5][N] pair-term fixed-point sums (cell order)
   // neighbour lists (ELL, per centre sorted by (element, reference index))
   int KR = 64, KA = 48;
   int32_t* d_cnt_r = nullptr;
