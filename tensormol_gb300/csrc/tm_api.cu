@@ -572,6 +572,8 @@ static int system_alloc(tm_system* s, int N_cap, int nmol_cap, int Mpad_cap, int
   A.get(&s->d_exhi, sizeof(float4) * N);
   A.get(&s->d_exlo, sizeof(float4) * N);
   A.get(&s->d_cacc, sizeof(unsigned long long) * 5 * (size_t)N);
+  A.get(&s->d_eblk, sizeof(int4) * ((size_t)N / 32 + ecell_alloc + 1));
+  A.get(&s->d_neblk, sizeof(int32_t));
   A.get(&s->d_cnt_r, sizeof(int32_t) * N);
   A.get(&s->d_cnt_a, sizeof(int32_t) * N);
   A.get(&s->d_nbr_r, sizeof(uint32_t) * (size_t)N * s->KR);
@@ -706,7 +708,7 @@ static void system_free(tm_system* s) {
                   s->d_chunk, s->d_mol_chunk, s->d_part, s->d_cbox,
                   s->d_egrid, s->d_encell, s->d_encell_m, s->d_ecell_cnt, s->d_ecell_start,
                   s->d_ecell_atoms, s->d_ecell_of_atom, s->d_epos, s->d_exhi, s->d_exlo, s->d_sort_tmp, s->d_scan_tmp, s->d_ccnt, s->d_cand, s->d_need_c, s->d_disp,
-                  s->d_cacc,
+                  s->d_cacc, s->d_eblk, s->d_neblk,
                   s->d_cell_cnt, s->d_cell_start, s->d_cell_atoms, s->d_cell_of_atom, s->d_cnt_r,
                   s->d_cnt_a, s->d_nbr_r, s->d_nbr_a, s->d_rev_r, s->d_rev_a, s->d_sr, s->d_va,
                   s->dEdG, s->epart, s->d_Eatom, s->d_qraw, s->d_q, s->d_dEdq, s->d_fself,

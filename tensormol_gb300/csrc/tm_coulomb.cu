@@ -7,21 +7,24 @@
 // halving TFBehlerParinelloSymEE.py:1550, 1620.
 //
 // Pair terms are evaluated without a stored pair list, on a second cell grid
-// sized for about 24 atoms per cell with the atoms packed in cell order: one
-// warp per (cell, share of the stencil), lane = centre atom; the cells of the
-// upper half of the stencil (offsets after (0,0,0) in x-major order, plus
-// the centre cell's own later atoms) are staged in shared memory and read by
-// all lanes as broadcasts, so every pair is evaluated once (Newton's third
-// law). The centre's sums stay in registers; the reaction on the staged
-// atom (its dE/dq~ share and gradient) is added into per-candidate
-// fixed-point sums in shared memory (32-bit integer atomics, each term split
-// into a coarse and a fine part) and then into per-atom 64-bit fixed-point
-// totals in global memory. Integer addition is associative, so the totals are
-// bit-identical whatever order the warps and lanes add them in. The vdW
-// energy of a pair is booked whole at the centre. Membership uses the same FP32 screen +
-// exact FP64 rule as the neighbour lists. Energies are returned as half-pair
-// sums per atom and reduced per molecule in FP64.
+// sized for about 24 atoms per cell with the atoms packed in cell order. One
+// warp per (centre block, share of the stencil): a centre block is a run of
+// up to 32 consecutive atoms of one (x, y) column of cells, lane = centre.
+// Candidates come from the upper half of the stencil (column offsets after
+// (0, 0) in x-major order; in the own column, the atoms after the centre in
+// cell order), so every pair is evaluated once (Newton's third law). They are
+// staged in shared memory after a screen against the centres' bounding box
+// and taken by all lanes in the same order. The centre's sums stay in
+// registers; the reaction on a candidate (its dE/dq~ share and gradient) is
+// summed over the lanes by a butterfly and added into per-atom 64-bit
+// fixed-point totals in global memory. Integer addition is associative, so
+// the totals are bit-identical whatever order the warps add them in. The vdW
+// energy of a pair is booked whole at the centre. Membership uses the same
+// FP32 screen + exact FP64 rule as the neighbour lists. Per-molecule energies
+// are reduced in FP64.
 #include <cuda_runtime.h>
+
+#include <climits>
 
 #include "tm_internal.h"
 
@@ -107,8 +110,10 @@ struct CoulArgs {
   const int32_t* mol;
   const tm_grid* grid;      // Coulomb grid per molecule
   const int32_t* cell_start;
-  const int32_t* ncell;
-  int ncell_cap;
+  const int32_t* cell_of;   // [N] Coulomb cell of each atom
+  const int4* blk;          // centre blocks (column head cell, first atom, end atom)
+  const int32_t* nblk;
+  int blk_cap;
   double* ecv;              // [N][2]
   float* dEdqt;             // [N]  dE/d q~_i
   float4* fcv;              // [N]  dE/dx_i of the pair terms
@@ -121,6 +126,7 @@ struct CoulArgs {
   float ree2, ree2_lo, ree2_hi;
   double reach;             // cell search radius: cutoff + skin (cells from an earlier build)
   float reach2;
+  float pre2;               // candidate-vs-centre-box screen: ree^2 (1 + 2e-5)
   float inv_bohr, inv_b2, inv_vdw_width, c_lin;   // 1/bohr, 1/bohr^2, 1/width, zz/R_lr + yy
   double lat[9];
   float sh_hi[27][3];
@@ -147,22 +153,6 @@ __device__ __forceinline__ void add_fix(unsigned long long* dst, float v, tm_dev
   }
   const long long t = __float2ll_rn(v * kFixScale);
   if (t) atomicAdd(dst, (unsigned long long)t);
-}
-
-// Adds v to a staged candidate's split sum: hi counts 2^-8, lo 2^-32 (the
-// rounding remainder of hi, |lo| <= 2^23). A stage adds at most 32 terms per
-// candidate (one per centre lane), so |v| < 2^17 keeps both int32 sums
-// exact; larger terms go straight to the global total.
-__device__ __forceinline__ void add_split(int* hi, int* lo, unsigned long long* glob, float v,
-                                          tm_dev_status* st) {
-  const float s = v * 256.f;
-  if (fabsf(s) < 33554432.f) {
-    const float h = rintf(s);
-    atomicAdd(hi, (int)h);
-    atomicAdd(lo, __float2int_rn((s - h) * 16777216.f));   // s - h is exact
-  } else {
-    add_fix(glob, v, st);
-  }
 }
 
 // r in Angstrom and ir = 1/r; s6 = sqrt(C6_i C6_j), R0 = R0_i + R0_j of the pair.
@@ -216,53 +206,44 @@ __device__ __forceinline__ PairOut pair_terms(float r, float ir, float qi, float
   return o;
 }
 
-// One warp per (Coulomb-grid cell, stencil share); lane = centre atom (cells
-// with more than 32 atoms loop). Positions are stored relative to the origin
-// of each atom's cell; a staged candidate is moved into the centre cell's
-// frame once (p_j + stencil offset x cell edge, periodic images included), so
-// a pair vector is one FP32 subtraction per axis, accurate to about 1e-6 A.
-// The candidate cells of one stencil column (culled by box distance) are
-// staged up to kStage atoms at a time in shared memory and read back as
-// broadcasts; each lane then walks its own set bits over the whole stage, so
-// the warp's divergence is set by the spread of per-lane pair counts over
-// kStage candidates rather than over 32.
+// Positions are stored relative to the origin of each atom's cell; the
+// block's centres and its staged candidates are moved into the frame of the
+// block's first cell once (stencil offset x cell edge, periodic images
+// included), so a pair vector is one FP32 subtraction per axis, accurate to
+// about 1e-6 A. Candidate cells are culled by box distance; of their atoms,
+// those within the cutoff of the centres' bounding box are staged (compacted
+// by ballot, up to kStage at a time across columns) in shared memory.
 constexpr int kStage = 128;
 
 struct StageSmem {
-  float4 p[kStage];                  // candidate position in the centre cell's frame (w = element)
+  float4 p[kStage];                  // candidate position in the block frame (w = element)
   float q[kStage];                   // candidate charge
   uint32_t meta[kStage];             // image code << 27 | cell-order index
-  int hi[4][kStage];                 // reaction sums on the candidates: dE/dq~, dE/dx xyz
-  int lo[4][kStage];
+  int key[kStage];                   // own column: cell-order index (+ column size past a z wrap);
+                                     // other columns: INT_MAX (every centre takes the pair)
+  float js[4][kStage];               // reaction sums on the candidates: dE/dq~, dE/dx xyz
 };
 
+// All lanes take the staged candidates in the same order (a warp-uniform
+// loop, so the broadcasts and the pair arithmetic of consecutive candidates
+// overlap); a lane's centre takes candidate q if it is within the cutoff and
+// the key rule allows it. The reaction on q (its dE/dq~ share and gradient)
+// is summed over the lanes by an xor butterfly, which gives every lane the
+// same bits, and stored once per stage.
 __device__ __forceinline__ void coulomb_flush(const CoulArgs& a, const tm_consts& k,
-                                              StageSmem& st, int n, int ti, int t0, float4 pi,
+                                              StageSmem& st, int n, int ti, bool have, float4 pi,
                                               float qi, const float* s6row, const float* r0row,
                                               float& acc_cc, float& acc_vdw, float& gx, float& gy,
-                                              float& gz) {
-  uint64_t m0 = 0, m1 = 0;
+                                              float& gz, int lane) {
   for (int q = 0; q < n; ++q) {
-    const float4 pj = st.p[q];
-    const float ex = pi.x - pj.x, ey = pi.y - pj.y, ez = pi.z - pj.z;
-    if (ex * ex + ey * ey + ez * ez <= a.ree2_hi) {
-      if (q < 64) m0 |= 1ull << q;
-      else m1 |= 1ull << (q - 64);
-    }
-  }
-  while (m0 | m1) {
-    int q;
-    if (m0) { q = __ffsll((long long)m0) - 1; m0 &= m0 - 1; }
-    else { q = 64 + __ffsll((long long)m1) - 1; m1 &= m1 - 1; }
-    const uint32_t meta = st.meta[q];
-    const int jp = (int)(meta & ((1u << 27) - 1)), r = (int)(meta >> 27);
-    // the centre cell itself (the only same-image candidates of this cell):
-    // each pair once, from its lower cell-order index
-    if (r == TM_IMG_SELF && jp >= t0 && jp <= ti) continue;
     const float4 pj = st.p[q];
     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
     const float d2 = dx * dx + dy * dy + dz * dz;
-    if (d2 >= a.ree2_lo) {   // within 1e-5 of the cutoff: the exact FP64 rule
+    bool hit = have && d2 <= a.ree2_hi && st.key[q] > ti;
+    const uint32_t meta = st.meta[q];
+    const int r = (int)(meta >> 27);
+    if (hit && d2 >= a.ree2_lo) {   // within 1e-5 of the cutoff: the exact FP64 rule
+      const int jp = (int)(meta & ((1u << 27) - 1));
       const int i = a.eatom[ti], j = a.eatom[jp];
       double xj = a.x[3 * j], yj = a.x[3 * j + 1], zj = a.x[3 * j + 2];
       if (a.periodic) {
@@ -272,23 +253,40 @@ __device__ __forceinline__ void coulomb_flush(const CoulArgs& a, const tm_consts
         yj = tm_image_coord(yj, sx, sy, sz, a.lat[1], a.lat[4], a.lat[7]);
         zj = tm_image_coord(zj, sx, sy, sz, a.lat[2], a.lat[5], a.lat[8]);
       }
-      if (!tm_exact_within(a.x[3 * i], a.x[3 * i + 1], a.x[3 * i + 2], xj, yj, zj, a.ree)) continue;
+      hit = tm_exact_within(a.x[3 * i], a.x[3 * i + 1], a.x[3 * i + 2], xj, yj, zj, a.ree);
     }
-    const float ir = rsqrtf(d2);
-    const int ej = __float_as_int(pj.w);
-    const PairOut po = pair_terms(d2 * ir, ir, qi, st.q[q], s6row[ej], r0row[ej], a, k);
-    acc_cc += st.q[q] * po.kc;
-    acc_vdw += po.e_vdw;
-    const float fscale = (a.ref_periodic && r != TM_IMG_SELF) ? 0.5f : 1.f;
-    const float sc = fscale * po.dedr * ir;
-    gx += sc * dx;
-    gy += sc * dy;
-    gz += sc * dz;
-    const size_t nat = (size_t)a.natoms;
-    add_split(&st.hi[0][q], &st.lo[0][q], a.acc + jp, qi * po.kc, a.st);
-    add_split(&st.hi[1][q], &st.lo[1][q], a.acc + 2 * nat + jp, -sc * dx, a.st);
-    add_split(&st.hi[2][q], &st.lo[2][q], a.acc + 3 * nat + jp, -sc * dy, a.st);
-    add_split(&st.hi[3][q], &st.lo[3][q], a.acc + 4 * nat + jp, -sc * dz, a.st);
+    if (!__any_sync(TM_FULL, hit)) continue;
+    float jc = 0.f, jx = 0.f, jy = 0.f, jz = 0.f;
+    if (hit) {
+      const float ir = rsqrtf(d2);
+      const int ej = __float_as_int(pj.w);
+      const float qj = st.q[q];
+      const PairOut po = pair_terms(d2 * ir, ir, qi, qj, s6row[ej], r0row[ej], a, k);
+      acc_cc += qj * po.kc;
+      acc_vdw += po.e_vdw;
+      const float fscale = (a.ref_periodic && r != TM_IMG_SELF) ? 0.5f : 1.f;
+      const float sc = fscale * po.dedr * ir;
+      gx += sc * dx;
+      gy += sc * dy;
+      gz += sc * dz;
+      jc = qi * po.kc;
+      jx = -sc * dx;
+      jy = -sc * dy;
+      jz = -sc * dz;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      jc += __shfl_xor_sync(TM_FULL, jc, o);
+      jx += __shfl_xor_sync(TM_FULL, jx, o);
+      jy += __shfl_xor_sync(TM_FULL, jy, o);
+      jz += __shfl_xor_sync(TM_FULL, jz, o);
+    }
+    if (lane == (q & 31)) {
+      st.js[0][q] = jc;
+      st.js[1][q] = jx;
+      st.js[2][q] = jy;
+      st.js[3][q] = jz;
+    }
   }
 }
 
@@ -299,13 +297,13 @@ __device__ __forceinline__ void coulomb_drain(const CoulArgs& a, const StageSmem
     const int jp = (int)(st.meta[t] & ((1u << 27) - 1));
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-      const long long v = (long long)st.hi[c][t] * 16777216ll + (long long)st.lo[c][t];
-      if (v) atomicAdd(a.acc + (size_t)(c == 0 ? 0 : c + 1) * a.natoms + jp, (unsigned long long)v);
+      const float v = st.js[c][t];
+      if (v != 0.f) add_fix(a.acc + (size_t)(c == 0 ? 0 : c + 1) * a.natoms + jp, v, a.st);
     }
   }
 }
 
-__global__ void __launch_bounds__(128, 4) k_coulomb(const CoulArgs a, const tm_consts k) {
+__global__ void __launch_bounds__(128, 6) k_coulomb(const CoulArgs a, const tm_consts k) {
   __shared__ StageSmem stage[4];
   __shared__ float tab[2][TM_MAX_ELE * TM_MAX_ELE];   // sqrt(C6_i C6_j), R0_i + R0_j
   if (threadIdx.x < k.nele * k.nele) {
@@ -316,45 +314,64 @@ __global__ void __launch_bounds__(128, 4) k_coulomb(const CoulArgs a, const tm_c
   __syncthreads();
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int wg = blockIdx.x * (blockDim.x >> 5) + wib;
-  const int c = wg / TM_EE_SPLIT, split = wg % TM_EE_SPLIT;
-  if (c >= a.ncell_cap || c >= *a.ncell) return;
-  const int t0 = a.cell_start[c], t1 = a.cell_start[c + 1];
-  if (t1 <= t0) return;
+  const int b = wg / TM_EE_SPLIT, split = wg % TM_EE_SPLIT;
+  if (b >= a.blk_cap || b >= *a.nblk) return;
+  const int4 bk = a.blk[b];
+  const int head = bk.x, t0 = bk.y, t1 = bk.z;
   const tm_grid g = a.grid[a.mol[a.eatom[t0]]];
-  const int lc = c - g.cell_off;
-  const int iz = lc % g.nz, iy = (lc / g.nz) % g.ny, ix = lc / (g.nz * g.ny);
+  const int lc = head - g.cell_off;
+  const int iy = (lc / g.nz) % g.ny, ix = lc / (g.nz * g.ny);
+  const int ncolumn = a.cell_start[head + g.nz] - a.cell_start[head];
+  // z range of the block's cells; positions are taken in the frame of cell
+  // (ix, iy, z0)
+  const int z0 = (a.cell_of[a.eatom[t0]] - head), z1 = (a.cell_of[a.eatom[t1 - 1]] - head);
   const float cx = (float)g.cx, cy = (float)g.cy, cz = (float)g.cz;
   // periodic: at most one wrap per axis (R <= n; edges are >= 2 * cutoff)
   const int Rx = a.periodic ? min((int)ceil(a.reach / g.cx), g.nx) : (int)ceil(a.reach / g.cx);
   const int Ry = a.periodic ? min((int)ceil(a.reach / g.cy), g.ny) : (int)ceil(a.reach / g.cy);
   const int Rz = a.periodic ? min((int)ceil(a.reach / g.cz), g.nz) : (int)ceil(a.reach / g.cz);
   StageSmem& st = stage[wib];
-  // upper half of the (ox, oy) columns: (0, 0) (oz >= 0 only), then the
-  // columns after it in x-major order (all oz); the box-distance cull is
-  // symmetric in the offset, so every pair is met exactly once
+  // Upper half of the (ox, oy) columns: (0, 0) first, then the columns
+  // after it in x-major order (every z). In the own column, cells from z0 up
+  // are staged and a centre takes a candidate only if the candidate's key
+  // (cell-order index, plus the column's atom count past a periodic wrap) is
+  // above its own index; the box-distance cull is symmetric in the offset, so
+  // every pair (and every periodic image of it) is met exactly once.
   const int ny2 = 2 * Ry + 1;
   const int col0 = Rx * ny2 + Ry;
   const int nhalf = (2 * Rx + 1) * ny2 - col0;
-  for (int ib = t0; ib < t1; ib += 32) {
-    const int ti = ib + lane;
+  {
+    const int ti = t0 + lane;
     const bool have = ti < t1;
-    const float4 pi = a.exhi[have ? ti : t0];
+    float4 pi = a.exhi[have ? ti : t0];
+    if (have) pi.z += (float)((a.cell_of[a.eatom[ti]] - head - z0) * g.cz);
     const float qi = a.exlo[have ? ti : t0].w;
     const int ei = __float_as_int(pi.w);
     const float* s6row = tab[0] + ei * k.nele;
     const float* r0row = tab[1] + ei * k.nele;
+    // bounding box of the block's centres (the lanes without one repeat t0)
+    float bx0 = pi.x, by0 = pi.y, bz0 = pi.z, bx1 = pi.x, by1 = pi.y, bz1 = pi.z;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      bx0 = fminf(bx0, __shfl_xor_sync(TM_FULL, bx0, o));
+      by0 = fminf(by0, __shfl_xor_sync(TM_FULL, by0, o));
+      bz0 = fminf(bz0, __shfl_xor_sync(TM_FULL, bz0, o));
+      bx1 = fmaxf(bx1, __shfl_xor_sync(TM_FULL, bx1, o));
+      by1 = fmaxf(by1, __shfl_xor_sync(TM_FULL, by1, o));
+      bz1 = fmaxf(bz1, __shfl_xor_sync(TM_FULL, bz1, o));
+    }
     float acc_cc = 0.f, acc_vdw = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
+    int n = 0;   // staged candidates (the stage spans columns: positions are in the block frame)
     for (int col = split; col < nhalf; col += TM_EE_SPLIT) {
       const int cf = col0 + col;
       const int ox = cf / ny2 - Rx, oy = cf % ny2 - Ry;
       const float gapx = fmaxf(0.f, (float)(abs(ox) - 1)) * cx;
       const float gapy = fmaxf(0.f, (float)(abs(oy) - 1)) * cy;
       const float offx = (float)(ox * g.cx), offy = (float)(oy * g.cy);
-      int n = 0;   // staged candidates
-      for (int oz = (col == 0 ? 0 : -Rz); oz <= Rz; ++oz) {
-        const float gapz = fmaxf(0.f, (float)(abs(oz) - 1)) * cz;
+      for (int zc = (col == 0 ? z0 : z0 - Rz); zc <= z1 + Rz; ++zc) {
+        const float gapz = fmaxf(0.f, (float)(max(z0 - zc, zc - z1) - 1)) * cz;
         if (gapx * gapx + gapy * gapy + gapz * gapz > a.reach2) continue;
-        int jx = ix + ox, jy = iy + oy, jz = iz + oz, sx = 0, sy = 0, sz = 0;
+        int jx = ix + ox, jy = iy + oy, jz = zc, sx = 0, sy = 0, sz = 0;
         if (a.periodic) {
           if (jx < 0) { jx += g.nx; sx = -1; } else if (jx >= g.nx) { jx -= g.nx; sx = 1; }
           if (jy < 0) { jy += g.ny; sy = -1; } else if (jy >= g.ny) { jy -= g.ny; sy = 1; }
@@ -364,40 +381,54 @@ __global__ void __launch_bounds__(128, 4) k_coulomb(const CoulArgs a, const tm_c
         }
         const int cj = g.cell_off + (jx * g.ny + jy) * g.nz + jz;
         const uint32_t rcode = (uint32_t)(9 * (sx + 1) + 3 * (sy + 1) + (sz + 1)) << 27;
-        const float offz = (float)(oz * g.cz);
-        int u0 = a.cell_start[cj];
+        const float offz = (float)((zc - z0) * g.cz);
+        const int kadd = col == 0 ? (sz > 0 ? ncolumn : 0) : -1;
         const int u1 = a.cell_start[cj + 1];
-        while (u0 < u1) {
-          const int take = min(u1 - u0, kStage - n);
-          __syncwarp();
-          for (int t = lane; t < take; t += 32) {
-            const float4 pj = a.exhi[u0 + t];
-            st.p[n + t] = make_float4(pj.x + offx, pj.y + offy, pj.z + offz, pj.w);
-            st.q[n + t] = a.exlo[u0 + t].w;
-            st.meta[n + t] = rcode | (uint32_t)(u0 + t);
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-              st.hi[e][n + t] = 0;
-              st.lo[e][n + t] = 0;
-            }
+        for (int u0 = a.cell_start[cj]; u0 < u1; u0 += 32) {
+          // one candidate per lane; kept if it comes within the cutoff of the
+          // centres' box (a bound on its distance to every centre)
+          const int t = u0 + lane;
+          bool keep = false;
+          float4 pj = make_float4(0.f, 0.f, 0.f, 0.f);
+          float qj = 0.f;
+          if (t < u1) {
+            const float4 pr = a.exhi[t];
+            pj = make_float4(pr.x + offx, pr.y + offy, pr.z + offz, pr.w);
+            qj = a.exlo[t].w;
+            const float ex = fmaxf(0.f, fmaxf(bx0 - pj.x, pj.x - bx1));
+            const float ey = fmaxf(0.f, fmaxf(by0 - pj.y, pj.y - by1));
+            const float ez = fmaxf(0.f, fmaxf(bz0 - pj.z, pj.z - bz1));
+            keep = ex * ex + ey * ey + ez * ez <= a.pre2;
           }
-          n += take;
-          u0 += take;
-          if (n == kStage) {
+          const unsigned m = __ballot_sync(TM_FULL, keep);
+          const int nk = __popc(m);
+          if (n + nk > kStage) {
             __syncwarp();
-            if (have) coulomb_flush(a, k, st, n, ti, t0, pi, qi, s6row, r0row, acc_cc, acc_vdw, gx, gy, gz);
+            coulomb_flush(a, k, st, n, ti, have, pi, qi, s6row, r0row, acc_cc, acc_vdw, gx, gy, gz, lane);
             __syncwarp();
             coulomb_drain(a, st, n, lane);
+            __syncwarp();
             n = 0;
           }
+          if (keep) {
+            const int pos = n + __popc(m & ((1u << lane) - 1u));
+            st.p[pos] = pj;
+            st.q[pos] = qj;
+            st.meta[pos] = rcode | (uint32_t)t;
+            st.key[pos] = kadd < 0 ? INT_MAX : t + kadd;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) st.js[e][pos] = 0.f;
+          }
+          n += nk;
         }
       }
-      if (n) {
-        __syncwarp();
-        if (have) coulomb_flush(a, k, st, n, ti, t0, pi, qi, s6row, r0row, acc_cc, acc_vdw, gx, gy, gz);
-        __syncwarp();
-        coulomb_drain(a, st, n, lane);
-      }
+    }
+    if (n) {
+      __syncwarp();
+      coulomb_flush(a, k, st, n, ti, have, pi, qi, s6row, r0row, acc_cc, acc_vdw, gx, gy, gz, lane);
+      __syncwarp();
+      coulomb_drain(a, st, n, lane);
+      __syncwarp();
     }
     if (have) {
       const size_t nn = (size_t)a.natoms;
@@ -499,8 +530,9 @@ int tm_launch_coulomb(tm_system* s, unsigned flags) {
   const tm_consts& k = s->model->k;
   CoulArgs a;
   a.x = s->d_x; a.exhi = s->d_exhi; a.exlo = s->d_exlo; a.eatom = s->d_ecell_atoms;
-  a.mol = s->d_mol; a.grid = s->d_egrid; a.cell_start = s->d_ecell_start; a.ncell = s->d_encell;
-  a.ncell_cap = s->ecell_cap; a.ecv = s->d_ecv; a.dEdqt = s->d_dEdq; a.fcv = s->d_fcv;
+  a.mol = s->d_mol; a.grid = s->d_egrid; a.cell_start = s->d_ecell_start;
+  a.cell_of = s->d_ecell_of_atom; a.blk = s->d_eblk; a.nblk = s->d_neblk;
+  a.blk_cap = s->N / 32 + s->ecell_cap + 1; a.ecv = s->d_ecv; a.dEdqt = s->d_dEdq; a.fcv = s->d_fcv;
   a.acc = s->d_cacc; a.natoms = s->N; a.st = ctx->d_status;
   a.ref_periodic = (s->periodic && (flags & TM_F_REFERENCE_PERIODIC_FORCE)) ? 1 : 0;
   a.periodic = s->periodic ? 1 : 0;
@@ -510,6 +542,7 @@ int tm_launch_coulomb(tm_system* s, unsigned flags) {
   a.ree2_hi = a.ree2 * (1.f + kBand);
   a.reach = k.ree_d + s->skin;
   a.reach2 = (float)(a.reach * a.reach) * (1.f + kBand);
+  a.pre2 = a.ree2 * (1.f + 2.f * kBand);
   a.inv_bohr = (float)(1.0 / (double)k.bohr);
   a.inv_b2 = (float)(1.0 / ((double)k.bohr * (double)k.bohr));
   a.inv_vdw_width = (float)(1.0 / (double)k.vdw_width);
@@ -517,7 +550,7 @@ int tm_launch_coulomb(tm_system* s, unsigned flags) {
   for (int q = 0; q < 9; ++q) a.lat[q] = s->lat[q];
   tm_fill_shifts(s, a.sh_hi, a.sh_lo);
   cudaMemsetAsync(s->d_cacc, 0, sizeof(unsigned long long) * 5 * (size_t)s->N, ctx->stream);
-  k_coulomb<<<tm_div_up(s->ecell_cap * TM_EE_SPLIT, 4), 128, 0, ctx->stream>>>(a, k);
+  k_coulomb<<<tm_div_up(a.blk_cap * TM_EE_SPLIT, 4), 128, 0, ctx->stream>>>(a, k);
   k_coulomb_finish<<<tm_div_up(s->N, 256), 256, 0, ctx->stream>>>(a);
   ctx->launches += 2;
   k_chunk_sum2<<<s->nchunk, 256, 0, ctx->stream>>>(s->d_chunk, s->d_ecv, s->d_dEdq, s->d_q,

@@ -15,7 +15,7 @@
 #define TM_MAX_HIDDEN 4
 #define TM_BN 256          // padding of the hidden width H and descriptor width Dp
 #define TM_BM 128          // GEMM M tile (rows per element are padded to this)
-#define TM_EE_SPLIT 8      // warps sharing one Coulomb cell's half stencil
+#define TM_EE_SPLIT 16     // warps sharing one centre block's half stencil
 
 // Constants of the model read by the device kernels (passed by value).
 struct tm_consts {
@@ -139,6 +139,9 @@ struct tm_system {
   float4* d_exhi = nullptr;            // [N] cell-ordered hi parts (w = element)
   float4* d_exlo = nullptr;            // [N] cell-ordered lo parts (w = charge)
   unsigned long long* d_cacc = nullptr; // [5][N] pair-term fixed-point sums (cell order)
+  int4* d_eblk = nullptr;              // [N/32 + ecell + 1] centre blocks: (column head cell,
+                                       //   first atom, end atom) in cell order
+  int32_t* d_neblk = nullptr;          // number of centre blocks (device scalar)
   // neighbour lists (ELL, per centre sorted by (element, reference index))
   int KR = 64, KA = 48;
   int32_t* d_cnt_r = nullptr;

@@ -297,6 +297,28 @@ __global__ void k_ee_pack(const int32_t* __restrict__ order, const double* __res
                        (float)(x[3 * a + 2] - (g.oz + iz * g.cz)), __int_as_float(elem[a]));
 }
 
+// Centre blocks of the pair-term kernel: runs of up to 32 consecutive atoms
+// (cell order) within one (x, y) column of a molecule's Coulomb grid. The
+// order of the table does not matter (every block's sums are exact integer
+// additions).
+__global__ void k_ee_blocks(const int32_t* __restrict__ order, const int32_t* __restrict__ mol,
+                            const tm_grid* __restrict__ grid, const int32_t* __restrict__ cell_of,
+                            const int32_t* __restrict__ cell_start, int4* __restrict__ blk,
+                            int32_t* __restrict__ nblk, int N, int cap, tm_dev_status* st) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= N) return;
+  const int a = order[p];
+  const tm_grid g = grid[mol[a]];
+  const int c = cell_of[a];
+  const int head = c - (c - g.cell_off) % g.nz;
+  const int cs = cell_start[head];
+  if ((p - cs) % 32) return;
+  const int ce = cell_start[head + g.nz];
+  const int slot = atomicAdd(nblk, 1);
+  if (slot < cap) blk[slot] = make_int4(head, p, min(p + 32, ce), 0);
+  else tm_flag(st, TM_E_CAPACITY, slot, 2);
+}
+
 __global__ void k_grid_offsets(tm_grid* __restrict__ grid, const int32_t* __restrict__ ncell_m,
                                int nmol, int32_t* __restrict__ total, int cap, tm_dev_status* st) {
   // single thread: nmol is at most a few thousand; this runs once per build
@@ -1037,7 +1059,12 @@ int tm_launch_nlist(tm_system* s) {
   k_ee_pack<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_ecell_atoms, s->d_x, s->d_elem, s->d_mol,
                                                   s->d_egrid, s->d_ecell_of_atom, s->d_epos,
                                                   s->d_exhi, s->N);
-  ctx->launches += 3;
+  cudaMemsetAsync(s->d_neblk, 0, sizeof(int32_t), st);
+  k_ee_blocks<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_ecell_atoms, s->d_mol, s->d_egrid,
+                                                    s->d_ecell_of_atom, s->d_ecell_start,
+                                                    s->d_eblk, s->d_neblk, s->N,
+                                                    s->N / 32 + s->ecell_cap + 1, ctx->d_status);
+  ctx->launches += 4;
   if (s->skin <= 0.0)
     cudaMemcpyAsync(s->d_x_at_build, s->d_x, sizeof(double) * 3 * s->N, cudaMemcpyDeviceToDevice, st);
   s->nlist_valid = true;
