@@ -435,10 +435,12 @@ template <bool PERIODIC>
 __global__ void __launch_bounds__(128) k_nbr_build(const NbrArgs a) {
   extern __shared__ uint64_t sh_keys[];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int i = blockIdx.x * (blockDim.x >> 5) + wib;
+  const int w = blockIdx.x * (blockDim.x >> 5) + wib;
   uint64_t* kr = sh_keys + (size_t)wib * (a.KR + a.KA);
   uint64_t* ka = kr + a.KR;
-  if (i >= a.N) return;
+  if (w >= a.N) return;
+  // centres in cell order: the warps of a block share their candidate cells
+  const int i = a.cell_atoms[w];
   const int m = a.mol[i];
   const tm_grid g = a.grid[m];
   const float4 hi = a.xhi[i], lo = a.xlo[i];
@@ -446,18 +448,23 @@ __global__ void __launch_bounds__(128) k_nbr_build(const NbrArgs a) {
   const int lc = a.cell_of[i] - g.cell_off;
   const int iz = lc % g.nz, iy = (lc / g.nz) % g.ny, ix = lc / (g.nz * g.ny);
   int nr = 0, na = 0;
+  // the three cells of a z column without a periodic wrap are one contiguous
+  // run of atoms (cell order); a wrapped column is taken cell by cell
+  const bool zrun = !PERIODIC || (iz >= 1 && iz + 1 < g.nz);
   for (int ox = -1; ox <= 1; ++ox) {
     for (int oy = -1; oy <= 1; ++oy) {
-      for (int oz = -1; oz <= 1; ++oz) {
+      for (int oz = zrun ? 0 : -1; oz <= (zrun ? 0 : 1); ++oz) {
         int jx = ix + ox, jy = iy + oy, jz = iz + oz, sx = 0, sy = 0, sz = 0;
         if (PERIODIC) {
           if (jx < 0) { jx += g.nx; sx = -1; } else if (jx >= g.nx) { jx -= g.nx; sx = 1; }
           if (jy < 0) { jy += g.ny; sy = -1; } else if (jy >= g.ny) { jy -= g.ny; sy = 1; }
           if (jz < 0) { jz += g.nz; sz = -1; } else if (jz >= g.nz) { jz -= g.nz; sz = 1; }
         } else {
-          if (jx < 0 || jx >= g.nx || jy < 0 || jy >= g.ny || jz < 0 || jz >= g.nz) continue;
+          if (jx < 0 || jx >= g.nx || jy < 0 || jy >= g.ny) continue;
         }
-        const int c = g.cell_off + (jx * g.ny + jy) * g.nz + jz;
+        const int cbase = g.cell_off + (jx * g.ny + jy) * g.nz;
+        const int c0 = cbase + (zrun ? max(iz - 1, 0) : jz);
+        const int c1 = cbase + (zrun ? min(iz + 1, g.nz - 1) : jz);
         const int r = 9 * (sx + 1) + 3 * (sy + 1) + (sz + 1);
         // shift added to the neighbour: s = sx*a0 + sy*a1 + sz*a2
         double shx = 0, shy = 0, shz = 0;
@@ -469,7 +476,7 @@ __global__ void __launch_bounds__(128) k_nbr_build(const NbrArgs a) {
           shx_h = (float)shx; shy_h = (float)shy; shz_h = (float)shz;
           shx_l = (float)(shx - shx_h); shy_l = (float)(shy - shy_h); shz_l = (float)(shz - shz_h);
         }
-        const int t0 = a.cell_start[c], t1 = a.cell_start[c + 1];
+        const int t0 = a.cell_start[c0], t1 = a.cell_start[c1 + 1];
         for (int tb = t0; tb < t1; tb += 32) {
           const int t = tb + lane;
           bool in_r = false, in_a = false;
