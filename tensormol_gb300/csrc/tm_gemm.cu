@@ -42,6 +42,8 @@ constexpr int EPI_FWD = 0, EPI_FWD_LAST = 1, EPI_BWD = 2, EPI_OUT = 3;
 
 struct GemmArgs {
   CUtensorMap a0, a1, b0, b1;
+  CUtensorMap o0, o1;  // FP32 mode: 32 x 32 boxes of the outputs (hi, lo); the
+                       // backward pass also loads the previous activation by them
   int K;             // reduction length
   int N;             // output width of one (net, element) block
   int a_net_rows;    // row offset of net 1 in A (0 when both nets read the same A)
@@ -100,6 +102,22 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
       "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
       : "memory");
+}
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y, const void* src) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(x), "r"(y), "r"(smem_u32(src))
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// the shared-memory source of every committed store has been read
+__device__ __forceinline__ void bulk_wait_read() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+// every committed store has completed
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 __device__ __forceinline__ void umma_commit(uint64_t* bar) {
   asm volatile(
@@ -267,7 +285,9 @@ struct Cfg {
   static constexpr int B_TILE = BN * 128;             // 16 KB (tf32) or 32 KB (bf16)
   static constexpr int STAGE = NSPLIT * (A_TILE + B_TILE);   // 64 KB or 48 KB
   static constexpr int NSTAGE = PREC == TM_PREC_FP32 ? 3 : 4;
-  static constexpr int SMEM = NSTAGE * STAGE + 1024 + 256;   // stages, alignment, barriers
+  // FP32 epilogue staging: per epilogue warp a 32 x 32 hi and lo box (8 KB)
+  static constexpr int EPI_BYTES = PREC == TM_PREC_FP32 ? 4 * 8192 : 0;
+  static constexpr int SMEM = NSTAGE * STAGE + EPI_BYTES + 1024 + 256;   // + alignment, barriers
   static constexpr uint32_t IDESC = make_idesc(PREC == TM_PREC_FP32 ? 2 : 1, BM, BN);
 };
 
@@ -291,11 +311,12 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~static_cast<uintptr_t>(1023));
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + C::NSTAGE * C::STAGE);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + C::NSTAGE * C::STAGE + C::EPI_BYTES);
   uint64_t* empty = full + C::NSTAGE;
   uint64_t* accf = empty + C::NSTAGE;   // [2] accumulator ready
   uint64_t* acce = accf + 2;            // [2] accumulator drained
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acce + 2);
+  uint64_t* ebar = acce + 2;            // [4] epilogue loads (one per epilogue warp)
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(ebar + 4);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -312,6 +333,7 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
       mbar_init(&accf[b], 1);
       mbar_init(&acce[b], 4);   // one arrival per epilogue warp
     }
+    for (int w = 0; w < 4; ++w) mbar_init(&ebar[w], 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -403,8 +425,17 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
     }
   } else {
     // ---- epilogue: warps 0..3, thread = accumulator row ----
+    // FP32 mode: each warp stages its 32 rows x 32 columns in shared memory in
+    // the TMA 128-byte-swizzle layout (16-byte chunk q of row r at chunk
+    // q ^ (r & 7): conflict-free for a row per lane) and writes them with one
+    // bulk tensor store per hi/lo part; the backward pass brings the previous
+    // activation in the same way.
+    float* ebh = reinterpret_cast<float*>(smem + C::NSTAGE * C::STAGE + warp * 8192);
+    float* ebl = ebh + 1024;
+    int eph = 0;   // uses of this warp's load barrier
+    bool eok = true;
     int lt = 0;
-    for (int t = blockIdx.x; t < total; t += gridDim.x, ++lt) {
+    for (int t = blockIdx.x; t < total && eok; t += gridDim.x, ++lt) {
       const int buf = lt & 1;
       if (!mbar_wait(&accf[buf], (lt >> 1) & 1)) {
         tm_flag(g.st, TM_E_TIMEOUT, t, 102);
@@ -417,10 +448,24 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
       const int elem = g.tile_elem[m_tile];
       const int row = m_tile * BM + warp * 32 + lane;          // row in this net
       const size_t orow = (size_t)net * g.Mpad + row;
+      const int orow0 = net * g.Mpad + m_tile * BM + warp * 32;   // first row of this warp
       const int pblk = (net * g.nele + elem) * g.N;
       const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(buf * C::ACC_COLS);
       float esum = 0.f;
-      for (int c = 0; c < BN; c += 32) {
+      for (int c = 0; c < BN && eok; c += 32) {
+        const int col = n_tile * BN + c;
+        if constexpr (PREC == TM_PREC_FP32) {
+          // the staging box is free once the previous stores have read it
+          if (lane == 0) bulk_wait_read();
+          __syncwarp();
+          if constexpr (EPI == EPI_BWD) {
+            if (lane == 0) {
+              mbar_expect_tx(&ebar[warp], 8192);
+              tma_load_2d(ebh, &g.o0, col, orow0, &ebar[warp]);
+              tma_load_2d(ebl, &g.o1, col, orow0, &ebar[warp]);
+            }
+          }
+        }
         uint32_t r[32];
         tmem_ld32(tbase + (uint32_t)c, r);
         if (C::NACC == 2) {
@@ -430,7 +475,6 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
           for (int q = 0; q < 32; ++q)
             r[q] = __float_as_uint(__uint_as_float(r[q]) + __uint_as_float(r2[q]));
         }
-        const int col = n_tile * BN + c;
         float v[32];
         if (EPI == EPI_FWD || EPI == EPI_FWD_LAST) {
           const float* bias = g.bias + pblk + col;
@@ -445,19 +489,64 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
               v[q] = w * actd_z<ACT>(z, g.alpha);
             }
           }
-          store32<PREC>(g.out0, g.out1, orow * g.ldo + col, v);
         } else if (EPI == EPI_BWD) {
           float h[32];
-          load32<PREC>(g.hprev0, g.hprev1, orow * g.ldo + col, h);
+          if constexpr (PREC == TM_PREC_FP32) {
+            if (!mbar_wait(&ebar[warp], eph & 1)) {
+              tm_flag(g.st, TM_E_TIMEOUT, t, 104);
+              *abort_flag = 1;
+              eok = false;
+            }
+            ++eph;
+            const float4* sh = reinterpret_cast<const float4*>(ebh) + lane * 8;
+            const float4* sl = reinterpret_cast<const float4*>(ebl) + lane * 8;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              const float4 a = sh[q ^ (lane & 7)], b = sl[q ^ (lane & 7)];
+              h[4 * q] = a.x + b.x;
+              h[4 * q + 1] = a.y + b.y;
+              h[4 * q + 2] = a.z + b.z;
+              h[4 * q + 3] = a.w + b.w;
+            }
+          } else {
+            load32<PREC>(g.hprev0, g.hprev1, orow * g.ldo + col, h);
+          }
 #pragma unroll
           for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]) * actd_h<ACT>(h[q], g.alpha);
-          store32<PREC>(g.out0, g.out1, orow * g.ldo + col, v);
         } else {
+#pragma unroll
+          for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]);
+        }
+        if constexpr (PREC == TM_PREC_FP32) {
+          float4* dh = reinterpret_cast<float4*>(ebh) + lane * 8;
+          float4* dl = reinterpret_cast<float4*>(ebl) + lane * 8;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            float4 hh, ll;
+            if (EPI == EPI_OUT) {   // one FP32 output
+              hh = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+            } else {
+              tm_tf32_split(v[4 * q], hh.x, ll.x);
+              tm_tf32_split(v[4 * q + 1], hh.y, ll.y);
+              tm_tf32_split(v[4 * q + 2], hh.z, ll.z);
+              tm_tf32_split(v[4 * q + 3], hh.w, ll.w);
+              dl[q ^ (lane & 7)] = ll;
+            }
+            dh[q ^ (lane & 7)] = hh;
+          }
+          fence_async_smem();
+          __syncwarp();
+          if (lane == 0) {
+            tma_store_2d(&g.o0, col, orow0, ebh);
+            if (EPI != EPI_OUT) tma_store_2d(&g.o1, col, orow0, ebl);
+            bulk_commit();
+          }
+        } else if (EPI == EPI_OUT) {
           float4* o = reinterpret_cast<float4*>(static_cast<float*>(g.out0) + orow * g.ldo + col);
 #pragma unroll
-          for (int q = 0; q < 8; ++q)
-            o[q] = make_float4(__uint_as_float(r[4 * q]), __uint_as_float(r[4 * q + 1]),
-                               __uint_as_float(r[4 * q + 2]), __uint_as_float(r[4 * q + 3]));
+          for (int q = 0; q < 8; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        } else {
+          store32<PREC>(g.out0, g.out1, orow * g.ldo + col, v);
         }
       }
       if (EPI == EPI_FWD_LAST) g.epart[orow * (g.N / BN) + n_tile] = esum;
@@ -465,6 +554,10 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&acce[buf]);
+    }
+    if constexpr (PREC == TM_PREC_FP32) {
+      if (lane == 0) bulk_wait_all();
+      __syncwarp();
     }
   }
   tc_fence_before();
@@ -571,6 +664,9 @@ static int mlp_layers(tm_system* s, bool forward, bool backward) {
   const CUtensorMap* lvH[TM_MAX_HIDDEN][2] = {{&s->tm_H1[0], &s->tm_H1[1]},
                                               {&s->tm_H2[0], &s->tm_H2[1]}};
   void* bufH[TM_MAX_HIDDEN][2] = {{s->H1[0], s->H1[1]}, {s->H2[0], s->H2[1]}};
+  // 32-row store boxes of the same buffers (FP32 mode)
+  const CUtensorMap* stH[TM_MAX_HIDDEN][2] = {{&s->ts_H1[0], &s->ts_H1[1]},
+                                              {&s->ts_H2[0], &s->ts_H2[1]}};
   GemmArgs g;
   memset(&g, 0, sizeof(g));
   g.nele = m->k.nele;
@@ -595,6 +691,8 @@ static int mlp_layers(tm_system* s, bool forward, bool backward) {
     g.ldo = H;
     g.out0 = last ? s->G3[0] : bufH[l][0];
     g.out1 = last ? s->G3[1] : bufH[l][1];
+    g.o0 = last ? s->ts_G3[0] : *stH[l][0];
+    g.o1 = last ? s->ts_G3[1] : *stH[l][1];
     if ((rc = dispatch(ctx, prec, last ? EPI_FWD_LAST : EPI_FWD, g, mt))) return rc;
   }
   if (!backward) return TM_OK;
@@ -616,12 +714,15 @@ static int mlp_layers(tm_system* s, bool forward, bool backward) {
       g.hprev1 = bufH[l - 1][1];
       g.out0 = bufH[l - 1][0];
       g.out1 = bufH[l - 1][1];
+      g.o0 = *stH[l - 1][0];
+      g.o1 = *stH[l - 1][1];
       if ((rc = dispatch(ctx, prec, EPI_BWD, g, mt))) return rc;
     } else {
       g.N = Dp;
       g.ldo = Dp;
       g.out0 = s->dEdG;
       g.out1 = nullptr;
+      g.o0 = s->ts_dEdG;
       if ((rc = dispatch(ctx, prec, EPI_OUT, g, mt))) return rc;
     }
   }
@@ -676,7 +777,8 @@ int tm_gemm_selftest(tm_ctx* ctx, int prec, int M, int N, int K, const float* A,
   if ((rc = tm_make_tmap(ctx, &g.a0, da0, eb, 2 * (uint64_t)M, K, BM)) ||
       (rc = tm_make_tmap(ctx, &g.a1, prec == TM_PREC_FP32 ? da1 : da0, eb, 2 * (uint64_t)M, K, BM)) ||
       (rc = tm_make_tmap(ctx, &g.b0, db0, eb, 2 * (uint64_t)N, K, BN)) ||
-      (rc = tm_make_tmap(ctx, &g.b1, prec == TM_PREC_FP32 ? db1 : db0, eb, 2 * (uint64_t)N, K, BN)))
+      (rc = tm_make_tmap(ctx, &g.b1, prec == TM_PREC_FP32 ? db1 : db0, eb, 2 * (uint64_t)N, K, BN)) ||
+      (prec == TM_PREC_FP32 && (rc = tm_make_tmap(ctx, &g.o0, dc, 4, 2 * (uint64_t)M, N, 32))))
     return rc;
   g.K = K; g.N = N; g.a_net_rows = M; g.nele = 1; g.tile_elem = dte; g.Mpad = M;
   g.out0 = dc; g.out1 = dc1; g.ldo = N; g.st = st;
