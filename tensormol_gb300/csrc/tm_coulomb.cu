@@ -314,7 +314,9 @@ __global__ void __launch_bounds__(128, 6) k_coulomb(const CoulArgs a, const tm_c
   __syncthreads();
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int wg = blockIdx.x * (blockDim.x >> 5) + wib;
-  const int b = wg / TM_EE_SPLIT, split = wg % TM_EE_SPLIT;
+  // split-major: the warps of a CTA share a stencil share (similar work) and
+  // take neighbouring centre blocks
+  const int split = wg / a.blk_cap, b = wg % a.blk_cap;
   if (b >= a.blk_cap || b >= *a.nblk) return;
   const int4 bk = a.blk[b];
   const int head = bk.x, t0 = bk.y, t1 = bk.z;

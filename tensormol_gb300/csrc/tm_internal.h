@@ -15,7 +15,8 @@
 #define TM_MAX_HIDDEN 4
 #define TM_BN 256          // padding of the hidden width H and descriptor width Dp
 #define TM_BM 128          // GEMM M tile (rows per element are padded to this)
-#define TM_EE_SPLIT 16     // warps sharing one centre block's half stencil
+#define TM_EE_SPLIT 25     // warps sharing one centre block's half stencil (one
+                           // (x, y) column each at a 3-cell reach)
 
 // Constants of the model read by the device kernels (passed by value).
 struct tm_consts {
