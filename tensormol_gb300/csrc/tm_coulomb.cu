@@ -49,7 +49,7 @@ __global__ void k_mlp_finish(const float* __restrict__ epart, const double* __re
 }
 
 // Per-molecule sums in two fixed-order levels: one block per chunk of at most
-// 1024 atoms of one molecule, then one thread per molecule over its chunks.
+// 1024 atoms of one molecule, then one warp per molecule over its chunks.
 template <int NV>
 __device__ __forceinline__ void block_sum_store(double (&v)[NV], double* __restrict__ dst) {
   __shared__ double sh[NV][256];
@@ -76,17 +76,31 @@ __global__ void k_chunk_sum1(const int2* __restrict__ chunk, const double* __res
   block_sum_store<2>(v, part + 8 * (size_t)blockIdx.x);
 }
 
+// One warp per molecule: lane l adds chunks l, l + 32, ...; the lanes are then
+// combined by a fixed xor butterfly (same order every call).
+template <int NV>
+__device__ __forceinline__ void warp_chunk_sum(const int32_t* __restrict__ mol_chunk,
+                                               const double* __restrict__ part, int m, int lane,
+                                               const int (&slot)[NV], double (&v)[NV]) {
+  for (int t = 0; t < NV; ++t) v[t] = 0.0;
+  for (int c = mol_chunk[m] + lane; c < mol_chunk[m + 1]; c += 32)
+    for (int t = 0; t < NV; ++t) v[t] += part[8 * (size_t)c + slot[t]];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    for (int t = 0; t < NV; ++t) v[t] += __shfl_xor_sync(TM_FULL, v[t], o);
+}
+
 __global__ void k_mol_final1(const int32_t* __restrict__ mol_chunk, const double* __restrict__ part,
                              double* __restrict__ molE, double* __restrict__ aux, int nmol) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  const int m = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (m >= nmol) return;
-  double e = 0.0, q = 0.0;
-  for (int c = mol_chunk[m]; c < mol_chunk[m + 1]; ++c) {
-    e += part[8 * (size_t)c];
-    q += part[8 * (size_t)c + 1];
+  const int slot[2] = {0, 1};
+  double v[2];
+  warp_chunk_sum<2>(mol_chunk, part, m, lane, slot, v);
+  if (lane == 0) {
+    molE[4 * m + 1] = v[0];
+    aux[8 * m + 0] = v[1];
   }
-  molE[4 * m + 1] = e;
-  aux[8 * m + 0] = q;
 }
 
 __global__ void k_neutralize(const int32_t* __restrict__ mol, const int32_t* __restrict__ off,
@@ -482,18 +496,20 @@ __global__ void k_chunk_sum2(const int2* __restrict__ chunk, const double* __res
 
 __global__ void k_mol_final2(const int32_t* __restrict__ mol_chunk, const double* __restrict__ part,
                              double* __restrict__ molE, double* __restrict__ aux, int nmol) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  const int m = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (m >= nmol) return;
-  double v[6] = {0, 0, 0, 0, 0, 0};
-  for (int c = mol_chunk[m]; c < mol_chunk[m + 1]; ++c)
-    for (int t = 0; t < 6; ++t) v[t] += part[8 * (size_t)c + t];
-  molE[4 * m + 2] = v[0];
-  molE[4 * m + 3] = v[1];
-  molE[4 * m + 0] = molE[4 * m + 1] + v[0] + v[1];
-  aux[8 * m + 1] = v[2];
-  aux[8 * m + 2] = v[3];
-  aux[8 * m + 3] = v[4];
-  aux[8 * m + 4] = v[5];
+  const int slot[6] = {0, 1, 2, 3, 4, 5};
+  double v[6];
+  warp_chunk_sum<6>(mol_chunk, part, m, lane, slot, v);
+  if (lane == 0) {
+    molE[4 * m + 2] = v[0];
+    molE[4 * m + 3] = v[1];
+    molE[4 * m + 0] = molE[4 * m + 1] + v[0] + v[1];
+    aux[8 * m + 1] = v[2];
+    aux[8 * m + 2] = v[3];
+    aux[8 * m + 3] = v[4];
+    aux[8 * m + 4] = v[5];
+  }
 }
 
 // dE/dq_i = dE/dq~_i - (1/N) sum_k dE/dq~_k (adjoint of the neutralisation)
@@ -518,7 +534,7 @@ int tm_launch_mlp_finish(tm_system* s) {
       s->epart, m->bout, s->row_of_atom, s->d_elem, nsplit, s->Mpad, m->k.nele, s->N, s->d_Eatom,
       s->d_qraw);
   k_chunk_sum1<<<s->nchunk, 256, 0, ctx->stream>>>(s->d_chunk, s->d_Eatom, s->d_qraw, s->d_part);
-  k_mol_final1<<<tm_div_up(s->nmol, 128), 128, 0, ctx->stream>>>(s->d_mol_chunk, s->d_part,
+  k_mol_final1<<<tm_div_up(s->nmol, 4), 128, 0, ctx->stream>>>(s->d_mol_chunk, s->d_part,
                                                                  s->d_mol_E, s->d_mol_aux, s->nmol);
   k_neutralize<<<tm_div_up(s->N, 256), 256, 0, ctx->stream>>>(s->d_mol, s->d_off, s->d_qraw,
                                                               s->d_mol_aux, s->d_q, s->d_epos,
@@ -557,7 +573,7 @@ int tm_launch_coulomb(tm_system* s, unsigned flags) {
   ctx->launches += 2;
   k_chunk_sum2<<<s->nchunk, 256, 0, ctx->stream>>>(s->d_chunk, s->d_ecv, s->d_dEdq, s->d_q,
                                                    s->d_x, 1.889725989, s->d_part);
-  k_mol_final2<<<tm_div_up(s->nmol, 128), 128, 0, ctx->stream>>>(s->d_mol_chunk, s->d_part,
+  k_mol_final2<<<tm_div_up(s->nmol, 4), 128, 0, ctx->stream>>>(s->d_mol_chunk, s->d_part,
                                                                  s->d_mol_E, s->d_mol_aux, s->nmol);
   k_dq<<<tm_div_up(s->N, 256), 256, 0, ctx->stream>>>(s->d_mol, s->d_off, s->d_mol_aux, s->d_dEdq,
                                                       s->N);

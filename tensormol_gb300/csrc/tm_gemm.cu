@@ -466,6 +466,25 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
             }
           }
         }
+        // bias and output weights of these 32 columns (same for every row):
+        // vector loads issued before the tensor-memory reads
+        float bq[32], wq[32];
+        if (EPI == EPI_FWD || EPI == EPI_FWD_LAST) {
+          const float4* b4 = reinterpret_cast<const float4*>(g.bias + pblk + col);
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const float4 u = __ldg(b4 + q);
+            bq[4 * q] = u.x; bq[4 * q + 1] = u.y; bq[4 * q + 2] = u.z; bq[4 * q + 3] = u.w;
+          }
+        }
+        if (EPI == EPI_FWD_LAST) {
+          const float4* w4 = reinterpret_cast<const float4*>(g.wout + pblk + col);
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const float4 u = __ldg(w4 + q);
+            wq[4 * q] = u.x; wq[4 * q + 1] = u.y; wq[4 * q + 2] = u.z; wq[4 * q + 3] = u.w;
+          }
+        }
         uint32_t r[32];
         tmem_ld32(tbase + (uint32_t)c, r);
         if (C::NACC == 2) {
@@ -477,16 +496,14 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
         }
         float v[32];
         if (EPI == EPI_FWD || EPI == EPI_FWD_LAST) {
-          const float* bias = g.bias + pblk + col;
 #pragma unroll
           for (int q = 0; q < 32; ++q) {
-            const float z = __uint_as_float(r[q]) + __ldg(bias + q);
+            const float z = __uint_as_float(r[q]) + bq[q];
             if (EPI == EPI_FWD) {
               v[q] = act_f<ACT>(z, g.alpha);
             } else {
-              const float w = __ldg(g.wout + pblk + col + q);
-              esum += act_f<ACT>(z, g.alpha) * w;
-              v[q] = w * actd_z<ACT>(z, g.alpha);
+              esum += act_f<ACT>(z, g.alpha) * wq[q];
+              v[q] = wq[q] * actd_z<ACT>(z, g.alpha);
             }
           }
         } else if (EPI == EPI_BWD) {
