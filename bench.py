@@ -40,7 +40,7 @@ METRIC = "atom-steps/s E+F, fused adjoint vs plain autograd, 1 GB300; serve p50/
 UNIT = "atom-steps/s"
 # DRAM bytes of the six k_gemm launches of one evaluation (one ncu capture; the
 # k_gemm summary under profiles/ gives the command and the per-launch figures)
-GEMM_DRAM_BYTES_PER_STEP = 2_250_700_000
+GEMM_DRAM_BYTES_PER_STEP = 2_278_800_000
 WORKLOAD = ("water cube: 8,000 H2O = 24,000 atoms, open boundary, O on a 3.1 A lattice "
             "+-0.2 A jitter, single energy+force")
 
