@@ -20,7 +20,9 @@
 //   * the centre's own dE/dx_i,
 //   * one scalar per radial edge and one vector per angular edge for the
 //     neighbour side, gathered per atom through the reverse-edge index
-//     (no atomics on global memory: forces are deterministic).
+//     (no atomics anywhere: the angular edge vectors are summed in one
+//     shared-memory copy per 8-lane group, added in group order, so forces
+//     are deterministic).
 #include <cuda_runtime.h>
 
 #include "tm_internal.h"
@@ -112,6 +114,8 @@ __device__ __forceinline__ WarpSmem warp_smem(float* base, int Dp, int KA) {
 }
 
 __host__ __device__ __forceinline__ int smem_floats(int Dp, int KA) { return Dp + 9 * KA; }
+// adjoint: the row, six geometry arrays and a [4 groups][3][KA] accumulator
+__host__ __device__ __forceinline__ int smem_floats_adj(int Dp, int KA) { return Dp + 18 * KA; }
 
 // angular neighbour geometry + element segments; returns segment starts in seg[]
 __device__ __forceinline__ void load_angular(const DescArgs& a, const tm_consts& k, int i,
@@ -303,7 +307,11 @@ __global__ void __launch_bounds__(128) k_desc_adj(const DescArgs a, const tm_con
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * (blockDim.x >> 5) + wib;
   if (i >= a.N) return;
-  WarpSmem w = warp_smem(sh + (size_t)wib * smem_floats(k.Dp, a.KA), k.Dp, a.KA);
+  WarpSmem w = warp_smem(sh + (size_t)wib * smem_floats_adj(k.Dp, a.KA), k.Dp, a.KA);
+  // neighbour-side angular gradients: one copy per 8-lane group, so that no
+  // two lanes of an instruction update the same word (no atomics); the copies
+  // are added in group order at the end
+  float* vacc = w.fcd + a.KA;
   // upstream dE/dG for this centre: energy net + dE/dq * charge net
   const int row = a.row_of_atom[i];
   const float dq = a.dEdq[i];
@@ -348,7 +356,7 @@ __global__ void __launch_bounds__(128) k_desc_adj(const DescArgs a, const tm_con
   const int ca = a.cnt_a[i];
   int seg[TM_MAX_ELE + 1];
   load_angular(a, k, i, hi, lo, ca, w, seg, lane);
-  for (int s = lane; s < ca; s += 32) { w.vx[s] = 0.f; w.vy[s] = 0.f; w.vz[s] = 0.f; }
+  for (int s = lane; s < 12 * a.KA; s += 32) vacc[s] = 0.f;
   __syncwarp();
   const int grp = lane >> 3, q = lane & 7;
   const float cth = k.cos_th[q], sth = k.sin_th[q], rsq = k.rs_a[q];
@@ -448,16 +456,22 @@ __global__ void __launch_bounds__(128) k_desc_adj(const DescArgs a, const tm_con
             const float perp = bside ? (U1[e] * n2 - U2[e] * n1) : (n1 * U2[e] - n2 * U1[e]);
             const float g = dr * U0[e] + (kc / w.r[e]) * perp;
             fown += g;
-            float* V = d == 0 ? w.vx : (d == 1 ? w.vy : w.vz);
-            atomicAdd(&V[e], -g);
+            vacc[(grp * 3 + d) * a.KA + e] -= g;
           }
         }
+        __syncwarp();
       }
     }
   }
   __syncwarp();
-  for (int s = lane; s < ca; s += 32)
-    a.va[(size_t)i * a.KA + s] = make_float4(w.vx[s], w.vy[s], w.vz[s], 0.f);
+  for (int s = lane; s < ca; s += 32) {
+    float v[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      v[d] = ((vacc[d * a.KA + s] + vacc[(3 + d) * a.KA + s]) + vacc[(6 + d) * a.KA + s]) +
+             vacc[(9 + d) * a.KA + s];
+    a.va[(size_t)i * a.KA + s] = make_float4(v[0], v[1], v[2], 0.f);
+  }
   fx += (q == 0 || q == 3) ? fown : 0.f;
   fy += (q == 1 || q == 4) ? fown : 0.f;
   fz += (q == 2 || q == 5) ? fown : 0.f;
@@ -592,7 +606,7 @@ int tm_launch_adjoint(tm_system* s, unsigned flags) {
   tm_ctx* ctx = s->ctx;
   DescArgs a = make_desc_args(s);
   const tm_consts& k = s->model->k;
-  const size_t shm = (size_t)4 * smem_floats(k.Dp, s->KA) * sizeof(float);
+  const size_t shm = (size_t)4 * smem_floats_adj(k.Dp, s->KA) * sizeof(float);
   if (shm > 48 * 1024)
     cudaFuncSetAttribute(k_desc_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
   k_desc_adj<<<tm_div_up(s->N, 4), 128, shm, ctx->stream>>>(a, k);
