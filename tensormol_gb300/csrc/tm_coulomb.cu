@@ -209,8 +209,8 @@ __device__ __forceinline__ PairOut pair_terms(float r, float ir, float qi, float
     const float xr = R0 * inv;                        // (rp/R0)^-1
     const float x2 = xr * xr, x4 = x2 * x2, x12 = x4 * x4 * x4;
     const float damp = __fdividef(1.f, 1.f + 6.f * x12);
-    // x12 * damp = 1 / (1/x12 + 6): finite even where x12 overflows at contact
-    const float xdamp = __fdividef(1.f, __fdividef(1.f, x12) + 6.f);
+    // x12 * damp = (1 - damp) / 6: finite even where x12 overflows at contact
+    const float xdamp = (1.f - damp) * (1.f / 6.f);
     const float K = -cut * s6 * inv6 * damp;
     // d damp / d rp = 72 x12 / (rp (1 + 6 x12)^2)
     const float dK = -s6 * inv6 * damp * (dcut - 6.f * cut * inv + 72.f * cut * xdamp * inv);
