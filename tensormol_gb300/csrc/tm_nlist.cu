@@ -181,8 +181,11 @@ __global__ void k_grid_from_chunks(const float* __restrict__ cbox, const int32_t
                                    const int32_t* __restrict__ off, tm_grid* __restrict__ grid,
                                    int32_t* __restrict__ ncell_m, int nmol, double rc, int periodic,
                                    double Lx, double Ly, double Lz, double occ, double cap_a,
-                                   double cap_c, int pnx, int pny, int pnz) {
-  // one warp per molecule: lanes reduce the chunk boxes, lane 0 sizes the grid
+                                   double cap_c, int pnx, int pny, int pnz, int32_t* total,
+                                   int cap, tm_dev_status* st) {
+  // one warp per molecule: lanes reduce the chunk boxes, lane 0 sizes the grid;
+  // with one molecule (total != nullptr) it also writes the cell total that
+  // k_grid_offsets would
   const int m = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (m >= nmol) return;
   float mnf[3] = {3e38f, 3e38f, 3e38f}, mxf[3] = {-3e38f, -3e38f, -3e38f};
@@ -206,6 +209,10 @@ __global__ void k_grid_from_chunks(const float* __restrict__ cbox, const int32_t
                                    cap_a, cap_c, pnx, pny, pnz);
   grid[m] = g;
   ncell_m[m] = g.nx * g.ny * g.nz;
+  if (total) {
+    *total = g.nx * g.ny * g.nz;
+    if (g.nx * g.ny * g.nz > cap) tm_flag(st, TM_E_CAPACITY, g.nx * g.ny * g.nz, 2);
+  }
 }
 
 __device__ __forceinline__ int cell_coord(double v, double o, double c, int n) {
@@ -558,13 +565,23 @@ __global__ void __launch_bounds__(128) k_nbr_build(const NbrArgs a) {
 
 // Reverse edge index: for entry s of centre i (neighbour j at image r),
 // the position of i (at image 26 - r) in j's list.
-__global__ void k_nbr_reverse(const uint32_t* __restrict__ nbr, const int32_t* __restrict__ cnt,
-                              int32_t* __restrict__ rev, const int32_t* __restrict__ elem,
+// One launch for both lists: warps [0, N) take the radial rows, [N, 2N) the
+// angular rows.
+__global__ void k_nbr_reverse(const uint32_t* __restrict__ nbr_r, const int32_t* __restrict__ cnt_r,
+                              int32_t* __restrict__ rev_r, int KR,
+                              const uint32_t* __restrict__ nbr_a, const int32_t* __restrict__ cnt_a,
+                              int32_t* __restrict__ rev_a, int KA, const int32_t* __restrict__ elem,
                               const int32_t* __restrict__ mol, const int32_t* __restrict__ off,
-                              int N, int K) {
+                              int N) {
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int i = blockIdx.x * (blockDim.x >> 5) + wib;
-  if (i >= N) return;
+  const int w = blockIdx.x * (blockDim.x >> 5) + wib;
+  if (w >= 2 * N) return;
+  const bool ang = w >= N;
+  const int i = ang ? w - N : w;
+  const uint32_t* nbr = ang ? nbr_a : nbr_r;
+  const int32_t* cnt = ang ? cnt_a : cnt_r;
+  int32_t* rev = ang ? rev_a : rev_r;
+  const int K = ang ? KA : KR;
   const int ci = cnt[i];
   const int ei = elem[i];
   const int li = i - off[mol[i]];
@@ -821,7 +838,11 @@ int scan_exclusive(tm_ctx* ctx, const T* in, T* out, int64_t n, T* total_dev,
   // scratch (4096 entries) keeps the per-step scans free of allocations
   T* bsum = scratch;
   if (!bsum && tm_alloc(ctx, (void**)&bsum, sizeof(T) * (size_t)(nb > 0 ? nb : 1))) return TM_E_CUDA;
-  if (n > 0) {
+  if (n > 0 && nb == 1) {
+    // one block: its exclusive scan is the result and its sum the total
+    k_scan_blocks<T><<<1, 1024, 0, ctx->stream>>>(in, out, total_dev ? total_dev : bsum, n);
+    ctx->launches += 1;
+  } else if (n > 0) {
     k_scan_blocks<T><<<(unsigned)nb, 1024, 0, ctx->stream>>>(in, out, bsum, n);
     k_scan_top<T><<<1, 1024, 0, ctx->stream>>>(bsum, (int)nb, total_dev);
     k_scan_add<T><<<(unsigned)nb, 1024, 0, ctx->stream>>>(out, bsum, n);
@@ -984,11 +1005,14 @@ int tm_launch_nlist(tm_system* s) {
   k_cbox_chunks<<<s->nchunk, 256, 0, st>>>(s->d_chunk, s->d_xhi, s->d_cbox);
   k_grid_from_chunks<<<tm_div_up(s->nmol, 4), 128, 0, st>>>(
       s->d_cbox, s->d_mol_chunk, s->d_off, s->d_grid, s->d_ncell_m, s->nmol, k.r_rc_d + s->skin,
-      s->periodic ? 1 : 0, s->lat[0], s->lat[4], s->lat[8], 0.0, 2.0, 64.0, 0, 0, 0);
-  ctx->launches++;
-  k_grid_offsets<<<1, 32, 0, st>>>(s->d_grid, s->d_ncell_m, s->nmol, s->d_ncell, s->ncell_cap,
-                                   ctx->d_status);
+      s->periodic ? 1 : 0, s->lat[0], s->lat[4], s->lat[8], 0.0, 2.0, 64.0, 0, 0, 0,
+      s->nmol == 1 ? s->d_ncell : nullptr, s->ncell_cap, ctx->d_status);
   ctx->launches += 2;
+  if (s->nmol > 1) {
+    k_grid_offsets<<<1, 32, 0, st>>>(s->d_grid, s->d_ncell_m, s->nmol, s->d_ncell, s->ncell_cap,
+                                     ctx->d_status);
+    ctx->launches++;
+  }
   cudaMemsetAsync(s->d_cell_cnt, 0, sizeof(int32_t) * (s->ncell_cap + 1), st);
   k_cell_count<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_x, s->d_mol, s->d_grid, s->d_cell_cnt,
                                                       s->d_cell_of_atom, s->N, s->ncell_cap,
@@ -1038,23 +1062,26 @@ int tm_launch_nlist(tm_system* s) {
     s->cand_valid = true;
     s->cand_rebuild = false;
   }
-  k_nbr_reverse<<<tm_div_up(s->N, 4), 128, 0, st>>>(s->d_nbr_r, s->d_cnt_r, s->d_rev_r, s->d_elem,
-                                                    s->d_mol, s->d_off, s->N, s->KR);
-  k_nbr_reverse<<<tm_div_up(s->N, 4), 128, 0, st>>>(s->d_nbr_a, s->d_cnt_a, s->d_rev_a, s->d_elem,
-                                                    s->d_mol, s->d_off, s->N, s->KA);
-  ctx->launches += 2;
+  k_nbr_reverse<<<tm_div_up(2 * s->N, 4), 128, 0, st>>>(s->d_nbr_r, s->d_cnt_r, s->d_rev_r, s->KR,
+                                                        s->d_nbr_a, s->d_cnt_a, s->d_rev_a, s->KA,
+                                                        s->d_elem, s->d_mol, s->d_off, s->N);
+  ctx->launches += 1;
   // Coulomb grid: about 24 atoms per cell, atoms packed in cell order
   k_grid_from_chunks<<<tm_div_up(s->nmol, 4), 128, 0, st>>>(
       s->d_cbox, s->d_mol_chunk, s->d_off, s->d_egrid, s->d_encell_m, s->nmol, 2.0,
       s->periodic ? 1 : 0, s->lat[0], s->lat[4], s->lat[8], 24.0, 0.125, 8.0, s->ee_dims[0],
-      s->ee_dims[1], s->ee_dims[2]);
-  k_grid_offsets<<<1, 32, 0, st>>>(s->d_egrid, s->d_encell_m, s->nmol, s->d_encell, s->ecell_cap,
-                                   ctx->d_status);
+      s->ee_dims[1], s->ee_dims[2], s->nmol == 1 ? s->d_encell : nullptr, s->ecell_cap,
+      ctx->d_status);
+  if (s->nmol > 1) {
+    k_grid_offsets<<<1, 32, 0, st>>>(s->d_egrid, s->d_encell_m, s->nmol, s->d_encell, s->ecell_cap,
+                                     ctx->d_status);
+    ctx->launches++;
+  }
   cudaMemsetAsync(s->d_ecell_cnt, 0, sizeof(int32_t) * (s->ecell_cap + 1), st);
   k_cell_count<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_x, s->d_mol, s->d_egrid, s->d_ecell_cnt,
                                                       s->d_ecell_of_atom, s->N, s->ecell_cap,
                                                       ctx->d_status);
-  ctx->launches += 3;
+  ctx->launches += 2;
   if ((rc = scan_exclusive<int32_t>(ctx, s->d_ecell_cnt, s->d_ecell_start, s->ecell_cap + 1,
                                     nullptr, s->d_scan_tmp)))
     return rc;
@@ -1088,14 +1115,13 @@ int tm_launch_nlist_filter(tm_system* s) {
   if ((rc = tm_launch_positions(s))) return rc;
   if (!s->need_sticky) cudaMemsetAsync(s->d_need, 0, sizeof(int32_t) * 2, st);
   if ((rc = launch_filter(s))) return rc;
-  k_nbr_reverse<<<tm_div_up(s->N, 4), 128, 0, st>>>(s->d_nbr_r, s->d_cnt_r, s->d_rev_r, s->d_elem,
-                                                    s->d_mol, s->d_off, s->N, s->KR);
-  k_nbr_reverse<<<tm_div_up(s->N, 4), 128, 0, st>>>(s->d_nbr_a, s->d_cnt_a, s->d_rev_a, s->d_elem,
-                                                    s->d_mol, s->d_off, s->N, s->KA);
+  k_nbr_reverse<<<tm_div_up(2 * s->N, 4), 128, 0, st>>>(s->d_nbr_r, s->d_cnt_r, s->d_rev_r, s->KR,
+                                                        s->d_nbr_a, s->d_cnt_a, s->d_rev_a, s->KA,
+                                                        s->d_elem, s->d_mol, s->d_off, s->N);
   k_ee_pack<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_ecell_atoms, s->d_x, s->d_elem, s->d_mol,
                                                   s->d_egrid, s->d_ecell_of_atom, s->d_epos,
                                                   s->d_exhi, s->N);
-  ctx->launches += 3;
+  ctx->launches += 2;
   s->nlist_valid = true;
   return tm_cuda_check(ctx, cudaGetLastError(), "nlist filter");
 }
