@@ -88,6 +88,12 @@ extern "C" int tm_ctx_create(int device, size_t budget, tm_ctx** out) {
     return rc;
   }
   c->own_stream = true;
+  if ((rc = tm_cuda_check(c, cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking), "aux stream")) ||
+      (rc = tm_cuda_check(c, cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "event")) ||
+      (rc = tm_cuda_check(c, cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming), "event"))) {
+    delete c;
+    return rc;
+  }
   if ((rc = tm_cuda_check(c, cudaMalloc(&c->d_status, sizeof(tm_dev_status)), "status")) ||
       (rc = tm_cuda_check(c, cudaMallocHost(&c->h_status, sizeof(tm_dev_status)), "status")) ||
       (rc = tm_cuda_check(c, cudaMemset(c->d_status, 0, sizeof(tm_dev_status)), "status"))) {
@@ -107,9 +113,13 @@ extern "C" int tm_ctx_create(int device, size_t budget, tm_ctx** out) {
 extern "C" int tm_ctx_destroy(tm_ctx* c) {
   if (!c) return TM_OK;
   cudaStreamSynchronize(c->stream);
+  cudaStreamSynchronize(c->aux);
   cudaFree(c->d_status);
   cudaFreeHost(c->h_status);
   if (c->own_stream) cudaStreamDestroy(c->stream);
+  cudaStreamDestroy(c->aux);
+  cudaEventDestroy(c->ev_fork);
+  cudaEventDestroy(c->ev_join);
   delete c;
   return TM_OK;
 }
@@ -850,16 +860,37 @@ static int energy_force_pipeline(tm_system* s, unsigned flags, cudaEvent_t* ev) 
   if ((rc = tm_launch_descriptors(s))) return rc;
   if (ev) cudaEventRecord(ev[2], st);
   if (ev) {
+    // stage timing: one stream, in order
     if ((rc = tm_launch_mlp(s, false))) return rc;
     cudaEventRecord(ev[3], st);
     if (force && (rc = tm_launch_mlp_backward_only(s))) return rc;
     cudaEventRecord(ev[4], st);
-  } else if ((rc = tm_launch_mlp(s, force))) {
-    return rc;
+    if ((rc = tm_launch_mlp_finish(s))) return rc;
+    if ((rc = tm_launch_coulomb(s, flags))) return rc;
+    cudaEventRecord(ev[5], st);
+  } else {
+    if ((rc = tm_launch_mlp(s, false))) return rc;
+    if ((rc = tm_launch_mlp_finish(s))) return rc;
+    if (force) {
+      // The backward pass of both networks needs no pair term (dE/dq enters
+      // in the adjoint), so the pair terms run on the second stream beside it:
+      // the layer GEMMs wait on their operand ring and leave most issue slots
+      // free, the pair kernel is issue bound, and one of its blocks fits
+      // beside a GEMM CTA on every SM.
+      tm_ctx* ctx = s->ctx;
+      cudaEventRecord(ctx->ev_fork, st);
+      cudaStreamWaitEvent(ctx->aux, ctx->ev_fork, 0);
+      ctx->stream = ctx->aux;
+      rc = tm_launch_coulomb(s, flags);
+      ctx->stream = st;
+      cudaEventRecord(ctx->ev_join, ctx->aux);
+      if (!rc) rc = tm_launch_mlp_backward_only(s);
+      cudaStreamWaitEvent(st, ctx->ev_join, 0);   // joined even after an error
+      if (rc) return rc;
+    } else if ((rc = tm_launch_coulomb(s, flags))) {
+      return rc;
+    }
   }
-  if ((rc = tm_launch_mlp_finish(s))) return rc;
-  if ((rc = tm_launch_coulomb(s, flags))) return rc;
-  if (ev) cudaEventRecord(ev[5], st);
   if (force && (rc = tm_launch_adjoint(s, flags))) return rc;
   if (ev) cudaEventRecord(ev[6], st);
   return TM_OK;

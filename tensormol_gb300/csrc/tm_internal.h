@@ -53,6 +53,10 @@ struct tm_ctx {
   int num_sms = 1;                     // streaming multiprocessors of the device
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  // second stream of the library's own: the pair terms run on it beside the
+  // network backward pass (forked from and joined back into `stream`)
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   size_t budget = 0, in_use = 0;
   int64_t launches = 0;
   tm_dev_status* d_status = nullptr;
