@@ -227,7 +227,7 @@ __device__ __forceinline__ PairOut pair_terms(float r, float ir, float qi, float
 // about 1e-6 A. Candidate cells are culled by box distance; of their atoms,
 // those within the cutoff of the centres' bounding box are staged (compacted
 // by ballot, up to kStage at a time across columns) in shared memory.
-constexpr int kStage = 128;
+constexpr int kStage = 64;
 
 struct StageSmem {
   float4 p[kStage];                  // candidate position in the block frame (w = element)
