@@ -563,6 +563,8 @@ static int system_alloc(tm_system* s, int N_cap, int nmol_cap, int Mpad_cap, int
   A.get(&s->d_cell_of_atom, sizeof(int32_t) * N);
   A.get(&s->d_sort_tmp, sizeof(int32_t) * N);
   A.get(&s->d_scan_tmp, sizeof(int32_t) * 4096);
+  A.get(&s->d_sort_tmp2, sizeof(int32_t) * N);
+  A.get(&s->d_scan_tmp2, sizeof(int32_t) * 4096);
   A.get(&s->d_ccnt, sizeof(int32_t) * N);
   A.get(&s->d_cand, sizeof(uint32_t) * (size_t)N * s->KC);
   A.get(&s->d_need_c, sizeof(int32_t) * 2);
@@ -725,7 +727,7 @@ static void system_free(tm_system* s) {
                   s->d_off, s->d_x, s->d_xhi, s->d_xlo, s->d_x_at_build, s->d_grid, s->d_ncell, s->d_ncell_m, s->d_need,
                   s->d_chunk, s->d_mol_chunk, s->d_part, s->d_cbox,
                   s->d_egrid, s->d_encell, s->d_encell_m, s->d_ecell_cnt, s->d_ecell_start,
-                  s->d_ecell_atoms, s->d_ecell_of_atom, s->d_epos, s->d_exhi, s->d_exlo, s->d_sort_tmp, s->d_scan_tmp, s->d_ccnt, s->d_cand, s->d_need_c, s->d_disp,
+                  s->d_ecell_atoms, s->d_ecell_of_atom, s->d_epos, s->d_exhi, s->d_exlo, s->d_sort_tmp, s->d_scan_tmp, s->d_sort_tmp2, s->d_scan_tmp2, s->d_ccnt, s->d_cand, s->d_need_c, s->d_disp,
                   s->d_cacc, s->d_eblk, s->d_neblk,
                   s->d_cell_cnt, s->d_cell_start, s->d_cell_atoms, s->d_cell_of_atom, s->d_cnt_r,
                   s->d_cnt_a, s->d_nbr_r, s->d_nbr_a, s->d_rev_r, s->d_rev_a, s->d_sr, s->d_va,

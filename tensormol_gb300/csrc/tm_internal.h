@@ -130,6 +130,8 @@ struct tm_system {
   int32_t* d_cell_of_atom = nullptr;   // [N]
   int32_t* d_sort_tmp = nullptr;       // [N] scratch of the cell sort (crowded cells)
   int32_t* d_scan_tmp = nullptr;       // [4096] block sums of the cell-count scans
+  int32_t* d_sort_tmp2 = nullptr;      // [N], [4096]: the same for the Coulomb grid, which
+  int32_t* d_scan_tmp2 = nullptr;      //   is built on the second stream
   // coarser grid for the Coulomb/vdW pair terms (about 24 atoms per cell)
   int ee_dims[3] = {0, 0, 0};          // periodic: host-chosen cells per edge
   int ecell_cap = 0;

@@ -992,6 +992,48 @@ int tm_launch_positions(tm_system* s) {
   return tm_cuda_check(ctx, cudaGetLastError(), "positions");
 }
 
+// The Coulomb grid: about 24 atoms per cell, atoms packed in cell order, and
+// the table of centre blocks. Enqueued on the ctx's second stream (which
+// `ctx->stream` names while this runs); needs only positions and chunk boxes.
+static int launch_ee_grid(tm_system* s) {
+  tm_ctx* ctx = s->ctx;
+  cudaStream_t st = ctx->stream;
+  int rc;
+  k_grid_from_chunks<<<tm_div_up(s->nmol, 4), 128, 0, st>>>(
+      s->d_cbox, s->d_mol_chunk, s->d_off, s->d_egrid, s->d_encell_m, s->nmol, 2.0,
+      s->periodic ? 1 : 0, s->lat[0], s->lat[4], s->lat[8], 24.0, 0.125, 8.0, s->ee_dims[0],
+      s->ee_dims[1], s->ee_dims[2], s->nmol == 1 ? s->d_encell : nullptr, s->ecell_cap,
+      ctx->d_status);
+  if (s->nmol > 1) {
+    k_grid_offsets<<<1, 32, 0, st>>>(s->d_egrid, s->d_encell_m, s->nmol, s->d_encell, s->ecell_cap,
+                                     ctx->d_status);
+    ctx->launches++;
+  }
+  cudaMemsetAsync(s->d_ecell_cnt, 0, sizeof(int32_t) * (s->ecell_cap + 1), st);
+  k_cell_count<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_x, s->d_mol, s->d_egrid, s->d_ecell_cnt,
+                                                      s->d_ecell_of_atom, s->N, s->ecell_cap,
+                                                      ctx->d_status);
+  ctx->launches += 2;
+  if ((rc = scan_exclusive<int32_t>(ctx, s->d_ecell_cnt, s->d_ecell_start, s->ecell_cap + 1,
+                                    nullptr, s->d_scan_tmp2)))
+    return rc;
+  cudaMemsetAsync(s->d_ecell_cnt, 0, sizeof(int32_t) * (s->ecell_cap + 1), st);
+  k_cell_fill<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_ecell_of_atom, s->d_ecell_start,
+                                                     s->d_ecell_cnt, s->d_ecell_atoms, s->N);
+  k_cell_sort<<<tm_div_up(s->ecell_cap, 4), 128, 0, st>>>(s->d_ecell_start, s->d_ecell_atoms,
+                                                            s->d_sort_tmp2, s->d_encell, s->ecell_cap);
+  k_ee_pack<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_ecell_atoms, s->d_x, s->d_elem, s->d_mol,
+                                                  s->d_egrid, s->d_ecell_of_atom, s->d_epos,
+                                                  s->d_exhi, s->N);
+  cudaMemsetAsync(s->d_neblk, 0, sizeof(int32_t), st);
+  k_ee_blocks<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_ecell_atoms, s->d_mol, s->d_egrid,
+                                                    s->d_ecell_of_atom, s->d_ecell_start,
+                                                    s->d_eblk, s->d_neblk, s->N,
+                                                    s->N / 32 + s->ecell_cap + 1, ctx->d_status);
+  ctx->launches += 4;
+  return tm_cuda_check(ctx, cudaGetLastError(), "coulomb grid");
+}
+
 // Bins atoms and builds both neighbour lists on the ctx stream without any
 // host synchronisation. A centre with more neighbours than its row capacity
 // records the count it needed in s->d_need; tm_nlist_grow() checks that after
@@ -1003,6 +1045,18 @@ int tm_launch_nlist(tm_system* s) {
   int rc;
   if ((rc = tm_launch_positions(s))) return rc;
   k_cbox_chunks<<<s->nchunk, 256, 0, st>>>(s->d_chunk, s->d_xhi, s->d_cbox);
+  // the Coulomb grid on the second stream, beside the neighbour rows; joined
+  // before this function returns
+  cudaEventRecord(ctx->ev_fork, st);
+  cudaStreamWaitEvent(ctx->aux, ctx->ev_fork, 0);
+  ctx->stream = ctx->aux;
+  rc = launch_ee_grid(s);
+  ctx->stream = st;
+  cudaEventRecord(ctx->ev_join, ctx->aux);
+  if (rc) {
+    cudaStreamWaitEvent(st, ctx->ev_join, 0);
+    return rc;
+  }
   k_grid_from_chunks<<<tm_div_up(s->nmol, 4), 128, 0, st>>>(
       s->d_cbox, s->d_mol_chunk, s->d_off, s->d_grid, s->d_ncell_m, s->nmol, k.r_rc_d + s->skin,
       s->periodic ? 1 : 0, s->lat[0], s->lat[4], s->lat[8], 0.0, 2.0, 64.0, 0, 0, 0,
@@ -1066,39 +1120,7 @@ int tm_launch_nlist(tm_system* s) {
                                                         s->d_nbr_a, s->d_cnt_a, s->d_rev_a, s->KA,
                                                         s->d_elem, s->d_mol, s->d_off, s->N);
   ctx->launches += 1;
-  // Coulomb grid: about 24 atoms per cell, atoms packed in cell order
-  k_grid_from_chunks<<<tm_div_up(s->nmol, 4), 128, 0, st>>>(
-      s->d_cbox, s->d_mol_chunk, s->d_off, s->d_egrid, s->d_encell_m, s->nmol, 2.0,
-      s->periodic ? 1 : 0, s->lat[0], s->lat[4], s->lat[8], 24.0, 0.125, 8.0, s->ee_dims[0],
-      s->ee_dims[1], s->ee_dims[2], s->nmol == 1 ? s->d_encell : nullptr, s->ecell_cap,
-      ctx->d_status);
-  if (s->nmol > 1) {
-    k_grid_offsets<<<1, 32, 0, st>>>(s->d_egrid, s->d_encell_m, s->nmol, s->d_encell, s->ecell_cap,
-                                     ctx->d_status);
-    ctx->launches++;
-  }
-  cudaMemsetAsync(s->d_ecell_cnt, 0, sizeof(int32_t) * (s->ecell_cap + 1), st);
-  k_cell_count<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_x, s->d_mol, s->d_egrid, s->d_ecell_cnt,
-                                                      s->d_ecell_of_atom, s->N, s->ecell_cap,
-                                                      ctx->d_status);
-  ctx->launches += 2;
-  if ((rc = scan_exclusive<int32_t>(ctx, s->d_ecell_cnt, s->d_ecell_start, s->ecell_cap + 1,
-                                    nullptr, s->d_scan_tmp)))
-    return rc;
-  cudaMemsetAsync(s->d_ecell_cnt, 0, sizeof(int32_t) * (s->ecell_cap + 1), st);
-  k_cell_fill<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_ecell_of_atom, s->d_ecell_start,
-                                                     s->d_ecell_cnt, s->d_ecell_atoms, s->N);
-  k_cell_sort<<<tm_div_up(s->ecell_cap, 4), 128, 0, st>>>(s->d_ecell_start, s->d_ecell_atoms,
-                                                            s->d_sort_tmp, s->d_encell, s->ecell_cap);
-  k_ee_pack<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_ecell_atoms, s->d_x, s->d_elem, s->d_mol,
-                                                  s->d_egrid, s->d_ecell_of_atom, s->d_epos,
-                                                  s->d_exhi, s->N);
-  cudaMemsetAsync(s->d_neblk, 0, sizeof(int32_t), st);
-  k_ee_blocks<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_ecell_atoms, s->d_mol, s->d_egrid,
-                                                    s->d_ecell_of_atom, s->d_ecell_start,
-                                                    s->d_eblk, s->d_neblk, s->N,
-                                                    s->N / 32 + s->ecell_cap + 1, ctx->d_status);
-  ctx->launches += 4;
+  cudaStreamWaitEvent(st, ctx->ev_join, 0);   // the Coulomb grid (second stream)
   if (s->skin <= 0.0)
     cudaMemcpyAsync(s->d_x_at_build, s->d_x, sizeof(double) * 3 * s->N, cudaMemcpyDeviceToDevice, st);
   s->nlist_valid = true;
