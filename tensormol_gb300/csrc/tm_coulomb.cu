@@ -182,10 +182,20 @@ __device__ __forceinline__ PairOut pair_terms(float r, float ir, float qi, float
         dkc = 0.f;
       } else {
         const float ar = k.alpha * rb;
-        const float ec = erfcf(ar);
+        const float ex2 = expf(-ar * ar);
+        float ec;
+        if (k.erfc_n) {   // exp(-x^2) erfcx(x), erfcx by its polynomial on this range
+          const float t = fmaf(ar, k.erfc_s, k.erfc_o);
+          float pp = k.erfc_c[10];
+#pragma unroll
+          for (int e = 9; e >= 0; --e) pp = fmaf(pp, t, k.erfc_c[e]);
+          ec = ex2 * pp;
+        } else {
+          ec = erfcf(ar);
+        }
         const float irb = ir * a.inv_bohr;
         kc = ec * irb - k.zz + (rb - k.r_lr) * a.c_lin;
-        dkc = a.c_lin - irb * (ec * irb + 1.1283791671f * k.alpha * expf(-ar * ar));
+        dkc = a.c_lin - irb * (ec * irb + 1.1283791671f * k.alpha * ex2);
       }
     } else {
       const float ex = expf(rb - k.r_sr);

@@ -31,6 +31,11 @@ struct tm_consts {
   // Coulomb / vdW (atomic units, see params.coulomb_constants)
   float bohr, alpha, r_lr, r_sr, elu_shift, elu_a, zz, yy;
   float vdw_width, vdw_begin;
+  // erfc(x) = exp(-x^2) P(t) on the DSF range x = alpha r, r in [r_sr, r_lr]:
+  // P interpolates erfcx at Chebyshev nodes, t = x erfc_s + erfc_o in [-1, 1];
+  // erfc_n = 0: the range needs more than degree 10 (erfcf is used instead)
+  float erfc_c[11], erfc_s, erfc_o;
+  int erfc_n;
   float c6[TM_MAX_ELE], r0[TM_MAX_ELE];
   double r_rc_d, a_rc_d, ree_d;             // membership radii (FP64 test)
   float ree;
