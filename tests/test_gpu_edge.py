@@ -123,3 +123,46 @@ def test_malformed_systems_are_rejected(gpu):
         m.system(x, np.array([8, 1, 6]), None)                         # element not in the model
     with pytest.raises(TmError):
         m.system(x, np.array([8, 1, 1]), np.array([0, 4]))             # offsets beyond natoms
+
+
+def test_pair_sums_are_bit_reproducible(gpu):
+    """The pair-term sums are 64-bit fixed point added by integer atomics from
+    many warps, and the pair terms run on a second stream beside the network
+    backward pass: repeated evaluations, on the same system and on a new one,
+    give bit-identical energies and forces."""
+    w = systems.water(1000, seed=3, spacing=3.1)
+    m, _ = _model(gpu, [1, 8])
+    s = m.system(w.x, w.Z, w.offsets)
+    a = s.energy_force(w.x, True)
+    b = s.energy_force(w.x, True)
+    s.close()
+    s2 = m.system(w.x, w.Z, w.offsets)
+    c = s2.energy_force(w.x, True)
+    s2.close()
+    for key in ("Etotal", "force"):
+        assert np.array_equal(a[key], b[key]) and np.array_equal(a[key], c[key]), key
+
+
+def test_pair_sums_out_of_range_are_reported(gpu):
+    """Charge networks whose outputs are absurd (|q| ~ 1e19) drive the pair
+    sums past the fixed-point range: the evaluation fails with a status
+    naming the pair terms, and the context stays usable."""
+    from tensormol_gb300._lib import TmError
+    w = systems.water_cluster_60(seed=0)
+    p = dict(PARAMS)
+    p["NeuronType"] = "sigmoid_with_param"
+    W = systems.random_weights([1, 8], descriptor_width(2), seed=7)
+    for e, shift in ((1, 1e19), (8, -2e19)):
+        Wl, bl = W["Q"][e][-1]
+        W["Q"][e][-1] = (Wl, bl + shift)
+    bad = gpu.BPEEModel([1, 8], W, params=p, precision="fp32")
+    s = bad.system(w.x, w.Z, w.offsets)
+    with pytest.raises(TmError, match="pair terms"):
+        s.energy_force(w.x, True)
+    s.close()
+    m, om = _model(gpu, [1, 8])
+    s = m.system(w.x, w.Z, w.offsets)
+    out = s.energy_force(w.x, True)
+    ref = orc.OpenSystemOracle(om, w.x, w.Z, w.offsets).terms(w.x)
+    _check(out, ref, w.offsets)
+    s.close()
