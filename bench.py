@@ -407,6 +407,12 @@ def time_serving(max_atoms=32768, max_mols=256, loads=(0.25, 0.5, 1.1, 1.5, 3.0)
         wall = srv.run_arrivals(reqs)
         st = srv.stats(wall)
         lat = np.array([(r.t_done - r.t_submit) * 1e3 for r in reqs])
+        info = np.array(srv.step_info, dtype=float)          # relayout?, layout ms, step ms, atoms
+        split = {"relayout_step_fraction": float(info[:, 0].mean()),
+                 "layout_ms_p50": float(np.percentile(info[:, 1], 50)),
+                 "layout_ms_p99": float(np.percentile(info[:, 1], 99)),
+                 "compute_ms_p50": float(np.percentile(info[:, 2], 50)),
+                 "compute_ms_p99": float(np.percentile(info[:, 2], 99))}
         srv.close()
         sweep.append({"offered_load_vs_offline": load, "arrival_rate_per_s": lam,
                       "atom_steps_per_s": st["atom_steps_per_s"],
@@ -415,7 +421,8 @@ def time_serving(max_atoms=32768, max_mols=256, loads=(0.25, 0.5, 1.1, 1.5, 3.0)
                       "p99_over_p50": st["p99_ms"] / st["p50_ms"],
                       "mean_batch_atoms": st["mean_batch_atoms"],
                       "request_latency_p50_ms": float(np.percentile(lat, 50)),
-                      "request_latency_p99_ms": float(np.percentile(lat, 99))})
+                      "request_latency_p99_ms": float(np.percentile(lat, 99)),
+                      "step_split": split})
     model.close()
     return {"requests": len(specs), "atom_steps": int(work),
             "kinds": {k: sum(1 for sp in specs if sp[2] == k) for k in ("md", "opt", "ef")},

@@ -553,23 +553,49 @@ static int upload_layout(tm_system* s, SysLayout& L) {
   s->nlist_valid = false;
   cudaStream_t st = ctx->stream;
   const int N = L.N, nmol = L.nmol;
-  cudaMemcpyAsync(s->row_of_atom, L.row_of_atom.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(s->atom_of_row, L.atom_of_row.data(), sizeof(int32_t) * L.Mpad, cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(s->tile_elem, L.tile_elem.data(), sizeof(int32_t) * L.ntiles, cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(s->d_Z, L.Z.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(s->d_elem, L.elem.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(s->d_mol, L.mol.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(s->d_off, L.off32.data(), sizeof(int32_t) * (nmol + 1), cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(s->d_chunk, L.chunks.data(), sizeof(int2) * L.nchunk, cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(s->d_mol_chunk, L.mol_chunk.data(), sizeof(int32_t) * (nmol + 1),
-                  cudaMemcpyHostToDevice, st);
+  // The tables go through one pinned staging buffer of the system (no
+  // pageable-copy staging, no stream sync); before it is refilled, the copies
+  // of the previous upload are waited for (normally long done).
+  struct Part { void* dst; const void* src; size_t bytes; };
+  const Part parts[] = {
+      {s->row_of_atom, L.row_of_atom.data(), sizeof(int32_t) * N},
+      {s->atom_of_row, L.atom_of_row.data(), sizeof(int32_t) * L.Mpad},
+      {s->tile_elem, L.tile_elem.data(), sizeof(int32_t) * L.ntiles},
+      {s->d_Z, L.Z.data(), sizeof(int32_t) * N},
+      {s->d_elem, L.elem.data(), sizeof(int32_t) * N},
+      {s->d_mol, L.mol.data(), sizeof(int32_t) * N},
+      {s->d_off, L.off32.data(), sizeof(int32_t) * (nmol + 1)},
+      {s->d_chunk, L.chunks.data(), sizeof(int2) * L.nchunk},
+      {s->d_mol_chunk, L.mol_chunk.data(), sizeof(int32_t) * (nmol + 1)}};
+  size_t total = 0;
+  for (const Part& p : parts) total += (p.bytes + 15) & ~(size_t)15;
+  int rc;
+  if (s->stage_ev && (rc = tm_cuda_check(ctx, cudaEventSynchronize(s->stage_ev), "upload staging")))
+    return rc;
+  if (total > s->h_stage_bytes) {
+    if (s->h_stage) cudaFreeHost(s->h_stage);
+    s->h_stage = nullptr;
+    s->h_stage_bytes = 0;
+    if ((rc = tm_cuda_check(ctx, cudaMallocHost(&s->h_stage, total), "upload staging"))) return rc;
+    s->h_stage_bytes = total;
+  }
+  if (!s->stage_ev &&
+      (rc = tm_cuda_check(ctx, cudaEventCreateWithFlags(&s->stage_ev, cudaEventDisableTiming), "event")))
+    return rc;
+  size_t o = 0;
+  for (const Part& p : parts) {
+    uint8_t* h = static_cast<uint8_t*>(s->h_stage) + o;
+    memcpy(h, p.src, p.bytes);
+    if (p.bytes) cudaMemcpyAsync(p.dst, h, p.bytes, cudaMemcpyHostToDevice, st);
+    o += (p.bytes + 15) & ~(size_t)15;
+  }
+  cudaEventRecord(s->stage_ev, st);
   const bool split = m->desc.precision == TM_PREC_FP32;
   const int words = (int)(m->k.Dp * m->elem_size / 4);
   k_zero_pad_rows<<<L.Mpad, 128, 0, st>>>(s->atom_of_row, L.Mpad, m->k.Dp, (float*)s->G[0],
                                           split ? (float*)s->G[1] : nullptr, words);
   ctx->launches++;
-  // the host tables must outlive the copies
-  return tm_cuda_check(ctx, cudaStreamSynchronize(st), "system upload");
+  return tm_cuda_check(ctx, cudaGetLastError(), "system upload");
 }
 
 // Device buffers for up to N_cap atoms / nmol_cap molecules and the given
@@ -790,6 +816,10 @@ static void system_free(tm_system* s) {
   }
   ctx->in_use -= std::min(ctx->in_use, s->bytes);
   cudaStreamSynchronize(ctx->stream);
+  if (s->h_stage) cudaFreeHost(s->h_stage);
+  if (s->stage_ev) cudaEventDestroy(s->stage_ev);
+  s->h_stage = nullptr;
+  s->stage_ev = nullptr;
   delete s;
 }
 

@@ -151,6 +151,9 @@ struct tm_system {
   float4* d_exhi = nullptr;            // [N] cell-ordered hi parts (w = element)
   float4* d_exlo = nullptr;            // [N] cell-ordered lo parts (w = charge)
   unsigned long long* d_cacc = nullptr; // [5][N] pair-term fixed-point sums (cell order)
+  void* h_stage = nullptr;             // pinned staging of the layout tables
+  size_t h_stage_bytes = 0;
+  cudaEvent_t stage_ev = nullptr;      // the staging buffer's copies are done
   int4* d_eblk = nullptr;              // [N/32 + ecell + 1] centre blocks: (column head cell,
                                        //   first atom, end atom) in cell order
   int32_t* d_neblk = nullptr;          // number of centre blocks (device scalar)

@@ -21,6 +21,8 @@
 
 #include <vector>
 
+#include <algorithm>
+
 #include "tm_internal.h"
 
 struct tm_serve {
@@ -341,9 +343,12 @@ extern "C" int tm_serve_layout(tm_serve* sv, int nmol, const int32_t* Z, const i
   std::vector<int32_t> msrc(nmol, -1);
   for (int q = 0; q < nmol; ++q) {
     const int first = src[offsets[q]];
-    if (first >= 0)
-      for (int o = 0; o < s->nmol; ++o)
-        if (first >= s->off[o] && first < s->off[o + 1]) { msrc[q] = o; break; }
+    if (first >= 0 && s->nmol > 0) {
+      // the old molecule whose rows contain `first` (offsets are increasing)
+      const auto it = std::upper_bound(s->off.begin(), s->off.begin() + s->nmol + 1, (int64_t)first);
+      const int o = (int)(it - s->off.begin()) - 1;
+      if (o >= 0 && o < s->nmol) msrc[q] = o;
+    }
   }
   cudaStream_t st = ctx->stream;
   int rc;
@@ -368,7 +373,8 @@ extern "C" int tm_serve_layout(tm_serve* sv, int nmol, const int32_t* Z, const i
   std::swap(s->d_x, sv->x2);
   std::swap(sv->v, sv->v2);
   std::swap(sv->a, sv->a2);
-  return tm_sync_status(ctx, "serve layout");
+  // device errors of the gathers surface at the next step's status check
+  return tm_cuda_check(ctx, cudaGetLastError(), "serve layout");
 }
 
 extern "C" int tm_serve_step(tm_serve* sv, double* E_out, double* fmax_out) {
