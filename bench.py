@@ -52,6 +52,19 @@ def _dist():
     return ws, rank, local
 
 
+def aggregate_ranks(ms, natoms, ws, device="cuda"):
+    """Replicas over ws ranks (one per GPU, each timing the same workload on
+    its own device): the step time is the maximum over ranks and the value
+    counts every rank's atoms. Needs an initialised process group when ws > 1
+    (NCCL on GPUs; gloo with device="cpu")."""
+    if ws > 1:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, ws * natoms / (ms / 1000.0)
+
+
 def _peaks():
     p = os.path.join(HERE, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -519,12 +532,7 @@ def main():
         torch.distributed.barrier()
     torch.cuda.synchronize()
     s, times, launches, clocks, E, F = time_fused_device(model, w, args.steps, args.warmup, flush, torch)
-    ms = sum(times) / len(times)
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * w.natoms / (ms / 1000.0)
+    ms, value = aggregate_ranks(sum(times) / len(times), w.natoms, ws)
     if args.fused_only:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,

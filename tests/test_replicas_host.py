@@ -1,0 +1,55 @@
+"""Multi-process path of bench.py on CPU (gloo, world size 2): the step time
+is the maximum over ranks and the value counts every rank's atoms; under
+torchrun the reference arm runs on rank 0 only. No GPU: the per-rank step
+times are planted."""
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank, ws, port, q):
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=ws)
+    sys.path.insert(0, ROOT)
+    import bench
+    ms, value = bench.aggregate_ranks(1.0 + rank, 24000, ws, device="cpu")
+    q.put((rank, ms, value))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_replica_aggregation_two_ranks():
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    for rank, ms, value in out:
+        assert ms == 2.0                                # the slower rank's time
+        assert value == pytest.approx(2 * 24000 / 2e-3)  # both ranks' atoms
+
+
+def test_reference_arm_runs_on_rank_0_only():
+    env = dict(os.environ, WORLD_SIZE="2", RANK="1", LOCAL_RANK="1")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference"],
+                       env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and r.stdout.strip() == ""
