@@ -279,6 +279,9 @@ int tm_system_descriptors(tm_system *s, float *G_out);
  * One energy(+force) evaluation of the resident positions with CUDA events on
  * the ctx stream between stages; stage_ms[7] = (lists, descriptors, network
  * forward, network backward, pair terms, adjoint + force gather, total) in ms.
+ * Every stage runs alone here, in this order on the ctx stream (an ordinary
+ * evaluation overlaps the pair terms with the network backward pass and the
+ * Coulomb grid with the neighbour rows on a second stream).
  * No counterpart in the reference (its TFMolManage timing is wall-clock).
  */
 int tm_energy_force_profile(tm_system *s, unsigned flags, float *stage_ms);
