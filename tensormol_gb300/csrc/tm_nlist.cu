@@ -1038,30 +1038,44 @@ static int launch_ee_grid(tm_system* s) {
 // host synchronisation. A centre with more neighbours than its row capacity
 // records the count it needed in s->d_need; tm_nlist_grow() checks that after
 // the caller's own sync point and enlarges the rows so the call can be redone.
+static int launch_nbr_rows(tm_system* s);
+
 int tm_launch_nlist(tm_system* s) {
   tm_ctx* ctx = s->ctx;
   cudaStream_t st = ctx->stream;
-  const tm_consts& k = s->model->k;
   int rc;
   if ((rc = tm_launch_positions(s))) return rc;
   k_cbox_chunks<<<s->nchunk, 256, 0, st>>>(s->d_chunk, s->d_xhi, s->d_cbox);
+  ctx->launches++;
   // the Coulomb grid on the second stream, beside the neighbour rows; joined
-  // before this function returns
+  // on every path before this function returns
   cudaEventRecord(ctx->ev_fork, st);
   cudaStreamWaitEvent(ctx->aux, ctx->ev_fork, 0);
   ctx->stream = ctx->aux;
   rc = launch_ee_grid(s);
   ctx->stream = st;
   cudaEventRecord(ctx->ev_join, ctx->aux);
-  if (rc) {
-    cudaStreamWaitEvent(st, ctx->ev_join, 0);
-    return rc;
-  }
+  if (!rc) rc = launch_nbr_rows(s);
+  cudaStreamWaitEvent(st, ctx->ev_join, 0);
+  if (rc) return rc;
+  if (s->skin <= 0.0)
+    cudaMemcpyAsync(s->d_x_at_build, s->d_x, sizeof(double) * 3 * s->N, cudaMemcpyDeviceToDevice, st);
+  s->nlist_valid = true;
+  return tm_cuda_check(ctx, cudaGetLastError(), "nlist");
+}
+
+// The neighbour grid and the exact rows (radial, angular; candidates when the
+// system has a skin) with their reverse-edge indices, on the ctx stream.
+static int launch_nbr_rows(tm_system* s) {
+  tm_ctx* ctx = s->ctx;
+  cudaStream_t st = ctx->stream;
+  const tm_consts& k = s->model->k;
+  int rc;
   k_grid_from_chunks<<<tm_div_up(s->nmol, 4), 128, 0, st>>>(
       s->d_cbox, s->d_mol_chunk, s->d_off, s->d_grid, s->d_ncell_m, s->nmol, k.r_rc_d + s->skin,
       s->periodic ? 1 : 0, s->lat[0], s->lat[4], s->lat[8], 0.0, 2.0, 64.0, 0, 0, 0,
       s->nmol == 1 ? s->d_ncell : nullptr, s->ncell_cap, ctx->d_status);
-  ctx->launches += 2;
+  ctx->launches++;
   if (s->nmol > 1) {
     k_grid_offsets<<<1, 32, 0, st>>>(s->d_grid, s->d_ncell_m, s->nmol, s->d_ncell, s->ncell_cap,
                                      ctx->d_status);
@@ -1120,11 +1134,7 @@ int tm_launch_nlist(tm_system* s) {
                                                         s->d_nbr_a, s->d_cnt_a, s->d_rev_a, s->KA,
                                                         s->d_elem, s->d_mol, s->d_off, s->N);
   ctx->launches += 1;
-  cudaStreamWaitEvent(st, ctx->ev_join, 0);   // the Coulomb grid (second stream)
-  if (s->skin <= 0.0)
-    cudaMemcpyAsync(s->d_x_at_build, s->d_x, sizeof(double) * 3 * s->N, cudaMemcpyDeviceToDevice, st);
-  s->nlist_valid = true;
-  return tm_cuda_check(ctx, cudaGetLastError(), "nlist");
+  return tm_cuda_check(ctx, cudaGetLastError(), "neighbour rows");
 }
 
 // Skin lists between candidate builds: positions, exact rows filtered from
