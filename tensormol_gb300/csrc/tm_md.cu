@@ -401,7 +401,7 @@ static int md_step(tm_md* md, double* dlog, int* dstep) {
 // skin > 0: the first step of every chunk builds candidate lists within the
 // cutoffs + skin and the other steps filter them (exact rows every step). The
 // chunk length adapts so that no atom moves more than skin/2 within a chunk
-// (judged from the largest displacement seen in the previous chunk); a chunk
+// (estimated from the largest displacement seen in the previous chunk); a chunk
 // that exceeded it anyway is run again from its copy, shorter.
 extern "C" int tm_md_run(tm_md* md, int nsteps, double skin, double* log) {
   if (!md || nsteps < 0 || !(skin >= 0)) return TM_E_ARG;
