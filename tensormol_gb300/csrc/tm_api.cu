@@ -705,15 +705,12 @@ static int system_alloc(tm_system* s, int N_cap, int nmol_cap, int Mpad_cap, int
         (rc = tm_make_tmap(ctx, &s->tm_H2[h], s->H2[h], eb, 2 * Mp, H, TM_BM)) ||
         (rc = tm_make_tmap(ctx, &s->tm_G3[h], s->G3[h], eb, 2 * Mp, H, TM_BM)))
       return rc;
-    if (m->desc.precision == TM_PREC_FP32 &&
-        ((rc = tm_make_tmap(ctx, &s->ts_H1[h], s->H1[h], eb, 2 * Mp, H, 32)) ||
-         (rc = tm_make_tmap(ctx, &s->ts_H2[h], s->H2[h], eb, 2 * Mp, H, 32)) ||
-         (rc = tm_make_tmap(ctx, &s->ts_G3[h], s->G3[h], eb, 2 * Mp, H, 32))))
+    if ((rc = tm_make_tmap(ctx, &s->ts_H1[h], s->H1[h], eb, 2 * Mp, H, 32)) ||
+        (rc = tm_make_tmap(ctx, &s->ts_H2[h], s->H2[h], eb, 2 * Mp, H, 32)) ||
+        (rc = tm_make_tmap(ctx, &s->ts_G3[h], s->G3[h], eb, 2 * Mp, H, 32)))
       return rc;
   }
-  if (m->desc.precision == TM_PREC_FP32 &&
-      (rc = tm_make_tmap(ctx, &s->ts_dEdG, s->dEdG, 4, 2 * Mp, Dp, 32)))
-    return rc;
+  if ((rc = tm_make_tmap(ctx, &s->ts_dEdG, s->dEdG, 4, 2 * Mp, Dp, 32))) return rc;
   return TM_OK;
 }
 

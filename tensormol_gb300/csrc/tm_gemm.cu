@@ -42,8 +42,9 @@ constexpr int EPI_FWD = 0, EPI_FWD_LAST = 1, EPI_BWD = 2, EPI_OUT = 3;
 
 struct GemmArgs {
   CUtensorMap a0, a1, b0, b1;
-  CUtensorMap o0, o1;  // FP32 mode: 32 x 32 boxes of the outputs (hi, lo); the
-                       // backward pass also loads the previous activation by them
+  CUtensorMap o0, o1;  // 32-row boxes of the outputs (FP32: 32 columns, hi and lo;
+                       // BF16: 64 columns in o0; dE/dG: 32 FP32 columns in o0);
+                       // the backward pass also loads the previous activation by them
   int K;             // reduction length
   int N;             // output width of one (net, element) block
   int a_net_rows;    // row offset of net 1 in A (0 when both nets read the same A)
@@ -215,65 +216,6 @@ __device__ __forceinline__ float actd_h(float h, float a) {
 }
 
 template <int PREC>
-__device__ __forceinline__ void store32(void* o0, void* o1, size_t idx, const float (&v)[32]) {
-  if (PREC == TM_PREC_FP32) {
-    float4* p0 = reinterpret_cast<float4*>(static_cast<float*>(o0) + idx);
-    float4* p1 = reinterpret_cast<float4*>(static_cast<float*>(o1) + idx);
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      float4 h, l;
-      tm_tf32_split(v[4 * q], h.x, l.x);
-      tm_tf32_split(v[4 * q + 1], h.y, l.y);
-      tm_tf32_split(v[4 * q + 2], h.z, l.z);
-      tm_tf32_split(v[4 * q + 3], h.w, l.w);
-      p0[q] = h;
-      p1[q] = l;
-    }
-  } else {
-    uint4* p0 = reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(o0) + idx);
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      __nv_bfloat162 b0 = __floats2bfloat162_rn(v[8 * q + 0], v[8 * q + 1]);
-      __nv_bfloat162 b1 = __floats2bfloat162_rn(v[8 * q + 2], v[8 * q + 3]);
-      __nv_bfloat162 b2 = __floats2bfloat162_rn(v[8 * q + 4], v[8 * q + 5]);
-      __nv_bfloat162 b3 = __floats2bfloat162_rn(v[8 * q + 6], v[8 * q + 7]);
-      p0[q] = make_uint4(*reinterpret_cast<uint32_t*>(&b0), *reinterpret_cast<uint32_t*>(&b1),
-                         *reinterpret_cast<uint32_t*>(&b2), *reinterpret_cast<uint32_t*>(&b3));
-    }
-  }
-}
-
-template <int PREC>
-__device__ __forceinline__ void load32(const void* h0, const void* h1, size_t idx, float (&v)[32]) {
-  if (PREC == TM_PREC_FP32) {
-    const float4* p0 = reinterpret_cast<const float4*>(static_cast<const float*>(h0) + idx);
-    const float4* p1 = reinterpret_cast<const float4*>(static_cast<const float*>(h1) + idx);
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const float4 a = p0[q], b = p1[q];
-      v[4 * q] = a.x + b.x;
-      v[4 * q + 1] = a.y + b.y;
-      v[4 * q + 2] = a.z + b.z;
-      v[4 * q + 3] = a.w + b.w;
-    }
-  } else {
-    const uint4* p0 = reinterpret_cast<const uint4*>(static_cast<const __nv_bfloat16*>(h0) + idx);
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      uint4 u = p0[q];
-      uint32_t w[4] = {u.x, u.y, u.z, u.w};
-#pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        __nv_bfloat162 b = *reinterpret_cast<__nv_bfloat162*>(&w[t]);
-        float2 f = __bfloat1622float2(b);
-        v[8 * q + 2 * t] = f.x;
-        v[8 * q + 2 * t + 1] = f.y;
-      }
-    }
-  }
-}
-
-template <int PREC>
 struct Cfg {
   static constexpr int ELEM = PREC == TM_PREC_FP32 ? 4 : 2;
   static constexpr int BK = 128 / ELEM;               // one 128-byte swizzle row
@@ -285,8 +227,9 @@ struct Cfg {
   static constexpr int B_TILE = BN * 128;             // 16 KB (tf32) or 32 KB (bf16)
   static constexpr int STAGE = NSPLIT * (A_TILE + B_TILE);   // 64 KB or 48 KB
   static constexpr int NSTAGE = PREC == TM_PREC_FP32 ? 3 : 4;
-  // FP32 epilogue staging: per epilogue warp a 32 x 32 hi and lo box (8 KB)
-  static constexpr int EPI_BYTES = PREC == TM_PREC_FP32 ? 4 * 8192 : 0;
+  // epilogue staging per epilogue warp (8 KB): FP32, a 32 x 32 hi and lo box;
+  // BF16, a 32-row x 64-column box (and an FP32 32 x 32 box for dE/dG)
+  static constexpr int EPI_BYTES = 4 * 8192;
   static constexpr int SMEM = NSTAGE * STAGE + EPI_BYTES + 1024 + 256;   // + alignment, barriers
   static constexpr uint32_t IDESC = make_idesc(PREC == TM_PREC_FP32 ? 2 : 1, BM, BN);
 };
@@ -425,11 +368,11 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
     }
   } else {
     // ---- epilogue: warps 0..3, thread = accumulator row ----
-    // FP32 mode: each warp stages its 32 rows x 32 columns in shared memory in
-    // the TMA 128-byte-swizzle layout (16-byte chunk q of row r at chunk
-    // q ^ (r & 7): conflict-free for a row per lane) and writes them with one
-    // bulk tensor store per hi/lo part; the backward pass brings the previous
-    // activation in the same way.
+    // Each warp stages its 32 rows in shared memory in the TMA 128-byte-swizzle
+    // layout (16-byte piece q of row r at piece q ^ (r & 7): conflict-free for
+    // a row per lane) and writes them with bulk tensor stores: FP32 32 columns
+    // per box (hi and lo parts), BF16 64 columns per box (two 32-column
+    // chunks); the backward pass brings the previous activation in the same way.
     float* ebh = reinterpret_cast<float*>(smem + C::NSTAGE * C::STAGE + warp * 8192);
     float* ebl = ebh + 1024;
     int eph = 0;   // uses of this warp's load barrier
@@ -454,15 +397,23 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
       float esum = 0.f;
       for (int c = 0; c < BN && eok; c += 32) {
         const int col = n_tile * BN + c;
-        if constexpr (PREC == TM_PREC_FP32) {
+        // BF16 (not dE/dG): one 64-column box covers two 32-column chunks
+        const bool box_start = PREC == TM_PREC_FP32 || EPI == EPI_OUT || (c & 32) == 0;
+        const bool box_end = PREC == TM_PREC_FP32 || EPI == EPI_OUT || (c & 32) != 0;
+        if (box_start) {
           // the staging box is free once the previous stores have read it
           if (lane == 0) bulk_wait_read();
           __syncwarp();
           if constexpr (EPI == EPI_BWD) {
             if (lane == 0) {
-              mbar_expect_tx(&ebar[warp], 8192);
-              tma_load_2d(ebh, &g.o0, col, orow0, &ebar[warp]);
-              tma_load_2d(ebl, &g.o1, col, orow0, &ebar[warp]);
+              if constexpr (PREC == TM_PREC_FP32) {
+                mbar_expect_tx(&ebar[warp], 8192);
+                tma_load_2d(ebh, &g.o0, col, orow0, &ebar[warp]);
+                tma_load_2d(ebl, &g.o1, col, orow0, &ebar[warp]);
+              } else {
+                mbar_expect_tx(&ebar[warp], 4096);
+                tma_load_2d(ebh, &g.o0, col, orow0, &ebar[warp]);
+              }
             }
           }
         }
@@ -508,13 +459,15 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
           }
         } else if (EPI == EPI_BWD) {
           float h[32];
-          if constexpr (PREC == TM_PREC_FP32) {
+          if (box_start) {
             if (!mbar_wait(&ebar[warp], eph & 1)) {
               tm_flag(g.st, TM_E_TIMEOUT, t, 104);
               *abort_flag = 1;
               eok = false;
             }
             ++eph;
+          }
+          if constexpr (PREC == TM_PREC_FP32) {
             const float4* sh = reinterpret_cast<const float4*>(ebh) + lane * 8;
             const float4* sl = reinterpret_cast<const float4*>(ebl) + lane * 8;
 #pragma unroll
@@ -526,7 +479,20 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
               h[4 * q + 3] = a.w + b.w;
             }
           } else {
-            load32<PREC>(g.hprev0, g.hprev1, orow * g.ldo + col, h);
+            // bf16 box: 16-byte piece p (8 values) of row r at p ^ (r & 7)
+            const uint4* sh = reinterpret_cast<const uint4*>(ebh) + lane * 8;
+            const int p0 = (c & 32) ? 4 : 0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              const uint4 u = sh[(p0 + q) ^ (lane & 7)];
+              const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+              for (int e = 0; e < 4; ++e) {
+                const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w[e]));
+                h[8 * q + 2 * e] = f.x;
+                h[8 * q + 2 * e + 1] = f.y;
+              }
+            }
           }
 #pragma unroll
           for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]) * actd_h<ACT>(h[q], g.alpha);
@@ -559,11 +525,37 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
             bulk_commit();
           }
         } else if (EPI == EPI_OUT) {
-          float4* o = reinterpret_cast<float4*>(static_cast<float*>(g.out0) + orow * g.ldo + col);
+          // FP32 dE/dG through a 32 x 32 FP32 box
+          float4* dh = reinterpret_cast<float4*>(ebh) + lane * 8;
 #pragma unroll
-          for (int q = 0; q < 8; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+          for (int q = 0; q < 8; ++q)
+            dh[q ^ (lane & 7)] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+          fence_async_smem();
+          __syncwarp();
+          if (lane == 0) {
+            tma_store_2d(&g.o0, col, orow0, ebh);   // the FP32 map of dE/dG
+            bulk_commit();
+          }
         } else {
-          store32<PREC>(g.out0, g.out1, orow * g.ldo + col, v);
+          uint4* dh = reinterpret_cast<uint4*>(ebh) + lane * 8;
+          const int p0 = (c & 32) ? 4 : 0;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            __nv_bfloat162 b[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) b[e] = __floats2bfloat162_rn(v[8 * q + 2 * e], v[8 * q + 2 * e + 1]);
+            dh[(p0 + q) ^ (lane & 7)] =
+                make_uint4(*reinterpret_cast<uint32_t*>(&b[0]), *reinterpret_cast<uint32_t*>(&b[1]),
+                           *reinterpret_cast<uint32_t*>(&b[2]), *reinterpret_cast<uint32_t*>(&b[3]));
+          }
+          if (box_end) {
+            fence_async_smem();
+            __syncwarp();
+            if (lane == 0) {
+              tma_store_2d(&g.o0, col - 32, orow0, ebh);
+              bulk_commit();
+            }
+          }
         }
       }
       if (EPI == EPI_FWD_LAST) g.epart[orow * (g.N / BN) + n_tile] = esum;
@@ -572,10 +564,8 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
       __syncwarp();
       if (lane == 0) mbar_arrive(&acce[buf]);
     }
-    if constexpr (PREC == TM_PREC_FP32) {
-      if (lane == 0) bulk_wait_all();
-      __syncwarp();
-    }
+    if (lane == 0) bulk_wait_all();
+    __syncwarp();
   }
   tc_fence_before();
   __syncthreads();
@@ -795,7 +785,7 @@ int tm_gemm_selftest(tm_ctx* ctx, int prec, int M, int N, int K, const float* A,
       (rc = tm_make_tmap(ctx, &g.a1, prec == TM_PREC_FP32 ? da1 : da0, eb, 2 * (uint64_t)M, K, BM)) ||
       (rc = tm_make_tmap(ctx, &g.b0, db0, eb, 2 * (uint64_t)N, K, BN)) ||
       (rc = tm_make_tmap(ctx, &g.b1, prec == TM_PREC_FP32 ? db1 : db0, eb, 2 * (uint64_t)N, K, BN)) ||
-      (prec == TM_PREC_FP32 && (rc = tm_make_tmap(ctx, &g.o0, dc, 4, 2 * (uint64_t)M, N, 32))))
+      (rc = tm_make_tmap(ctx, &g.o0, dc, 4, 2 * (uint64_t)M, N, 32)))
     return rc;
   g.K = K; g.N = N; g.a_net_rows = M; g.nele = 1; g.tile_elem = dte; g.Mpad = M;
   g.out0 = dc; g.out1 = dc1; g.ldo = N; g.st = st;

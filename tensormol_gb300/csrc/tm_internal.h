@@ -185,8 +185,8 @@ struct tm_system {
   float* dEdG = nullptr;               // [2*Mpad][Dp]
   float* epart = nullptr;              // [2][Mpad][H/tm_gemm_bn(precision)]
   CUtensorMap tm_G[2], tm_H1[2], tm_H2[2], tm_G3[2];
-  // FP32 mode: 32-row boxes of the layer outputs for the GEMM epilogue's TMA
-  // stores (and the backward pass's loads of the previous activation)
+  // 32-row boxes of the layer outputs for the GEMM epilogue's TMA stores (and
+  // the backward pass's loads of the previous activation)
   CUtensorMap ts_H1[2], ts_H2[2], ts_G3[2], ts_dEdG;
   // per atom
   double* d_Eatom = nullptr;           // [N]
