@@ -32,22 +32,6 @@ namespace {
 
 constexpr float kBand = 1e-5f;
 
-__global__ void k_mlp_finish(const float* __restrict__ epart, const double* __restrict__ bout,
-                             const int32_t* __restrict__ row_of_atom,
-                             const int32_t* __restrict__ elem, int nsplit, int Mpad, int nele,
-                             int N, double* __restrict__ Eatom, float* __restrict__ qraw) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= N) return;
-  const int row = row_of_atom[i], e = elem[i];
-  double E = bout[e], q = bout[nele + e];
-  for (int s = 0; s < nsplit; ++s) {
-    E += (double)epart[(size_t)row * nsplit + s];
-    q += (double)epart[((size_t)Mpad + row) * nsplit + s];
-  }
-  Eatom[i] = E;
-  qraw[i] = (float)q;
-}
-
 // Per-molecule sums in two fixed-order levels: one block per chunk of at most
 // 1024 atoms of one molecule, then one warp per molecule over its chunks.
 template <int NV>
@@ -64,14 +48,28 @@ __device__ __forceinline__ void block_sum_store(double (&v)[NV], double* __restr
     for (int c = 0; c < NV; ++c) dst[c] = sh[c][0];
 }
 
-// chunk partials [c][0] = sum Eatom, [c][1] = sum q_raw
-__global__ void k_chunk_sum1(const int2* __restrict__ chunk, const double* __restrict__ Eatom,
-                             const float* __restrict__ qraw, double* __restrict__ part) {
+// Network outputs -> per-atom energy and raw charge (output bias plus the
+// N-tile partials of the last layer), and the chunk partials [c][0] = sum
+// Eatom, [c][1] = sum q_raw: one block per chunk.
+__global__ void k_mlp_finish(const int2* __restrict__ chunk, const float* __restrict__ epart,
+                             const double* __restrict__ bout, const int32_t* __restrict__ row_of_atom,
+                             const int32_t* __restrict__ elem, int nsplit, int Mpad, int nele,
+                             double* __restrict__ Eatom, float* __restrict__ qraw,
+                             double* __restrict__ part) {
   const int2 ch = chunk[blockIdx.x];
   double v[2] = {0.0, 0.0};
   for (int i = ch.x + threadIdx.x; i < ch.y; i += blockDim.x) {
-    v[0] += Eatom[i];
-    v[1] += (double)qraw[i];
+    const int row = row_of_atom[i], e = elem[i];
+    double E = bout[e], q = bout[nele + e];
+    for (int s = 0; s < nsplit; ++s) {
+      E += (double)epart[(size_t)row * nsplit + s];
+      q += (double)epart[((size_t)Mpad + row) * nsplit + s];
+    }
+    Eatom[i] = E;
+    const float qf = (float)q;
+    qraw[i] = qf;
+    v[0] += E;
+    v[1] += (double)qf;
   }
   block_sum_store<2>(v, part + 8 * (size_t)blockIdx.x);
 }
@@ -540,16 +538,15 @@ int tm_launch_mlp_finish(tm_system* s) {
   tm_ctx* ctx = s->ctx;
   tm_model* m = s->model;
   const int nsplit = m->H / tm_gemm_bn(m->desc.precision);
-  k_mlp_finish<<<tm_div_up(s->N, 256), 256, 0, ctx->stream>>>(
-      s->epart, m->bout, s->row_of_atom, s->d_elem, nsplit, s->Mpad, m->k.nele, s->N, s->d_Eatom,
-      s->d_qraw);
-  k_chunk_sum1<<<s->nchunk, 256, 0, ctx->stream>>>(s->d_chunk, s->d_Eatom, s->d_qraw, s->d_part);
+  k_mlp_finish<<<s->nchunk, 256, 0, ctx->stream>>>(s->d_chunk, s->epart, m->bout, s->row_of_atom,
+                                                   s->d_elem, nsplit, s->Mpad, m->k.nele,
+                                                   s->d_Eatom, s->d_qraw, s->d_part);
   k_mol_final1<<<tm_div_up(s->nmol, 4), 128, 0, ctx->stream>>>(s->d_mol_chunk, s->d_part,
                                                                  s->d_mol_E, s->d_mol_aux, s->nmol);
   k_neutralize<<<tm_div_up(s->N, 256), 256, 0, ctx->stream>>>(s->d_mol, s->d_off, s->d_qraw,
                                                               s->d_mol_aux, s->d_q, s->d_epos,
                                                               s->d_exlo, s->N);
-  ctx->launches += 4;
+  ctx->launches += 3;
   return tm_cuda_check(ctx, cudaGetLastError(), "mlp finish");
 }
 
