@@ -270,6 +270,15 @@ int tm_nlist_build_static(const double *x, const int32_t *elem, int natoms, doub
 int tm_selftest_gemm(tm_ctx *ctx, int precision, int M, int N, int K, const float *A,
                      const float *B, float *C);
 /*
+ * The polynomial the pair kernel evaluates erfc with on this model's DSF range
+ * (erfc(x) = exp(-x^2) P(t), t = x * scale + offset in [-1, 1], x = alpha r
+ * for r from the elu width to the Coulomb cutoff, in bohr): coeffs[11]
+ * (monomials in t, degree *n; *n = 0 when erfcf is used instead) and the
+ * range [*x0, *x1]. No counterpart in the reference (it calls tf.math.erfc).
+ */
+int tm_model_erfc_poly(const tm_model *m, float *coeffs, int *n, float *scale, float *offset,
+                       double *x0, double *x1);
+/*
  * Descriptor rows of every atom in atom order, FP32 [natoms][D], for the
  * current positions (lists are built if needed). Replaces reading
  * TFSymSet_Scattered_Linear_WithEle_Release's SymList (RawSymFunc.py:2267-2309).

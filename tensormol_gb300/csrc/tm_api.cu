@@ -306,6 +306,19 @@ extern "C" int tm_model_create(tm_ctx* ctx, const tm_model_desc* d, tm_model** o
 
 extern "C" int tm_model_descriptor_width(const tm_model* m) { return m ? m->k.D : -1; }
 
+extern "C" int tm_model_erfc_poly(const tm_model* m, float* coeffs, int* n, float* scale,
+                                  float* offset, double* x0, double* x1) {
+  if (!m || !coeffs || !n || !scale || !offset || !x0 || !x1) return TM_E_ARG;
+  for (int e = 0; e < 11; ++e) coeffs[e] = m->k.erfc_c[e];
+  *n = m->k.erfc_n;
+  *scale = m->k.erfc_s;
+  *offset = m->k.erfc_o;
+  const double alpha = m->desc.dsf_alpha / kBohr;
+  *x0 = alpha * m->desc.elu_width * kBohr;
+  *x1 = alpha * m->desc.ee_cut_off * kBohr;
+  return TM_OK;
+}
+
 extern "C" int tm_model_set_layer(tm_model* m, int net, int e, int layer, const double* W,
                                   const double* b, int fan_in, int fan_out) {
   if (!m || !W || !b || net < 0 || net > 1 || e < 0 || e >= m->k.nele || layer < 0 ||

@@ -48,6 +48,39 @@ def _errors(out, ref, natoms_per_mol):
 
 
 # ---------------------------------------------------------------------------
+@pytest.mark.parametrize("cutoff", [15.0, 9.0])
+def test_erfc_polynomial_against_scipy(gpu, cutoff):
+    """The pair kernel forms erfc(x) = exp(-x^2) P(t) on the model's DSF range
+    with P a polynomial fitted on the host (erfcx at Chebyshev nodes). Against
+    scipy's erfc over the range: within 2e-7 relative with the coefficients as
+    stored (FP32) and evaluated in FP64, and within 6e-7 of erfc at the same
+    FP32 argument evaluated all in FP32 as the kernel does (Horner's rule;
+    exp(-x^2) with x^2 rounded to FP32 contributes up to 2 x^2 ulp)."""
+    import ctypes
+    special = pytest.importorskip("scipy.special")
+    m, _ = _model(gpu, [1, 8], EECutoffOff=cutoff)
+    c = np.zeros(11, dtype=np.float32)
+    n = ctypes.c_int()
+    sc, of = ctypes.c_float(), ctypes.c_float()
+    x0, x1 = ctypes.c_double(), ctypes.c_double()
+    m.ctx.check(m.lib.tm_model_erfc_poly(m.h, c.ctypes.data, ctypes.byref(n), ctypes.byref(sc),
+                                         ctypes.byref(of), ctypes.byref(x0), ctypes.byref(x1)))
+    assert 4 <= n.value <= 10
+    x = np.linspace(x0.value, x1.value, 5001)
+    ref = special.erfc(x)
+    t64 = x * np.float64(sc.value) + np.float64(of.value)
+    p64 = np.polyval(c[::-1].astype(np.float64), t64)
+    assert np.max(np.abs(np.exp(-x * x) * p64 / ref - 1.0)) < 2e-7
+    x32 = x.astype(np.float32)
+    t32 = (x32 * np.float32(sc.value) + np.float32(of.value)).astype(np.float32)
+    p32 = np.float32(c[10])
+    for e in range(9, -1, -1):
+        p32 = (p32 * t32 + c[e]).astype(np.float32)
+    e32 = np.exp(-(x32 * x32).astype(np.float64)).astype(np.float32)
+    ref32 = special.erfc(x32.astype(np.float64))
+    assert np.max(np.abs((e32 * p32).astype(np.float64) / ref32 - 1.0)) < 6e-7
+
+
 def test_tensor_core_gemm_selftest(gpu):
     rng = np.random.default_rng(0)
     M, N, K = 256, 512, 512
