@@ -180,7 +180,9 @@ __device__ __forceinline__ PairOut pair_terms(float r, float ir, float qi, float
         dkc = 0.f;
       } else {
         const float ar = k.alpha * rb;
-        const float ex2 = expf(-ar * ar);
+        // exp(-x^2) with the rounding error of x^2 (exact by an FMA) folded in
+        const float x2 = ar * ar;
+        const float ex2 = expf(-x2) * (1.f - fmaf(ar, ar, -x2));
         float ec;
         if (k.erfc_n) {   // exp(-x^2) erfcx(x), erfcx by its polynomial on this range
           const float t = fmaf(ar, k.erfc_s, k.erfc_o);
