@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(128) k_desc_fwd(const DescArgs a, const tm_con
   }
 }
 
-__global__ void __launch_bounds__(128) k_desc_adj(const DescArgs a, const tm_consts k) {
+__global__ void __launch_bounds__(128, 6) k_desc_adj(const DescArgs a, const tm_consts k) {
   extern __shared__ float sh[];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * (blockDim.x >> 5) + wib;
