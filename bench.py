@@ -372,6 +372,25 @@ def time_md(model_fp32, torch):
     return out
 
 
+def time_chno512(steps, flush, torch):
+    """C3: 512 CHNO molecules of 8-64 atoms (seed 3) as one batch, one fused
+    E+F per step with device-resident positions (FP32 networks, 4 elements,
+    3 x 512); median of the CUDA-event times, L2 flushed before each step."""
+    from tensormol_gb300 import systems
+    from tensormol_gb300.model import BPEEModel
+    from tensormol_gb300.params import PARAMS, descriptor_width
+    eles = [1, 6, 7, 8]
+    b = systems.chno_batch(nmol=512, seed=3)
+    model = BPEEModel(eles, systems.random_weights(eles, descriptor_width(4), seed=7),
+                      params=dict(PARAMS))
+    s, times, _, _, _, _ = time_fused_device(model, b, max(steps, 20), 3, flush, torch)
+    s.close()
+    model.close()
+    ms = float(np.median(times))
+    return {"molecules": 512, "atoms": int(b.natoms), "ms_per_step": ms,
+            "atom_steps_per_s": b.natoms / (ms / 1000.0)}
+
+
 def time_serving(max_atoms=32768, max_mols=256, loads=(0.25, 0.5, 1.1, 1.5, 3.0)):
     """Offline: every request submitted at once, batches kept full. Online:
     Poisson arrivals whose offered atom-steps/s is `load` x the offline rate,
@@ -556,6 +575,7 @@ def main():
     s.close()
     serving = None if args.no_serve else time_serving()
     md_runs = None if args.no_md else time_md(model, torch)
+    chno = time_chno512(args.steps, flush, torch)
     # BF16 variant
     _, _, _, model16 = build_workload("bf16")
     s16, t16, _, _, E16, F16 = time_fused_device(model16, w, args.steps, args.warmup, flush, torch)
@@ -616,6 +636,7 @@ def main():
             "plain_autograd": plain,
             "serve": serving,
             "md": md_runs,
+            "chno512": chno,
             "published_reference": {"value": 274.0, "unit": UNIT, "hardware": "2015 Core i7, 1 core",
                                     "source": "24,000 atoms / ~87.5 s read off doc/images/Timings.png"}}
     if rank == 0:
