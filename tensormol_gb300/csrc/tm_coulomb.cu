@@ -330,6 +330,16 @@ __device__ __forceinline__ void coulomb_drain(const CoulArgs& a, const StageSmem
 __global__ void __launch_bounds__(128, 6) k_coulomb(const CoulArgs a, const tm_consts k) {
   __shared__ StageSmem stage[4];
   __shared__ float tab[2][TM_MAX_ELE * TM_MAX_ELE];   // sqrt(C6_i C6_j), R0_i + R0_j
+  {
+    // the grid is sized for the block capacity: a CTA whose four centre
+    // blocks all lie beyond the ones that exist leaves at once (the same
+    // decision in every thread, before the barrier)
+    const int nb = *a.nblk;
+    bool work = false;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+      work |= (blockIdx.x * (blockDim.x >> 5) + w) % a.blk_cap < nb;
+    if (!work) return;
+  }
   if (threadIdx.x < k.nele * k.nele) {
     const int ei = threadIdx.x / k.nele, ej = threadIdx.x % k.nele;
     tab[0][threadIdx.x] = sqrtf(k.c6[ei] * k.c6[ej]);
@@ -347,15 +357,27 @@ __global__ void __launch_bounds__(128, 6) k_coulomb(const CoulArgs a, const tm_c
   const tm_grid g = a.grid[a.mol[a.eatom[t0]]];
   const int lc = head - g.cell_off;
   const int iy = (lc / g.nz) % g.ny, ix = lc / (g.nz * g.ny);
+  // periodic: at most one wrap per axis (R <= n; edges are >= 2 * cutoff)
+  const int Rx = a.periodic ? min((int)ceil(a.reach / g.cx), g.nx) : (int)ceil(a.reach / g.cx);
+  const int Ry = a.periodic ? min((int)ceil(a.reach / g.cy), g.ny) : (int)ceil(a.reach / g.cy);
+  const int Rz = a.periodic ? min((int)ceil(a.reach / g.cz), g.nz) : (int)ceil(a.reach / g.cz);
+  if (!a.periodic) {
+    // a small molecule's grid has few columns: most stencil shares lie
+    // outside it, and the warp leaves before loading any centre
+    const int ny2s = 2 * Ry + 1, col0s = Rx * ny2s + Ry, nhalfs = (2 * Rx + 1) * ny2s - col0s;
+    bool any = false;
+    for (int col = split; col < nhalfs && !any; col += TM_EE_SPLIT) {
+      const int cf = col0s + col;
+      const int jx = ix + cf / ny2s - Rx, jy = iy + cf % ny2s - Ry;
+      any = jx >= 0 && jx < g.nx && jy >= 0 && jy < g.ny;
+    }
+    if (!any) return;
+  }
   const int ncolumn = a.cell_start[head + g.nz] - a.cell_start[head];
   // z range of the block's cells; positions are taken in the frame of cell
   // (ix, iy, z0)
   const int z0 = (a.cell_of[a.eatom[t0]] - head), z1 = (a.cell_of[a.eatom[t1 - 1]] - head);
   const float cx = (float)g.cx, cy = (float)g.cy, cz = (float)g.cz;
-  // periodic: at most one wrap per axis (R <= n; edges are >= 2 * cutoff)
-  const int Rx = a.periodic ? min((int)ceil(a.reach / g.cx), g.nx) : (int)ceil(a.reach / g.cx);
-  const int Ry = a.periodic ? min((int)ceil(a.reach / g.cy), g.ny) : (int)ceil(a.reach / g.cy);
-  const int Rz = a.periodic ? min((int)ceil(a.reach / g.cz), g.nz) : (int)ceil(a.reach / g.cz);
   StageSmem& st = stage[wib];
   // Upper half of the (ox, oy) columns: (0, 0) first, then the columns
   // after it in x-major order (every z). In the own column, cells from z0 up
