@@ -326,17 +326,35 @@ __global__ void k_ee_blocks(const int32_t* __restrict__ order, const int32_t* __
   else tm_flag(st, TM_E_CAPACITY, slot, 2);
 }
 
+// First cell of every molecule's grid (exclusive prefix sum of the cell
+// counts) and the total, by one block of 256 threads: thread t sums a
+// contiguous run of molecules, the run sums are scanned in shared memory, and
+// each thread then writes its run's offsets (one fixed order of additions).
 __global__ void k_grid_offsets(tm_grid* __restrict__ grid, const int32_t* __restrict__ ncell_m,
                                int nmol, int32_t* __restrict__ total, int cap, tm_dev_status* st) {
-  // single thread: nmol is at most a few thousand; this runs once per build
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  int acc = 0;
-  for (int m = 0; m < nmol; ++m) {
+  __shared__ int part[256];
+  const int t = threadIdx.x;
+  const int per = (nmol + 255) / 256;
+  const int m0 = min(t * per, nmol), m1 = min(m0 + per, nmol);
+  int sum = 0;
+  for (int m = m0; m < m1; ++m) sum += ncell_m[m];
+  part[t] = sum;
+  __syncthreads();
+  for (int o = 1; o < 256; o <<= 1) {
+    const int v = t >= o ? part[t - o] : 0;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  int acc = part[t] - sum;   // exclusive
+  for (int m = m0; m < m1; ++m) {
     grid[m].cell_off = acc;
     acc += ncell_m[m];
   }
-  *total = acc;
-  if (acc > cap) tm_flag(st, TM_E_CAPACITY, acc, 2);
+  if (t == 255) {
+    *total = part[255];
+    if (part[255] > cap) tm_flag(st, TM_E_CAPACITY, part[255], 2);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1005,7 +1023,7 @@ static int launch_ee_grid(tm_system* s) {
       s->ee_dims[1], s->ee_dims[2], s->nmol == 1 ? s->d_encell : nullptr, s->ecell_cap,
       ctx->d_status);
   if (s->nmol > 1) {
-    k_grid_offsets<<<1, 32, 0, st>>>(s->d_egrid, s->d_encell_m, s->nmol, s->d_encell, s->ecell_cap,
+    k_grid_offsets<<<1, 256, 0, st>>>(s->d_egrid, s->d_encell_m, s->nmol, s->d_encell, s->ecell_cap,
                                      ctx->d_status);
     ctx->launches++;
   }
@@ -1077,7 +1095,7 @@ static int launch_nbr_rows(tm_system* s) {
       s->nmol == 1 ? s->d_ncell : nullptr, s->ncell_cap, ctx->d_status);
   ctx->launches++;
   if (s->nmol > 1) {
-    k_grid_offsets<<<1, 32, 0, st>>>(s->d_grid, s->d_ncell_m, s->nmol, s->d_ncell, s->ncell_cap,
+    k_grid_offsets<<<1, 256, 0, st>>>(s->d_grid, s->d_ncell_m, s->nmol, s->d_ncell, s->ncell_cap,
                                      ctx->d_status);
     ctx->launches++;
   }
@@ -1414,7 +1432,7 @@ extern "C" int tm_nlist_build_static(const double* x, const int32_t* elem, int n
   k_positions<<<tm_div_up(N, 256), 256, 0, st>>>(x, elem, S->xhi, S->xlo, N, &S->status);
   k_grid_setup<<<1, 256, 0, st>>>(x, S->off, &S->grid, &S->ncell_m, r_rc, 0, 0.0, 0.0, 0.0, 0.0,
                                   2.0, 64.0, 0, 0, 0);
-  k_grid_offsets<<<1, 32, 0, st>>>(&S->grid, &S->ncell_m, 1, &S->ncell, cap, &S->status);
+  k_grid_offsets<<<1, 256, 0, st>>>(&S->grid, &S->ncell_m, 1, &S->ncell, cap, &S->status);
   cudaMemsetAsync(S->cell_cnt, 0, sizeof(int32_t) * (cap + 1), st);
   k_cell_count<<<tm_div_up(N, 256), 256, 0, st>>>(x, S->mol, &S->grid, S->cell_cnt, S->cell_of_atom,
                                                    N, cap, &S->status);
