@@ -25,9 +25,6 @@ __device__ __forceinline__ void tm_flag(tm_dev_status* st, int code, int detail,
   }
 }
 
-// Raise *p to at least v (int).
-__device__ __forceinline__ void tm_atomic_max(int* p, int v) { atomicMax(p, v); }
-
 // ---------------------------------------------------------------------------
 // Double-single positions: x = hi + lo with hi = fp32(x), lo = fp32(x - hi).
 // The difference of two such positions is accurate to about one fp32 ulp of
@@ -104,11 +101,6 @@ __device__ __forceinline__ void tm_img_ijk(int r, int& i, int& j, int& k) {
 }
 
 __device__ __forceinline__ float warp_sum(float v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(TM_FULL, v, o);
-  return v;
-}
-__device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(TM_FULL, v, o);
   return v;
