@@ -113,3 +113,33 @@ def test_periodic_oracle_conservative_force_fd(golden_loader):
             ep = o.terms(xp, grad=False)["Etotal"].sum()
             em = o.terms(xm, grad=False)["Etotal"].sum()
             assert abs((ep - em) / (2 * h) - out["gradient"][a, c]) < 1e-7
+
+
+def test_ragged_batch_equals_molecules_alone():
+    """Molecules of 1, 2, 3 and 60 atoms in one batch, all overlapping in
+    space, give the same energies and forces as each molecule evaluated
+    alone: no pair, triple or Coulomb term crosses a molecule boundary. A
+    lone atom has no neighbours and feels no force; a two-atom molecule has
+    pairs but no triples. The GPU ragged-batch test compares against this
+    batched oracle, so the batching itself is checked here."""
+    w = systems.water_cluster_60(seed=0)
+    xs = [np.zeros((1, 3)), np.array([[0.0, 0.0, 0.0], [0.0, 0.0, 0.97]]),
+          np.array([[0.0, 0.0, 0.0], [0.96, 0.0, 0.0], [-0.24, 0.93, 0.0]]), w.x]
+    Zs = [np.array([8]), np.array([8, 1]), np.array([8, 1, 1]), w.Z]
+    x = np.concatenate(xs)
+    Z = np.concatenate(Zs).astype(np.int32)
+    off = np.concatenate([[0], np.cumsum([len(z) for z in Zs])]).astype(np.int64)
+    p = dict(PARAMS)
+    p["NeuronType"] = "sigmoid_with_param"
+    W = systems.random_weights([1, 8], descriptor_width(2), seed=7)
+    model = orc.Model([1, 8], W, params=p)
+    batch = orc.OpenSystemOracle(model, x, Z, off)
+    out = batch.terms(x)
+    assert not np.any(batch.P[:, 0] == 0) and not np.any(batch.T[:, 0] == 0)   # lone atom
+    assert np.any(batch.P[:, 0] == 1) and not np.any(batch.T[:, 0] == 1)       # pair only
+    assert np.all(out["force"][0] == 0.0)
+    for m, (xm, Zm) in enumerate(zip(xs, Zs)):
+        alone = orc.OpenSystemOracle(model, xm, Zm, np.array([0, len(Zm)])).terms(xm)
+        for key in ("Etotal", "Ebp", "Ecc", "Evdw"):
+            np.testing.assert_allclose(out[key][m], alone[key][0], rtol=1e-12, atol=1e-14)
+        np.testing.assert_allclose(out["force"][off[m]:off[m + 1]], alone["force"], rtol=0, atol=1e-8)
