@@ -962,10 +962,13 @@ static int energy_force_pipeline(tm_system* s, unsigned flags, cudaEvent_t* ev) 
     if ((rc = tm_launch_mlp_finish(s))) return rc;
     if (force) {
       // The backward pass of both networks needs no pair term (dE/dq enters
-      // in the adjoint), so the pair terms run on the second stream beside it:
-      // the layer GEMMs wait on their operand ring and leave most issue slots
-      // free, the pair kernel is issue bound, and one of its blocks fits
-      // beside a GEMM CTA on every SM.
+      // in the adjoint), so the pair terms run on the second stream beside it.
+      // A GEMM CTA takes 225 KB of the SM's 228 KB of shared memory, so the
+      // two kernels do not share an SM. Submitted first, the pair kernel fills
+      // the GEMM's idle SMs and the launch gaps at both ends, and the GEMMs
+      // then start on SMs that it has drained. Submitted second (measured),
+      // its blocks slip in between the three GEMM launches and delay the
+      // persistent CTAs of the next one.
       tm_ctx* ctx = s->ctx;
       cudaEventRecord(ctx->ev_fork, st);
       cudaStreamWaitEvent(ctx->aux, ctx->ev_fork, 0);
