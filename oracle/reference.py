@@ -454,6 +454,24 @@ class PeriodicOracle:
 # ---------------------------------------------------------------------------
 # Integrators (FP64), Simulations/SimpleMD.py
 # ---------------------------------------------------------------------------
+def anharmonic_wells(x0, k=4.0e5, c=1.0e5):
+    """A force field for pinning the integrators, not a reference function:
+    every atom sits in its own well E = k/2 |d|^2 + c/4 |d|^4 about x0
+    (d = x - x0; k in J/mol/A^2, c in J/mol/A^4, about an O-H stretch).
+    Returns ef(x) -> (E [J/mol], F [N,3] J/mol/A), the (energy, force)
+    routine the integrators take."""
+    x0 = np.array(x0, dtype=np.float64)
+
+    def ef(x):
+        d = x - x0
+        r2 = np.einsum("ia,ia->i", d, d)
+        e = float(np.sum(0.5 * k * r2 + 0.25 * c * r2 * r2))
+        f = -(k + c * r2)[:, None] * d
+        return e, f
+
+    return ef
+
+
 def kinetic_energy(v, m):
     """Per-atom KE in J/mol (SimpleMD.py:40-51)."""
     return 0.5 * np.dot(np.einsum("ia,ia->i", v, v) * 1e10, m) / len(m)
@@ -476,7 +494,8 @@ class Nose:
         self.m, self.N, self.T, self.dt = m, len(m), T, dt
         self.eta = 0.0
         self.kT = IDEALGASR * 1e-10 * T
-        self.Q = self.kT * (20.0 * dt * self.N) ** 2
+        tau = 20.0 * dt * self.N
+        self.Q = self.kT * tau * tau
 
     def step(self, ef, a, x, v):
         dt, m, N, kT = self.dt, self.m, self.N, self.kT
@@ -498,10 +517,22 @@ class NoseHooverChain:
     (SimpleMD.py:206-320): nc = 2, ny = 3 Suzuki-Yoshida weights,
     Q0 = 3 N kT tau^2, Qi = kT tau^2, tau = 80 dt, Nf = 3N. The particle
     velocities are scaled by the first chain element (the paper), not by the
-    second one as SimpleMD.py:304 does."""
+    second one as SimpleMD.py:304 does.
 
-    def __init__(self, m, T, dt, M=3):
+    as_simplemd=True reproduces SimpleMD.py's two departures from the paper,
+    for pinning this restatement against the reference's own code: the
+    velocity scale uses the second chain element (SimpleMD.py:304), and the
+    chain forces G[1:] start at zero (SimpleMD.py:245) and carry over between
+    half steps instead of being formed from the chain velocities at the start
+    of each half step (SimpleMD.py:291). After the first half step the carried
+    values equal the formed ones, so only the first half step and the scale
+    differ."""
+
+    def __init__(self, m, T, dt, M=3, as_simplemd=False):
         from tensormol_gb300.params import IDEALGASR
+        if as_simplemd and M < 2:
+            raise ValueError("SimpleMD.py's velocity scale reads the second chain element")
+        self.as_simplemd = as_simplemd
         self.m, self.N, self.M, self.dt = m, len(m), M, dt
         self.kT = IDEALGASR * 1e-10 * T
         self.GNKT = 3 * self.N * self.kT
@@ -522,8 +553,10 @@ class NoseHooverChain:
         M, Q, kT = self.M, self.Q, self.kT
         ake2 = self._ke2(v)
         self.G[0] = (ake2 - self.GNKT) / Q[0]
-        for i in range(M - 1):
-            self.G[i + 1] = (Q[i] * self.veta[i] ** 2 - kT) / Q[i + 1]
+        if not self.as_simplemd:
+            for i in range(M - 1):
+                self.G[i + 1] = (Q[i] * self.veta[i] ** 2 - kT) / Q[i + 1]
+        iscale = 1 if self.as_simplemd else 0
         scale = 1.0
         for _ in range(self.nc):
             for wj in self.wj:
@@ -533,7 +566,7 @@ class NoseHooverChain:
                 for i in range(M - 2, -1, -1):
                     aa = math.exp(-d8 * self.veta[i + 1])
                     self.veta[i] = self.veta[i] * aa * aa + d4 * self.G[i] * aa
-                aa = math.exp(-d2 * self.veta[0])
+                aa = math.exp(-d2 * self.veta[iscale])
                 scale *= aa
                 self.G[0] = (scale * scale * ake2 - self.GNKT) / Q[0]
                 self.eta += self.veta * d2
