@@ -16,7 +16,8 @@ What is produced, per case (seeded inputs from ``tensormol_gb300.systems``):
   ``EvalBPDirectEEUpdateSinglePeriodic`` (TFMolManage.py:1342-1345) on a
   tessellated box;
 * ``MolEmb.Make_ANI1_Sym`` descriptor rows and ``Make_ANI1_Sym_deri`` Jacobian
-  slices (C_API/MolEmb.cpp:1844-1988).
+  slices (C_API/MolEmb.cpp:1844-1988); for the periodic box, the rows of its
+  real atoms computed over the tessellated cell (no Jacobian there).
 
 Usage: python tests/golden/make_golden.py
 """
@@ -135,7 +136,10 @@ def ani1(molemb, x, Z, eles, atoms_deri):
     xyz = np.ascontiguousarray(x, dtype=np.float64)
     at = np.ascontiguousarray(Z, dtype=np.uint8)
     el = np.ascontiguousarray(eles, dtype=np.uint8)
+    # -1: every atom, each in its own iteration of the outer parallel loop
     G = molemb.Make_ANI1_Sym(prm, xyz, at, el, -1)
+    if not len(atoms_deri):
+        return G, None
     J = np.stack([molemb.Make_ANI1_Sym_deri(prm, xyz, at, el, int(a))[0] for a in atoms_deri])
     return G, J
 
@@ -164,8 +168,12 @@ def main():
     lat = np.eye(3) * L
     xw = orc.modulo_lattice(pb.x, lat)
     c = periodic_case(nb, xw, pb.Z, lat, [1, 8], 6.0)
+    # descriptor rows of the real atoms among their 26 image shells
+    # (tessellated cell, real atoms first; Periodic.py:131-181)
+    xt = orc.tessellate(xw, lat, 1)
+    Gt, _ = ani1(molemb, xt, np.tile(pb.Z, xt.shape[0] // len(pb.Z)), [1, 8], [])
     np.savez_compressed(os.path.join(HERE, "waterbox192.npz"), x=xw, Z=pb.Z, lattice=lat,
-                        ree_cut=np.array(6.0), **c)
+                        ree_cut=np.array(6.0), ani1_G=Gt[:len(pb.Z)], **c)
     out["waterbox192"] = {k: v.shape for k, v in c.items()}
     for k, v in out.items():
         print(k, v)

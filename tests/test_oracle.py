@@ -143,3 +143,15 @@ def test_ragged_batch_equals_molecules_alone():
         for key in ("Etotal", "Ebp", "Ecc", "Evdw"):
             np.testing.assert_allclose(out[key][m], alone[key][0], rtol=1e-12, atol=1e-14)
         np.testing.assert_allclose(out["force"][off[m]:off[m + 1]], alone["force"], rtol=0, atol=1e-8)
+
+
+def test_periodic_descriptor_matches_molemb(golden_loader):
+    """Descriptor rows of the 192 real atoms of the periodic box against
+    MolEmb's Make_ANI1_Sym over the tessellated cell (real atoms first)."""
+    g = golden_loader("waterbox192")
+    W = systems.random_weights([1, 8], descriptor_width(2), seed=7)
+    model = orc.Model([1, 8], W)
+    o = orc.PeriodicOracle(model, g["x"], g["Z"], g["lattice"], ree_cut=float(g["ree_cut"]))
+    out = o.terms(g["x"], grad=False)
+    # MolEmb writes pi as 3.14159265358979, the TF graph as 3.14159265359
+    np.testing.assert_allclose(out["G"], g["ani1_G"], rtol=0, atol=1e-11)
