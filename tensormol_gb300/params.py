@@ -125,7 +125,7 @@ def descriptor_width(n_ele, params=None):
 
 
 def dsf(r, rc, alpha):
-    """Damped shifted force kernel value (Util.py:174-183)."""
+    """Damped shifted force kernel value (Util.py:172-181)."""
     from math import erfc, exp
     if r > rc:
         return 0.0
@@ -136,7 +136,7 @@ def dsf(r, rc, alpha):
 
 
 def dsf_gradient(r, rc, alpha):
-    """Derivative of the DSF kernel (Util.py:185-193)."""
+    """Derivative of the DSF kernel (Util.py:183-192)."""
     from math import erfc, exp
     if r > rc:
         return 0.0
