@@ -155,3 +155,29 @@ def test_periodic_descriptor_matches_molemb(golden_loader):
     out = o.terms(g["x"], grad=False)
     # MolEmb writes pi as 3.14159265358979, the TF graph as 3.14159265359
     np.testing.assert_allclose(out["G"], g["ani1_G"], rtol=0, atol=1e-11)
+
+
+@pytest.mark.parametrize("case", ["a", "b"])
+def test_tessellation_matches_lattice(golden_loader, case):
+    """Image coordinates and order against the reference's Lattice.TessLattice
+    (one shell for the water box, three for a small orthorhombic cell):
+    real atoms first, then the images in (i, j, k) raster order, each
+    coordinate x + i a0 + j a1 + k a2 in FP64, bit for bit."""
+    g = golden_loader("lattice")
+    x, lat = g["tess_%s_x" % case], g["tess_%s_lattice" % case]
+    ntess = int(g["tess_%s_ntess" % case])
+    xt = orc.tessellate(x, lat, ntess)
+    assert np.array_equal(xt, g["tess_%s_coords" % case])
+    shifts = orc.image_shift_table(lat, ntess)
+    assert shifts.shape[0] * x.shape[0] == g["tess_%s_atoms" % case].shape[0]
+
+
+@pytest.mark.parametrize("name", ["orth", "tric"])
+def test_modulo_lattice_matches_reference(golden_loader, name):
+    """Wrap into the cell against Lattice.ModuloLattice. The oracle uses a
+    plain inverse, the reference an SVD matrix power, so the two agree to
+    rounding, not bit for bit."""
+    g = golden_loader("lattice")
+    lat = g["mod_%s_lattice" % name]
+    out = orc.modulo_lattice(g["mod_%s_in" % name], lat)
+    np.testing.assert_allclose(out, g["mod_%s_out" % name], rtol=0, atol=1e-12)
