@@ -85,3 +85,19 @@ def test_weights_by_reference_names():
         for e in (1, 8):
             for (W0, b0), (W1, b1) in zip(W[net][e], back[net][e]):
                 assert np.array_equal(W0, W1) and np.array_equal(b0, b1)
+
+
+def test_xyz_text_matches_the_reference(tmp_path):
+    """The XYZ text of Mol.__str__ / WriteXYZfile equals what the reference's
+    own Mol.__str__ and PropertyString produce for the same molecule
+    (tests/golden/make_golden_xyz.py), with and without the property line."""
+    import ast
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "xyz.npz"))
+    for name in ("water60", "water60_props", "chno0"):
+        m = Mol(g[name + "_Z"], g[name + "_x"])
+        m.properties.update(ast.literal_eval(str(g[name + "_props"])))
+        wprop = bool(g[name + "_wprop"])
+        assert m.__str__(wprop) == str(g[name + "_text"]), name
+        m.WriteXYZfile(str(tmp_path), name, mode="w", wprop=wprop)
+        assert (tmp_path / (name + ".xyz")).read_text() == str(g[name + "_text"]) + "\n", name
