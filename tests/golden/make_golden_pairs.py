@@ -1,0 +1,202 @@
+"""Golden molecular Coulomb and vdW energies from the reference's own
+TensorFlow-graph functions, run on a numpy implementation of the TF ops.
+
+``TFCoulombEluSRDSFLR`` and ``TFVdwPolyLR`` (TFDescriptors/RawSymFunc.py:1307-1414)
+and the helpers they call, ``DifferenceVectorsLinear`` (:123-133) and
+``AllDoublesSet`` (:63-78), are taken from the file's syntax tree and run
+unchanged. TensorFlow is absent, so ``tf`` in their namespace is the small
+numpy stand-in below: each op does what the TF 1.x op of that name does for
+the shapes these functions use. Arguments follow the reference's calls
+(TFBehlerParinelloSymEE.py:941, 1012):
+* positions in bohr, as a padded [nmol, maxnatom, 3] tensor;
+* charges as [nmol, maxnatom];
+* the Coulomb pair list (mol, i, j) the reference's ``buildPairs`` made,
+  stored in the water60 and chno6 fixtures;
+* C6 and vdW radii converted as the model constructor does
+  (TFBehlerParinelloSymEE.py:719-723), from the reference's own
+  PhysicalData.py;
+* the elu shift and slope from its own ``DSF`` / ``DSF_Gradient`` (Util.py).
+Charges are seeded values, not network outputs: the functions do not care
+where the charges come from.
+
+Writes ``tests/golden/pairs.npz``.
+
+Usage (where the reference tree is present): python tests/golden/make_golden_pairs.py
+"""
+from __future__ import annotations
+
+import ast
+import importlib.util
+import math
+import os
+import sys
+import warnings
+
+import numpy as np
+import scipy.special
+
+# the reference's modules are imported from its own (read-only) tree: no
+# bytecode caches may be written there
+sys.dont_write_bytecode = True
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = os.path.join(os.environ.get("TM_REFERENCE", "/root/reference"), "TensorMol")
+
+
+class _SparseTensor:
+    def __init__(self, indices, values, dense_shape):
+        self.indices = np.asarray(indices, dtype=np.int64)
+        self.values = np.asarray(values)
+        self.dense_shape = [int(d) for d in dense_shape]
+
+
+class _NumpyTF:
+    """The TF 1.x ops the two pair functions and their helpers call."""
+    float64, float32, int64, int32 = np.float64, np.float32, np.int64, np.int32
+    SparseTensor = _SparseTensor
+
+    @staticmethod
+    def shape(x):
+        return np.array(np.shape(x), dtype=np.int64)
+
+    sqrt = staticmethod(np.sqrt)
+    exp = staticmethod(np.exp)
+    multiply = staticmethod(np.multiply)
+    pow = staticmethod(np.power)
+    greater = staticmethod(np.greater)
+    equal = staticmethod(np.equal)
+    is_nan = staticmethod(np.isnan)
+    zeros_like = staticmethod(np.zeros_like)
+    ones_like = staticmethod(np.ones_like)
+    erfc = staticmethod(scipy.special.erfc)
+
+    @staticmethod
+    def reduce_sum(x, axis=None):
+        return np.sum(x, axis=axis)
+
+    @staticmethod
+    def constant(v, dtype=None):
+        return np.array(v, dtype=dtype)
+
+    @staticmethod
+    def cast(x, dtype):
+        return np.asarray(x).astype(dtype)
+
+    @staticmethod
+    def reshape(x, shape):
+        return np.reshape(x, [int(s) for s in shape])
+
+    @staticmethod
+    def range(n, dtype=np.int32):
+        return np.arange(int(n), dtype=dtype)
+
+    @staticmethod
+    def stack(xs, axis=0):
+        return np.stack(xs, axis)
+
+    @staticmethod
+    def concat(xs, axis):
+        return np.concatenate(xs, axis)
+
+    @staticmethod
+    def tile(x, reps):
+        return np.tile(x, [int(r) for r in reps])
+
+    @staticmethod
+    def transpose(x, perm):
+        return np.transpose(x, perm)
+
+    @staticmethod
+    def slice(x, begin, size):
+        sl = tuple(slice(int(b), None if int(s) == -1 else int(b) + int(s)) for b, s in zip(begin, size))
+        return np.asarray(x)[sl]
+
+    @staticmethod
+    def gather_nd(params, indices):
+        idx = np.asarray(indices).astype(np.int64)
+        return np.asarray(params)[tuple(idx[..., k] for k in range(idx.shape[-1]))]
+
+    @staticmethod
+    def where(cond, x=None, y=None):
+        if x is None:
+            return np.argwhere(cond).astype(np.int64)   # row-major, as tf.where
+        return np.where(cond, x, y)
+
+    @staticmethod
+    def sparse_reduce_sum(sp, axis):
+        assert axis == 1
+        out = np.zeros(sp.dense_shape[0], dtype=sp.values.dtype)
+        np.add.at(out, sp.indices[:, 0], sp.values)
+        return out
+
+
+def load(name, path):
+    spec = importlib.util.spec_from_file_location(name, path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def reference_functions(params, pd):
+    def take(path, names, ns):
+        with warnings.catch_warnings():   # escape sequences in the file's docstrings
+            warnings.simplefilter("ignore", SyntaxWarning)
+            tree = ast.parse(open(path).read())
+        defs = [n for n in tree.body if isinstance(n, ast.FunctionDef) and n.name in names]
+        assert len(defs) == len(names), names
+        exec(compile(ast.Module(body=defs, type_ignores=[]), path, "exec"), ns)
+
+    ns = {"tf": _NumpyTF, "np": np, "PARAMS": params, "BOHRPERA": pd.BOHRPERA}
+    take(os.path.join(REF, "TFDescriptors", "RawSymFunc.py"),
+         ("DifferenceVectorsLinear", "AllDoublesSet", "TFCoulombEluSRDSFLR", "TFVdwPolyLR"), ns)
+    util = {"math": math, "scipy": scipy}
+    take(os.path.join(REF, "Util.py"), ("DSF", "DSF_Gradient"), util)
+    return ns, util
+
+
+def padded(x, Z, off):
+    nmol = len(off) - 1
+    n = int(np.max(np.diff(off)))
+    R = np.zeros((nmol, n, 3))
+    Zs = np.zeros((nmol, n), dtype=np.int64)
+    for m in range(nmol):
+        a, b = off[m], off[m + 1]
+        R[m, :b - a] = x[a:b]
+        Zs[m, :b - a] = Z[a:b]
+    return R, Zs
+
+
+def main():
+    pd = load("tm_ref_physicaldata", os.path.join(REF, "PhysicalData.py"))
+    params = {"EECutoffOff": 15.0, "Poly_Width": 4.6}
+    ns, util = reference_functions(params, pd)
+    b = pd.BOHRPERA
+    elu_width, dsf_alpha, ee_on = 4.6, 0.18, 0.0
+    elu_shift = util["DSF"](elu_width * b, params["EECutoffOff"] * b, dsf_alpha / b)
+    elu_alpha = util["DSF_Gradient"](elu_width * b, params["EECutoffOff"] * b, dsf_alpha / b)
+    out = {}
+    rng = np.random.default_rng(31)
+    for case, eles in (("water60", [1, 8]), ("chno6", [1, 6, 7, 8])):
+        g = np.load(os.path.join(HERE, case + ".npz"))
+        x, Z, off = g["x"], g["Z"], g["offsets"]
+        R, Zs = padded(x, Z, off)
+        q = rng.normal(0.0, 0.4, size=len(Z))
+        Qs, _ = padded(np.repeat(q[:, None], 3, 1), Z, off)
+        Qs = Qs[:, :, 0]
+        pairs = g["rad_eep"].astype(np.int64)
+        c6 = np.array([pd.C6_coff[e] * (b * 10.0) ** 6.0 / pd.JOULEPERHARTREE for e in eles])
+        rvdw = np.array([pd.atomic_vdw_radius[e] * b for e in eles])
+        Rb = R * b
+        ecc = ns["TFCoulombEluSRDSFLR"](Rb, Qs, elu_width * b, pairs, dsf_alpha, elu_alpha, elu_shift)
+        evdw = ns["TFVdwPolyLR"](Rb, Zs, np.array(eles, dtype=np.int64), c6, rvdw, ee_on * b, pairs)
+        out[case + "_q"] = q
+        out[case + "_Ecc"] = np.asarray(ecc)
+        out[case + "_Evdw"] = np.asarray(evdw)
+        print(case, "Ecc", out[case + "_Ecc"][:3], "Evdw", out[case + "_Evdw"][:3])
+    path = os.path.join(HERE, "pairs.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
+if __name__ == "__main__":
+    main()

@@ -181,3 +181,30 @@ def test_modulo_lattice_matches_reference(golden_loader, name):
     lat = g["mod_%s_lattice" % name]
     out = orc.modulo_lattice(g["mod_%s_in" % name], lat)
     np.testing.assert_allclose(out, g["mod_%s_out" % name], rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("case,eles", [("water60", [1, 8]), ("chno6", [1, 6, 7, 8])])
+def test_pair_energies_match_reference_functions(golden_loader, case, eles):
+    """Molecular Coulomb (DSF/elu) and vdW energies of the oracle against the
+    reference's own TFCoulombEluSRDSFLR and TFVdwPolyLR, run on a numpy
+    implementation of the TF ops. Both use the same seeded charges and the
+    reference's own Coulomb pair list (tests/golden/make_golden_pairs.py)."""
+    import torch
+    from tensormol_gb300.params import BOHRPERA
+    g = golden_loader(case)
+    gp = golden_loader("pairs")
+    x, Z, off = g["x"], g["Z"], g["offsets"]
+    W = systems.random_weights(eles, descriptor_width(len(eles)), seed=7)
+    model = orc.Model(eles, W)
+    pairs = g["rad_eep"].astype(np.int64)
+    ei = torch.as_tensor(off[pairs[:, 0]] + pairs[:, 1])
+    ej = torch.as_tensor(off[pairs[:, 0]] + pairs[:, 2])
+    mol = torch.as_tensor(pairs[:, 0])
+    nmol = len(off) - 1
+    Xb = torch.as_tensor(x * BOHRPERA)
+    q = torch.as_tensor(gp[case + "_q"])
+    eidx = torch.as_tensor([eles.index(int(z)) for z in Z])
+    ecc = torch.zeros(nmol, dtype=torch.float64).index_add(0, mol, model.coulomb(Xb, q, ei, ej))
+    evdw = torch.zeros(nmol, dtype=torch.float64).index_add(0, mol, model.vdw(Xb, eidx, ei, ej))
+    np.testing.assert_allclose(ecc.numpy(), gp[case + "_Ecc"], rtol=1e-12, atol=1e-15)
+    np.testing.assert_allclose(evdw.numpy(), gp[case + "_Evdw"], rtol=1e-12, atol=1e-15)
