@@ -4,9 +4,8 @@ TensorFlow-graph functions, run on a numpy implementation of the TF ops.
 ``TFCoulombEluSRDSFLR`` and ``TFVdwPolyLR`` (TFDescriptors/RawSymFunc.py:1307-1414)
 and the helpers they call, ``DifferenceVectorsLinear`` (:123-133) and
 ``AllDoublesSet`` (:63-78), are taken from the file's syntax tree and run
-unchanged. TensorFlow is absent, so ``tf`` in their namespace is the small
-numpy stand-in below: each op does what the TF 1.x op of that name does for
-the shapes these functions use. Arguments follow the reference's calls
+unchanged. TensorFlow is absent, so ``tf`` in their namespace is the numpy
+stand-in of ``numpy_tf.py`` beside this file. Arguments follow the reference's calls
 (TFBehlerParinelloSymEE.py:941, 1012):
 * positions in bohr, as a padded [nmol, maxnatom, 3] tensor;
 * charges as [nmol, maxnatom];
@@ -41,93 +40,9 @@ sys.dont_write_bytecode = True
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF = os.path.join(os.environ.get("TM_REFERENCE", "/root/reference"), "TensorMol")
+sys.path.insert(0, HERE)
 
-
-class _SparseTensor:
-    def __init__(self, indices, values, dense_shape):
-        self.indices = np.asarray(indices, dtype=np.int64)
-        self.values = np.asarray(values)
-        self.dense_shape = [int(d) for d in dense_shape]
-
-
-class _NumpyTF:
-    """The TF 1.x ops the two pair functions and their helpers call."""
-    float64, float32, int64, int32 = np.float64, np.float32, np.int64, np.int32
-    SparseTensor = _SparseTensor
-
-    @staticmethod
-    def shape(x):
-        return np.array(np.shape(x), dtype=np.int64)
-
-    sqrt = staticmethod(np.sqrt)
-    exp = staticmethod(np.exp)
-    multiply = staticmethod(np.multiply)
-    pow = staticmethod(np.power)
-    greater = staticmethod(np.greater)
-    equal = staticmethod(np.equal)
-    is_nan = staticmethod(np.isnan)
-    zeros_like = staticmethod(np.zeros_like)
-    ones_like = staticmethod(np.ones_like)
-    erfc = staticmethod(scipy.special.erfc)
-
-    @staticmethod
-    def reduce_sum(x, axis=None):
-        return np.sum(x, axis=axis)
-
-    @staticmethod
-    def constant(v, dtype=None):
-        return np.array(v, dtype=dtype)
-
-    @staticmethod
-    def cast(x, dtype):
-        return np.asarray(x).astype(dtype)
-
-    @staticmethod
-    def reshape(x, shape):
-        return np.reshape(x, [int(s) for s in shape])
-
-    @staticmethod
-    def range(n, dtype=np.int32):
-        return np.arange(int(n), dtype=dtype)
-
-    @staticmethod
-    def stack(xs, axis=0):
-        return np.stack(xs, axis)
-
-    @staticmethod
-    def concat(xs, axis):
-        return np.concatenate(xs, axis)
-
-    @staticmethod
-    def tile(x, reps):
-        return np.tile(x, [int(r) for r in reps])
-
-    @staticmethod
-    def transpose(x, perm):
-        return np.transpose(x, perm)
-
-    @staticmethod
-    def slice(x, begin, size):
-        sl = tuple(slice(int(b), None if int(s) == -1 else int(b) + int(s)) for b, s in zip(begin, size))
-        return np.asarray(x)[sl]
-
-    @staticmethod
-    def gather_nd(params, indices):
-        idx = np.asarray(indices).astype(np.int64)
-        return np.asarray(params)[tuple(idx[..., k] for k in range(idx.shape[-1]))]
-
-    @staticmethod
-    def where(cond, x=None, y=None):
-        if x is None:
-            return np.argwhere(cond).astype(np.int64)   # row-major, as tf.where
-        return np.where(cond, x, y)
-
-    @staticmethod
-    def sparse_reduce_sum(sp, axis):
-        assert axis == 1
-        out = np.zeros(sp.dense_shape[0], dtype=sp.values.dtype)
-        np.add.at(out, sp.indices[:, 0], sp.values)
-        return out
+from numpy_tf import tf as _NumpyTF  # noqa: E402
 
 
 def load(name, path):

@@ -208,3 +208,26 @@ def test_pair_energies_match_reference_functions(golden_loader, case, eles):
     evdw = torch.zeros(nmol, dtype=torch.float64).index_add(0, mol, model.vdw(Xb, eidx, ei, ej))
     np.testing.assert_allclose(ecc.numpy(), gp[case + "_Ecc"], rtol=1e-12, atol=1e-15)
     np.testing.assert_allclose(evdw.numpy(), gp[case + "_Evdw"], rtol=1e-12, atol=1e-15)
+
+
+@pytest.mark.parametrize("case,eles", [("water60", [1, 8]), ("chno6", [1, 6, 7, 8])])
+def test_descriptors_match_reference_tf_functions(golden_loader, case, eles):
+    """Descriptor rows and element partition against the reference's own
+    TFSymSet_Scattered_Linear_WithEle_Release (radial + angular TF functions,
+    run on a numpy implementation of the TF ops, fed the reference's own
+    neighbour lists; tests/golden/make_golden_desc.py). Each element's rows
+    come in (molecule, atom) order. The library's element-sorted network rows
+    use the same order. The values agree to rounding: same formulas, same
+    pi literal and clamps."""
+    g = golden_loader(case)
+    gd = golden_loader("desc")
+    x, Z, off = g["x"], g["Z"], g["offsets"]
+    W = systems.random_weights(eles, descriptor_width(len(eles)), seed=7)
+    G = orc.OpenSystemOracle(orc.Model(eles, W), x, Z, off).terms(x, grad=False)["G"]
+    maxn = int(gd[case + "_maxn"])
+    for e, z in enumerate(eles):
+        idx = gd["%s_idx%d" % (case, e)]
+        atoms = off[idx[:, 0]] + (idx[:, 1] - idx[:, 0] * maxn)
+        assert np.array_equal(atoms, np.flatnonzero(Z == z))
+        ref = gd["%s_G%d" % (case, e)]
+        np.testing.assert_allclose(G[atoms[:len(ref)]], ref, rtol=1e-12, atol=1e-14)
