@@ -1,14 +1,26 @@
 """A numpy implementation of the TensorFlow 1.x ops that the reference's
-descriptor and pair-term functions call (TFDescriptors/RawSymFunc.py), so
-that the golden-fixture scripts beside this file can run those functions
+descriptor, pair-term and network-graph functions call
+(TFDescriptors/RawSymFunc.py, TFNetworks/TFBehlerParinelloSymEE.py), so that
+the golden-fixture scripts beside this file can run those functions
 unchanged where TensorFlow is absent. Each op does what the TF op of that
 name does for the shapes those functions use: eager, FP64, no graph.
 Used only by the fixture generators, never at test time.
 """
 from __future__ import annotations
 
+import contextlib
+
 import numpy as np
 import scipy.special
+
+# Graph building: the open name scopes, and the values that tf.Variable and a
+# model's weight factory hand out, keyed by "scope/.../name"
+SCOPE = []
+VARIABLES = {}
+
+
+def scoped(name):
+    return "/".join(SCOPE + [name])
 
 
 class SparseTensor:
@@ -37,9 +49,62 @@ def constant_tensor(a, dtype=None):
     return np.asarray(a, dtype=dtype).view(Tensor)
 
 
+class _NN:
+    @staticmethod
+    def relu(x):
+        return np.maximum(x, 0.0)
+
+    @staticmethod
+    def dropout(x, keep_prob):
+        assert float(keep_prob) == 1.0, "evaluation runs with keep = 1"
+        return x
+
+
+class _GraphKeys:
+    TRAINABLE_VARIABLES = "trainable_variables"
+
+
 class tf:
     float64, float32, int64, int32, bool = np.float64, np.float32, np.int64, np.int32, np.bool_
     SparseTensor = SparseTensor
+    nn = _NN
+    GraphKeys = _GraphKeys
+    matmul = staticmethod(np.matmul)
+    add = staticmethod(np.add)
+    subtract = staticmethod(np.subtract)
+    log = staticmethod(np.log)
+
+    @staticmethod
+    @contextlib.contextmanager
+    def name_scope(name):
+        SCOPE.append(name)
+        try:
+            yield name
+        finally:
+            SCOPE.pop()
+
+    @staticmethod
+    def Variable(initial, trainable=True, dtype=None, name=None):
+        if name is not None and scoped(name) in VARIABLES:
+            return VARIABLES[scoped(name)]
+        return np.asarray(initial, dtype=dtype)
+
+    @staticmethod
+    def zeros(shape, dtype=np.float64):
+        return np.zeros([int(s) for s in shape], dtype=dtype)
+
+    @staticmethod
+    def verify_tensor_all_finite(x, msg):
+        assert np.all(np.isfinite(x)), msg
+        return x
+
+    @staticmethod
+    def cond(pred, f1, f2):
+        return f1() if bool(pred) else f2()
+
+    @staticmethod
+    def get_collection(key, scope=None):
+        return []
 
     @staticmethod
     def shape(x):

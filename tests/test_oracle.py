@@ -231,3 +231,36 @@ def test_descriptors_match_reference_tf_functions(golden_loader, case, eles):
         assert np.array_equal(atoms, np.flatnonzero(Z == z))
         ref = gd["%s_G%d" % (case, e)]
         np.testing.assert_allclose(G[atoms[:len(ref)]], ref, rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.parametrize("tag", ["c0", "c1", "c2"])
+def test_energy_terms_match_reference_graph(golden_loader, tag):
+    """Total, network, Coulomb and vdW energies, neutralised charges, dipoles
+    and per-atom network energies. They are compared with the reference's
+    own graph (SetANI1Param, the descriptor set, dipole_inference and
+    energy_inference), run on a numpy implementation of the TF ops and fed
+    its own neighbour and Coulomb lists (tests/golden/make_golden_nets.py).
+    Cases: 60-atom water with relu and with sigmoid_with_param, six CHNO
+    molecules with sigmoid_with_param. The weights are seeded with random
+    biases, and the reference's graph reads them by its own variable names."""
+    gn = golden_loader("nets")
+    case, act = str(gn[tag + "_case"]), str(gn[tag + "_act"])
+    eles = [1, 8] if case == "water60" else [1, 6, 7, 8]
+    g = golden_loader(case)
+    x, Z, off = g["x"], g["Z"], g["offsets"]
+    W = systems.random_weights(eles, descriptor_width(len(eles)), seed=7)
+    flat, k = gn[tag + "_biases"], 0
+    for net in ("E", "Q"):
+        for e in eles:
+            for li, (w, b) in enumerate(W[net][e]):
+                W[net][e][li] = (w, flat[k:k + b.size].reshape(b.shape))
+                k += b.size
+    assert k == flat.size
+    p = dict(PARAMS)
+    p["NeuronType"] = act
+    out = orc.OpenSystemOracle(orc.Model(eles, W, params=p), x, Z, off).terms(x, grad=False)
+    for key in ("Etotal", "Ebp", "Ecc", "Evdw"):
+        np.testing.assert_allclose(out[key], gn[tag + "_" + key], rtol=1e-12, atol=1e-14, err_msg=key)
+    np.testing.assert_allclose(out["dipole"], gn[tag + "_dipole"], rtol=1e-11, atol=1e-13)
+    np.testing.assert_allclose(out["charge"], gn[tag + "_charge"], rtol=1e-11, atol=1e-14)
+    np.testing.assert_allclose(out["Ebp_atom"], gn[tag + "_Ebp_atom"], rtol=1e-11, atol=1e-14)
