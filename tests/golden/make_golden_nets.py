@@ -12,7 +12,9 @@ TFVdwPolyLR and helpers) and ``sigmoid_with_param``, ``DSF`` and
 (:826-841): descriptors, then the charge network with neutralisation, dipole
 and Coulomb, then the energy network with vdW. It is fed the reference's own
 neighbour and Coulomb lists from the water60 and chno6 fixtures, with
-keep = 1 and natom = 1/N per molecule.
+keep = 1 and natom = 1/N per molecule. The 192-atom periodic water box goes
+through the periodic variants (EvalPrepare_Periodic, :1503-1621, 1671-1703,
+and the periodic descriptor and vdW functions of RawSymFunc.py).
 
 The weights are the seeded ``random_weights`` of this package with seeded
 random biases (stored here). The reference's graph code looks them up by
@@ -115,6 +117,54 @@ def padded(x, Z, off):
     return R, Zs
 
 
+def periodic_case(ns, pd, dsf, rng, act_name="sigmoid_with_param"):
+    """The 192-atom water box as EvalPrepare_Periodic wires it
+    (TFBehlerParinelloSymEE.py:1671-1703) and EvalBPDirectEEUpdateSinglePeriodic
+    feeds it (TFMolManage.py:1324-1358): the tessellated cell, real atoms first
+    (the oracle's tessellate, equal to Lattice.TessLattice bit for bit), the
+    periodic lists of the waterbox192 fixture, natom = 1/nreal."""
+    from oracle import reference as orc
+    b = pd.BOHRPERA
+    eles = [1, 8]
+    g = np.load(os.path.join(HERE, "waterbox192.npz"))
+    nreal = len(g["Z"])
+    xt = orc.tessellate(g["x"], g["lattice"], 1)
+    R = xt[None]
+    Zs = np.tile(g["Z"], xt.shape[0] // nreal)[None].astype(np.int64)
+    W = systems.random_weights(eles, descriptor_width(len(eles)), hidden=tuple(HIDDEN), seed=7)
+    biases = []
+    for net in ("E", "Q"):
+        for e in eles:
+            for li, (w, bb) in enumerate(W[net][e]):
+                nb = rng.normal(0.0, 0.05, size=bb.shape)
+                W[net][e][li] = (w, nb)
+                biases.append(nb)
+    table = _Lookups(tensormol_names(W))
+    numpy_tf.VARIABLES = table
+    inst = _Instance(eles, ns[act_name], 1, R.shape[1], dsf)
+    inst.nreal = nreal
+    ns["SetANI1Param"](inst)
+    Ele = constant_tensor(np.asarray(eles).reshape(len(eles), 1), np.int64)
+    Elep = constant_tensor(np.asarray(inst.eles_pairs), np.int64)
+    lists = [g[key].astype(np.int64) for key in ("RadpEle", "AngtEle", "mil_j", "mil_jk")]
+    sym, idx = ns["TFSymSet_Scattered_Linear_WithEle_Periodic"](
+        R, Zs, Ele, inst.SFPr2, inst.Rr_cut, Elep, inst.SFPa2, inst.zeta, inst.eta, inst.Ra_cut, *lists, nreal)
+    c6 = np.array([pd.C6_coff[e] * (b * 10.0) ** 6.0 / pd.JOULEPERHARTREE for e in eles])
+    rvdw = np.array([pd.atomic_vdw_radius[e] * b for e in eles])
+    reep5 = g["rad_eep_e1e2"].astype(np.int64)
+    keep = np.ones(len(HIDDEN) + 1)
+    natom = np.array([1.0 / nreal])
+    ecc, dipole, charge_all, _ = ns["dipole_inference_periodic"](inst, sym, idx, R, natom, 4.6, 15.0,
+                                                                 reep5[:, :3], True, keep)
+    etot, ebp, evdw, _, ebp_atom = ns["energy_inference_periodic"](inst, sym, idx, ecc, R, Zs, Ele, c6, rvdw,
+                                                                   reep5, 0.0, 15.0, keep)
+    assert table.read == set(table), sorted(set(table) - table.read)
+    print("waterbox192", act_name, "Etotal", np.asarray(etot))
+    return {"p_act": np.array(act_name), "p_biases": np.concatenate([v.ravel() for v in biases]),
+            "p_Etotal": etot, "p_Ebp": ebp, "p_Ecc": ecc, "p_Evdw": evdw, "p_dipole": dipole,
+            "p_charge": np.asarray(charge_all)[0, :nreal], "p_Ebp_atom": np.asarray(ebp_atom)[0]}
+
+
 def main():
     spec = importlib.util.spec_from_file_location("tm_ref_physicaldata", os.path.join(REF, "PhysicalData.py"))
     pd = importlib.util.module_from_spec(spec)
@@ -128,10 +178,13 @@ def main():
     take(os.path.join(REF, "TFDescriptors", "RawSymFunc.py"),
          ("DifferenceVectorsLinear", "AllSinglesSet", "AllDoublesSet", "TFSymRSet_Linear_WithEle_Release",
           "TFSymASet_Linear_WithEle", "TFSymSet_Scattered_Linear_WithEle_Release",
-          "TFCoulombEluSRDSFLR", "TFVdwPolyLR"), ns)
+          "TFCoulombEluSRDSFLR", "TFVdwPolyLR", "TFSymRSet_Linear_WithElePeriodic",
+          "TFSymASet_Linear_WithElePeriodic", "TFSymSet_Scattered_Linear_WithEle_Periodic",
+          "TFVdwPolyLRWithEle"), ns)
     take(os.path.join(REF, "Util.py"), ("DSF", "DSF_Gradient", "sigmoid_with_param"), ns)
     take(os.path.join(REF, "TFNetworks", "TFBehlerParinelloSymEE.py"),
-         ("SetANI1Param", "energy_inference", "dipole_inference"), ns,
+         ("SetANI1Param", "energy_inference", "dipole_inference", "energy_inference_periodic",
+          "dipole_inference_periodic"), ns,
          cls="MolInstance_DirectBP_EE_SymFunction")
     elu_w, dsf_alpha = 4.6, 0.18
     dsf = (dsf_alpha, ns["DSF_Gradient"](elu_w * b, 15.0 * b, dsf_alpha / b),
@@ -177,6 +230,7 @@ def main():
                     tag + "_dipole": dipole, tag + "_charge": np.asarray(charge).ravel()[real],
                     tag + "_Ebp_atom": np.asarray(ebp_atom).ravel()[real]})
         print(case, act, "Etotal", np.asarray(etot)[:3])
+    out.update(periodic_case(ns, pd, dsf, rng))
     path = os.path.join(HERE, "nets.npz")
     np.savez_compressed(path, **out)
     print("wrote", path, os.path.getsize(path), "bytes")

@@ -73,6 +73,7 @@ class tf:
     add = staticmethod(np.add)
     subtract = staticmethod(np.subtract)
     log = staticmethod(np.log)
+    div = staticmethod(np.floor_divide)   # TF 1.x integer division
 
     @staticmethod
     @contextlib.contextmanager

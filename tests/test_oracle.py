@@ -264,3 +264,31 @@ def test_energy_terms_match_reference_graph(golden_loader, tag):
     np.testing.assert_allclose(out["dipole"], gn[tag + "_dipole"], rtol=1e-11, atol=1e-13)
     np.testing.assert_allclose(out["charge"], gn[tag + "_charge"], rtol=1e-11, atol=1e-14)
     np.testing.assert_allclose(out["Ebp_atom"], gn[tag + "_Ebp_atom"], rtol=1e-11, atol=1e-14)
+
+
+def test_periodic_energy_terms_match_reference_graph(golden_loader):
+    """The periodic box: the oracle's per-cell Etotal, Ebp, Ecc, Evdw,
+    charges and dipole against the reference's own periodic graph
+    (TFSymSet_Scattered_Linear_WithEle_Periodic, dipole_inference_periodic,
+    energy_inference_periodic, TFVdwPolyLRWithEle; halved pair sums) on the
+    tessellated cell and its own periodic lists."""
+    gn = golden_loader("nets")
+    g = golden_loader("waterbox192")
+    eles = [1, 8]
+    W = systems.random_weights(eles, descriptor_width(2), seed=7)
+    flat, k = gn["p_biases"], 0
+    for net in ("E", "Q"):
+        for e in eles:
+            for li, (w, b) in enumerate(W[net][e]):
+                W[net][e][li] = (w, flat[k:k + b.size].reshape(b.shape))
+                k += b.size
+    p = dict(PARAMS)
+    p["NeuronType"] = str(gn["p_act"])
+    o = orc.PeriodicOracle(orc.Model(eles, W, params=p), g["x"], g["Z"], g["lattice"],
+                           ree_cut=float(g["ree_cut"]))
+    out = o.terms(g["x"], grad=False)
+    for key in ("Etotal", "Ebp", "Ecc", "Evdw"):
+        np.testing.assert_allclose(out[key], gn["p_" + key], rtol=1e-12, atol=1e-14, err_msg=key)
+    np.testing.assert_allclose(out["dipole"], gn["p_dipole"], rtol=1e-11, atol=1e-13)
+    np.testing.assert_allclose(out["charge"], gn["p_charge"], rtol=1e-11, atol=1e-14)
+    np.testing.assert_allclose(out["Ebp_atom"], gn["p_Ebp_atom"], rtol=1e-11, atol=1e-14)
