@@ -16,6 +16,10 @@ keep = 1 and natom = 1/N per molecule. The 192-atom periodic water box goes
 through the periodic variants (EvalPrepare_Periodic, :1503-1621, 1671-1703,
 and the periodic descriptor and vdW functions of RawSymFunc.py).
 
+For the smooth activation it also stores central differences of the
+reference's own total energy at a few atoms (lists held fixed, as
+tf.gradients differentiates the graph), which pin the oracle's forces.
+
 The weights are the seeded ``random_weights`` of this package with seeded
 random biases (stored here). The reference's graph code looks them up by
 its own variable names, and every name that ``weights.tensormol_names``
@@ -194,8 +198,8 @@ def main():
     for k, (case, eles, act) in enumerate(CASES):
         g = np.load(os.path.join(HERE, case + ".npz"))
         x, Z, off = g["x"], g["Z"], g["offsets"]
-        R, Zs = padded(x, Z, off)
-        nmol, maxn = R.shape[0], R.shape[1]
+        R0, Zs = padded(x, Z, off)
+        nmol, maxn = R0.shape[0], R0.shape[1]
         W = systems.random_weights(eles, descriptor_width(len(eles)), hidden=tuple(HIDDEN), seed=7)
         biases = []
         for net in ("E", "Q"):
@@ -211,16 +215,23 @@ def main():
         Ele = constant_tensor(np.asarray(eles).reshape(len(eles), 1), np.int64)
         Elep = constant_tensor(np.asarray(inst.eles_pairs), np.int64)
         lists = [g[key].astype(np.int64) for key in ("RadpEle", "AngtEle", "mil_j", "mil_jk")]
-        sym, idx = ns["TFSymSet_Scattered_Linear_WithEle_Release"](
-            R, Zs, Ele, inst.SFPr2, inst.Rr_cut, Elep, inst.SFPa2, inst.zeta, inst.eta, inst.Ra_cut, *lists)
         c6 = np.array([pd.C6_coff[e] * (b * 10.0) ** 6.0 / pd.JOULEPERHARTREE for e in eles])   # :719-723
         rvdw = np.array([pd.atomic_vdw_radius[e] * b for e in eles])
         reep = g["rad_eep"].astype(np.int64)
         keep = np.ones(len(HIDDEN) + 1)
         natom = 1.0 / np.diff(off).astype(np.float64)
-        ecc, dipole, charge, _ = ns["dipole_inference"](inst, sym, idx, R, natom, elu_w, 15.0, reep, True, keep)
-        etot, ebp, evdw, _, ebp_atom = ns["energy_inference"](inst, sym, idx, ecc, R, Zs, Ele, c6, rvdw, reep,
-                                                              0.0, 15.0, keep)
+
+        def graph(xx):
+            R, _ = padded(xx, Z, off)
+            sym, idx = ns["TFSymSet_Scattered_Linear_WithEle_Release"](
+                R, Zs, Ele, inst.SFPr2, inst.Rr_cut, Elep, inst.SFPa2, inst.zeta, inst.eta, inst.Ra_cut, *lists)
+            ecc, dipole, charge, _ = ns["dipole_inference"](inst, sym, idx, R, natom, elu_w, 15.0, reep, True,
+                                                            keep)
+            etot, ebp, evdw, _, ebp_atom = ns["energy_inference"](inst, sym, idx, ecc, R, Zs, Ele, c6, rvdw,
+                                                                  reep, 0.0, 15.0, keep)
+            return etot, ebp, ecc, evdw, dipole, charge, ebp_atom
+
+        etot, ebp, ecc, evdw, dipole, charge, ebp_atom = graph(x)
         assert table.read == set(table), sorted(set(table) - table.read)
         real = np.concatenate([np.arange(off[m + 1] - off[m]) + m * maxn for m in range(nmol)])
         tag = "c%d" % k
@@ -229,6 +240,17 @@ def main():
                     tag + "_Etotal": etot, tag + "_Ebp": ebp, tag + "_Ecc": ecc, tag + "_Evdw": evdw,
                     tag + "_dipole": dipole, tag + "_charge": np.asarray(charge).ravel()[real],
                     tag + "_Ebp_atom": np.asarray(ebp_atom).ravel()[real]})
+        if act != "relu":
+            # central differences of the reference's own total energy, lists
+            # held fixed (what tf.gradients differentiates), h = 1e-4 A
+            fd_atoms = np.array([0, 1, 2, 17, 44]) if case == "water60" else np.array([0, 5, 40, 120])
+            fd = np.zeros((len(fd_atoms), 3))
+            for ai, a in enumerate(fd_atoms):
+                for c in range(3):
+                    xp = x.copy(); xp[a, c] += 1e-4
+                    xm = x.copy(); xm[a, c] -= 1e-4
+                    fd[ai, c] = (np.sum(graph(xp)[0]) - np.sum(graph(xm)[0])) / 2e-4
+            out.update({tag + "_fd_atoms": fd_atoms, tag + "_fd_grad": fd})
         print(case, act, "Etotal", np.asarray(etot)[:3])
     out.update(periodic_case(ns, pd, dsf, rng))
     path = os.path.join(HERE, "nets.npz")

@@ -292,3 +292,28 @@ def test_periodic_energy_terms_match_reference_graph(golden_loader):
     np.testing.assert_allclose(out["dipole"], gn["p_dipole"], rtol=1e-11, atol=1e-13)
     np.testing.assert_allclose(out["charge"], gn["p_charge"], rtol=1e-11, atol=1e-14)
     np.testing.assert_allclose(out["Ebp_atom"], gn["p_Ebp_atom"], rtol=1e-11, atol=1e-14)
+
+
+@pytest.mark.parametrize("tag", ["c1", "c2"])
+def test_forces_match_reference_energy_differences(golden_loader, tag):
+    """The oracle's autograd gradient (the force before the -JOULEPERHARTREE
+    scale) against central differences of the reference's own total energy
+    graph (tests/golden/make_golden_nets.py; lists held fixed, h = 1e-4 A)
+    for water and CHNO molecules with the smooth activation."""
+    gn = golden_loader("nets")
+    case, act = str(gn[tag + "_case"]), str(gn[tag + "_act"])
+    eles = [1, 8] if case == "water60" else [1, 6, 7, 8]
+    g = golden_loader(case)
+    x, Z, off = g["x"], g["Z"], g["offsets"]
+    W = systems.random_weights(eles, descriptor_width(len(eles)), seed=7)
+    flat, k = gn[tag + "_biases"], 0
+    for net in ("E", "Q"):
+        for e in eles:
+            for li, (w, b) in enumerate(W[net][e]):
+                W[net][e][li] = (w, flat[k:k + b.size].reshape(b.shape))
+                k += b.size
+    p = dict(PARAMS)
+    p["NeuronType"] = act
+    out = orc.OpenSystemOracle(orc.Model(eles, W, params=p), x, Z, off).terms(x)
+    atoms = gn[tag + "_fd_atoms"]
+    np.testing.assert_allclose(out["gradient"][atoms], gn[tag + "_fd_grad"], rtol=0, atol=1e-7)
