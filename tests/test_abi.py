@@ -36,3 +36,45 @@ def test_desc_struct_layout_matches_header():
         subprocess.check_call(["gcc", "-I" + os.path.join(REPO, "include"), c, "-o", exe])
         n = int(subprocess.check_output([exe]).strip())
     assert n == ctypes.sizeof(_lib.tm_model_desc)
+
+
+def _c_class(decl):
+    """Type class of one C parameter or return type."""
+    d = decl.strip()
+    if "*" in d or "[" in d:    # an array parameter is a pointer
+        return "ptr"
+    words = d.replace("const", "").split()
+    for t, cls in (("double", "f64"), ("size_t", "size"), ("int64_t", "i64"), ("unsigned", "u32"),
+                   ("int", "i32"), ("void", "void")):
+        if t in words:
+            return cls
+    raise ValueError(decl)
+
+
+def _ctypes_class(t):
+    if t is None:
+        return "void"
+    if t in (ctypes.c_void_p, ctypes.c_char_p) or issubclass(t, ctypes._Pointer):
+        return "ptr"
+    return {ctypes.c_double: "f64", ctypes.c_size_t: "size", ctypes.c_int64: "i64",
+            ctypes.c_uint: "u32", ctypes.c_int: "i32"}[t]
+
+
+def test_ctypes_signatures_match_header():
+    """Every prototype of include/tmgpu.h against the ctypes declaration of
+    tensormol_gb300/_lib.py: return type and each parameter's class
+    (pointer, double, int, unsigned, size_t, int64_t), so that a header
+    change cannot silently desynchronise the Python side."""
+    build.build()
+    lib = _lib.load()
+    src = open(os.path.join(REPO, "include", "tmgpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    protos = re.findall(r"([A-Za-z_][A-Za-z_0-9 \t]*\**)\s*\b(tm_[a-z_0-9]+)\s*\(([^)]*)\)\s*;", src)
+    assert len(protos) == len(header_symbols())
+    for ret, name, params in protos:
+        f = getattr(lib, name)
+        args = [p for p in params.split(",") if p.strip() and p.strip() != "void"]
+        assert len(args) == len(f.argtypes), (name, args, f.argtypes)
+        assert _c_class(ret) == _ctypes_class(f.restype), (name, ret, f.restype)
+        for a, t in zip(args, f.argtypes):
+            assert _c_class(a) == _ctypes_class(t), (name, a, t)
