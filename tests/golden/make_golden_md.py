@@ -7,7 +7,9 @@ star-imports replaced by stubs (numpy, PARAMS, the gas constant of the
 reference's own PhysicalData.py), on a 60-atom water cluster in the
 ``anharmonic_wells`` force field of the oracle. The thermostats' constructors
 rescale the starting velocities in place (SimpleMD.py:82-88); the rescaled
-velocities are stored as each run's start. Writes ``tests/golden/md_simplemd.npz``.
+velocities are stored as each run's start. It also runs the driver
+``VelocityVerlet.Prop`` (SimpleMD.py:322-424), NVE from the same start, and
+stores its ``md_log``. Writes ``tests/golden/md_simplemd.npz``.
 
 Usage (where the reference tree is present): python tests/golden/make_golden_md.py
 """
@@ -58,7 +60,16 @@ def load_simplemd(params):
         m.__path__ = []
         sys.modules["TensorMol." + sub] = m
     phys = load("TensorMol.PhysicalData", os.path.join(REF, "PhysicalData.py"))
-    common = {"np": np, "PARAMS": params, "IDEALGASR": phys.IDEALGASR}
+
+    class _Logger:
+        def info(self, *a, **k):
+            pass
+
+    common = {"np": np, "PARAMS": params, "IDEALGASR": phys.IDEALGASR,
+              "ATOMICMASSES": phys.ATOMICMASSES, "JOULEPERHARTREE": phys.JOULEPERHARTREE,
+              "KJPERHARTREE": phys.KJPERHARTREE, "time": __import__("time"), "LOGGER": _Logger(),
+              # running energy statistics of Prop, never logged (Math/Statistics.py)
+              "OnlineEstimator": lambda e0: (lambda e: (0.0, 0.0))}
     for name in ("TensorMol.Containers.Sets", "TensorMol.TFNetworks.TFManage",
                  "TensorMol.ForceModels.Electrostatics", "TensorMol.Math.QuasiNewtonTools",
                  "TensorMol.Math.Statistics"):
@@ -121,6 +132,34 @@ def main():
             x, v, a, e = th.step(None, a, x, v, m, DT, ef)
         X.append(x); V.append(v); ETA.append(th.eta.copy()); VETA.append(th.Veta.copy())
     out.update(nhc_x=np.array(X), nhc_v=np.array(V), nhc_eta=np.array(ETA), nhc_veta=np.array(VETA))
+
+    # the driver's log: VelocityVerlet.Prop (SimpleMD.py:391-424), NVE, zero
+    # starting velocities, energies in Hartree (the wells' J/mol scaled), run in
+    # a scratch directory because Prop saves ./results/MDLog<name>.txt
+    import tempfile
+
+    class _G0:
+        atoms = np.asarray(systems.water_cluster_60(seed=0).Z)
+        coords = xs.copy()
+
+    jph = smd.JOULEPERHARTREE   # the reference's own constant
+
+    def ef_h(x):
+        e, f = ef(x)
+        return e / jph, f
+
+    params.update(MDMaxStep=20, MDV0=None, MDThermostat=None, MDLogTrajectory=False)
+    here = os.getcwd()
+    with tempfile.TemporaryDirectory() as d:
+        os.chdir(d)
+        os.makedirs("results")
+        try:
+            with contextlib.redirect_stdout(io.StringIO()):
+                vv = smd.VelocityVerlet(None, _G0(), "w60", ef_h)
+                vv.Prop()
+        finally:
+            os.chdir(here)
+    out.update(prop_md_log=vv.md_log, prop_x=vv.x, prop_v=vv.v, prop_nsteps=20)
 
     for key in list(out):
         if key.startswith(("vv_", "nose_", "nhc_")) and not key.endswith("_v0"):
