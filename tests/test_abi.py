@@ -78,3 +78,20 @@ def test_ctypes_signatures_match_header():
         assert _c_class(ret) == _ctypes_class(f.restype), (name, ret, f.restype)
         for a, t in zip(args, f.argtypes):
             assert _c_class(a) == _ctypes_class(t), (name, a, t)
+
+
+def test_product_does_not_use_the_oracle():
+    """The package (Python and CUDA sources) never imports, links or names
+    the oracle: the oracle checks results, it is never the thing measured or
+    shipped, and without the CUDA library every call raises."""
+    pkg = os.path.join(REPO, "tensormol_gb300")
+    hits = []
+    for root, _, files in os.walk(pkg):
+        if "__pycache__" in root or "_build" in root:
+            continue
+        for f in files:
+            if f.endswith((".py", ".cu", ".cuh", ".h", ".cpp", ".c")):
+                text = open(os.path.join(root, f), encoding="utf-8").read()
+                if re.search(r"\boracle\b|tmoracle", text):
+                    hits.append(os.path.relpath(os.path.join(root, f), REPO))
+    assert hits == [], hits
