@@ -151,22 +151,39 @@ def periodic_case(ns, pd, dsf, rng, act_name="sigmoid_with_param"):
     Ele = constant_tensor(np.asarray(eles).reshape(len(eles), 1), np.int64)
     Elep = constant_tensor(np.asarray(inst.eles_pairs), np.int64)
     lists = [g[key].astype(np.int64) for key in ("RadpEle", "AngtEle", "mil_j", "mil_jk")]
-    sym, idx = ns["TFSymSet_Scattered_Linear_WithEle_Periodic"](
-        R, Zs, Ele, inst.SFPr2, inst.Rr_cut, Elep, inst.SFPa2, inst.zeta, inst.eta, inst.Ra_cut, *lists, nreal)
     c6 = np.array([pd.C6_coff[e] * (b * 10.0) ** 6.0 / pd.JOULEPERHARTREE for e in eles])
     rvdw = np.array([pd.atomic_vdw_radius[e] * b for e in eles])
     reep5 = g["rad_eep_e1e2"].astype(np.int64)
     keep = np.ones(len(HIDDEN) + 1)
     natom = np.array([1.0 / nreal])
-    ecc, dipole, charge_all, _ = ns["dipole_inference_periodic"](inst, sym, idx, R, natom, 4.6, 15.0,
-                                                                 reep5[:, :3], True, keep)
-    etot, ebp, evdw, _, ebp_atom = ns["energy_inference_periodic"](inst, sym, idx, ecc, R, Zs, Ele, c6, rvdw,
-                                                                   reep5, 0.0, 15.0, keep)
+
+    def graph(RR):
+        sym, idx = ns["TFSymSet_Scattered_Linear_WithEle_Periodic"](
+            RR, Zs, Ele, inst.SFPr2, inst.Rr_cut, Elep, inst.SFPa2, inst.zeta, inst.eta, inst.Ra_cut, *lists,
+            nreal)
+        ecc, dipole, charge_all, _ = ns["dipole_inference_periodic"](inst, sym, idx, RR, natom, 4.6, 15.0,
+                                                                     reep5[:, :3], True, keep)
+        etot, ebp, evdw, _, ebp_atom = ns["energy_inference_periodic"](inst, sym, idx, ecc, RR, Zs, Ele, c6,
+                                                                       rvdw, reep5, 0.0, 15.0, keep)
+        return etot, ebp, ecc, evdw, dipole, charge_all, ebp_atom
+
+    etot, ebp, ecc, evdw, dipole, charge_all, ebp_atom = graph(R)
     assert table.read == set(table), sorted(set(table) - table.read)
+    # the reference's returned periodic force is tf.gradients with respect to
+    # the real rows of the tessellated input, images held fixed
+    # (TFMolManage.py:1353): central differences moving those rows alone
+    fd_atoms = np.array([0, 1, 2, 100])
+    fd = np.zeros((len(fd_atoms), 3))
+    for ai, a in enumerate(fd_atoms):
+        for c in range(3):
+            Rp = R.copy(); Rp[0, a, c] += 1e-4
+            Rm = R.copy(); Rm[0, a, c] -= 1e-4
+            fd[ai, c] = (np.sum(graph(Rp)[0]) - np.sum(graph(Rm)[0])) / 2e-4
     print("waterbox192", act_name, "Etotal", np.asarray(etot))
     return {"p_act": np.array(act_name), "p_biases": np.concatenate([v.ravel() for v in biases]),
             "p_Etotal": etot, "p_Ebp": ebp, "p_Ecc": ecc, "p_Evdw": evdw, "p_dipole": dipole,
-            "p_charge": np.asarray(charge_all)[0, :nreal], "p_Ebp_atom": np.asarray(ebp_atom)[0]}
+            "p_charge": np.asarray(charge_all)[0, :nreal], "p_Ebp_atom": np.asarray(ebp_atom)[0],
+            "p_fd_atoms": fd_atoms, "p_fd_grad_real_rows": fd}
 
 
 def main():

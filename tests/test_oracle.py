@@ -317,3 +317,34 @@ def test_forces_match_reference_energy_differences(golden_loader, tag):
     out = orc.OpenSystemOracle(orc.Model(eles, W, params=p), x, Z, off).terms(x)
     atoms = gn[tag + "_fd_atoms"]
     np.testing.assert_allclose(out["gradient"][atoms], gn[tag + "_fd_grad"], rtol=0, atol=1e-7)
+
+
+def test_periodic_reference_force_matches_reference_energy_differences(golden_loader):
+    """The reference's returned periodic force is the gradient with respect
+    to the real rows of the tessellated input, images held fixed
+    (TFMolManage.py:1353). The oracle's force_ref, which
+    TM_F_REFERENCE_PERIODIC_FORCE reproduces on the GPU, must match central
+    differences of the reference's own periodic energy graph that move only
+    those rows. The conservative force, images moving with their atoms, is a
+    different quantity."""
+    from tensormol_gb300.params import JOULEPERHARTREE
+    gn = golden_loader("nets")
+    g = golden_loader("waterbox192")
+    eles = [1, 8]
+    W = systems.random_weights(eles, descriptor_width(2), seed=7)
+    flat, k = gn["p_biases"], 0
+    for net in ("E", "Q"):
+        for e in eles:
+            for li, (w, b) in enumerate(W[net][e]):
+                W[net][e][li] = (w, flat[k:k + b.size].reshape(b.shape))
+                k += b.size
+    p = dict(PARAMS)
+    p["NeuronType"] = str(gn["p_act"])
+    o = orc.PeriodicOracle(orc.Model(eles, W, params=p), g["x"], g["Z"], g["lattice"],
+                           ree_cut=float(g["ree_cut"]))
+    out = o.terms(g["x"])
+    atoms = gn["p_fd_atoms"]
+    grad_ref = -out["force_ref"][atoms] / JOULEPERHARTREE
+    fd = gn["p_fd_grad_real_rows"]
+    np.testing.assert_allclose(grad_ref, fd, rtol=0, atol=1e-7)
+    assert np.abs(out["gradient"][atoms] - fd).max() > 1e-4
