@@ -18,7 +18,8 @@ forward and backward, pair terms, forces).
   cpu_baseline  the FP64 oracle on the host cores (one full E+F)
 
 ``--impl reference`` times the CPU implementation of the path (the oracle
-port: the reference's TensorFlow graph cannot run here) on a bounded sample.
+port: the reference's TensorFlow graph cannot run here) on the same 24,000-atom
+cube, one full E+F per step.
 Multi-GPU runs are independent replicas (the path does not shard).
 """
 from __future__ import annotations
@@ -194,28 +195,35 @@ def time_plain(model, W, w, steps, warmup, torch):
     pl = PlainAutograd(model, W)
     x = torch.tensor(w.x, dtype=torch.float64, device="cuda")
 
-    def step():
+    for _ in range(warmup):
         s.build_nlist()
         pl.prepare(s)
-        return pl.energy_force(x)
-    for _ in range(warmup):
-        step()
+        pl.energy_force(x)
     torch.cuda.synchronize()
-    times = []
+    times, t_lists, t_graph = [], [], []
     E = F = None
     for _ in range(steps):
         a = torch.cuda.Event(enable_timing=True)
+        m = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record()
-        E, F = step()
+        # lists: the library's build, exported to index tensors (as the
+        # reference's graph is fed its lists by the host)
+        s.build_nlist()
+        pl.prepare(s)
+        m.record()
+        # the framework-op graph and torch.autograd.grad
+        E, F = pl.energy_force(x)
         b.record()
         b.synchronize()
         times.append(a.elapsed_time(b))
+        t_lists.append(a.elapsed_time(m))
+        t_graph.append(m.elapsed_time(b))
     out = (E.cpu().numpy(), F.cpu().numpy())
     s.close()
     del pl
     torch.cuda.empty_cache()
-    return times, out
+    return times, out, t_lists, t_graph
 
 
 def oracle_eval(w, eles, W):
@@ -236,6 +244,38 @@ def errors(E, F, ref, natoms):
     return {"dE_per_atom_eV": dE, "max_dF_eV_per_A": float(per_atom.max()),
             "p999_dF_eV_per_A": float(np.quantile(per_atom, 0.999)),
             "frac_atoms_within_1e-4": float(np.mean(per_atom < 1e-4))}
+
+
+def relu_decisions(model, w, eles, W, ref):
+    """The fused FP32 path's relu decisions (sign of every hidden pre-activation,
+    from the layer outputs of an energy-only evaluation) against the FP64
+    oracle's: how many differ, and how close to the kink the differing units
+    lie (|z| / sum|a||w| of the exact pre-activation)."""
+    s = model.system(w.x, w.Z, w.offsets)
+    s.energy_force(w.x, False)
+    refined = s.refined_units()
+    outs = [s.layer_outputs(l) for l in range(len(model.p["HiddenLayers"]))]
+    s.close()
+    Z = np.asarray(w.Z)
+    rel, total = [], 0
+    for ni, net in enumerate(("E", "Q")):
+        for e in eles:
+            idx = np.nonzero(Z == e)[0]
+            h = ref["G"][idx]
+            for li, (Wm, b) in enumerate(W[net][e][:-1]):
+                Wm = np.asarray(Wm, np.float64)
+                b = np.asarray(b, np.float64).reshape(-1)
+                z = h @ Wm + b
+                sc = np.abs(h) @ np.abs(Wm) + np.abs(b)
+                o = outs[li][ni][idx]
+                on = o != 0 if li == len(outs) - 1 else o > 0
+                bad = on != (z > 0)
+                rel.extend((np.abs(z[bad]) / sc[bad]).tolist())
+                total += z.size
+                h = np.maximum(z, 0.0)
+    return {"units": total, "differing_from_fp64": len(rel),
+            "max_rel_distance_of_differing": max(rel, default=0.0),
+            "refined_in_fp64_class_arithmetic": refined}
 
 
 def smooth_accuracy(w, eles, flush, torch):
@@ -291,7 +331,32 @@ def serve_requests(specs):
             for (Z, x, kind, v) in specs]
 
 
-def time_md(model_fp32, torch):
+def box_snapshot_accuracy(W, box, lat, x0):
+    """The 12,288-atom box at its initial positions: BF16 and FP32 networks
+    against each other and against the FP64 oracle (27-image tessellation),
+    the same relu networks as the MD runs."""
+    from oracle import reference as orc
+    from tensormol_gb300.model import BPEEModel
+    from tensormol_gb300.params import PARAMS
+    out = {}
+    for prec in ("bf16", "fp32"):
+        m = BPEEModel([1, 8], W, params=dict(PARAMS), precision=prec)
+        s = m.system(x0, box.Z, None, lat)
+        out[prec] = s.energy_force(x0, True)
+        s.close()
+        m.close()
+    import torch
+    torch.set_num_threads(os.cpu_count() or 1)
+    ref = orc.PeriodicOracle(orc.Model([1, 8], W, dict(PARAMS)), x0, box.Z, lat).terms(x0)
+    n = box.natoms
+    return {"fp32_vs_fp64": errors(out["fp32"]["Etotal"], out["fp32"]["force"], ref, n),
+            "bf16_vs_fp64": errors(out["bf16"]["Etotal"], out["bf16"]["force"], ref, n),
+            "bf16_vs_fp32": errors(out["bf16"]["Etotal"], out["bf16"]["force"],
+                                   {"Etotal": out["fp32"]["Etotal"], "force": out["fp32"]["force"]}, n),
+            "snapshot": "initial positions (wrapped), relu networks with output layers scaled by 0.01"}
+
+
+def time_md(model_fp32, torch, oracle=True):
     """The MD workloads: (1) the 60-atom cluster, one E+F then 100 NVE steps of
     0.5 fs, FP32 networks; (2) the 12,288-atom periodic box (49.7 A), 1,000 Nose-Hoover-chain
     (length 3) steps at 300 K, dt 0.5 fs, BF16 networks, 1.0 A neighbour skin,
@@ -363,6 +428,8 @@ def time_md(model_fp32, torch):
         s.close()
         m.close()
     out["waterbox12288_nhc3_1000"] = res
+    if oracle:
+        res["snapshot_accuracy"] = box_snapshot_accuracy(W, box, lat, x0)
     out["note"] = ("periodic box: 1.0 A skin lists (candidates rebuilt on displacement, exact "
                    "rows filtered every step); 60-atom cluster: a full build every step; drift is the "
                    "least-squares slope of the extended-system conserved energy over the run; "
@@ -475,7 +542,9 @@ def time_serving(max_atoms=32768, max_mols=256, loads=(0.25, 0.5, 1.1, 1.5, 3.0)
 
 
 def run_reference(args):
-    """CPU implementation of the path (the oracle port), bounded sample."""
+    """CPU implementation of the path (the oracle port) on the same workload as
+    the GPU arm: one full E+F of the 24,000-atom cube per step (lists, FP64
+    descriptors, networks, pair terms, autograd forces), all host threads."""
     ws, rank, _ = _dist()
     if rank != 0:
         return 0
@@ -485,7 +554,7 @@ def run_reference(args):
     from oracle import reference as orc
     from tensormol_gb300 import systems
     from tensormol_gb300.params import PARAMS, descriptor_width
-    sample = systems.water(1000, seed=1, spacing=3.1)   # 3,000-atom piece of the same lattice
+    sample = systems.water_cube_24k(seed=1)   # the GPU arm's system
     eles = [1, 8]
     W = systems.random_weights(eles, descriptor_width(2), seed=7)
     model = orc.Model(eles, W, dict(PARAMS))
@@ -508,9 +577,9 @@ def run_reference(args):
             "config": {"workload": WORKLOAD, "elements": [1, 8], "hidden": [512, 512, 512],
                        "activation": "relu"},
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": ncores, "kind": "port",
-                             "sample": "one E+F per step of a 3,000-atom (1,000 H2O) cube of the "
-                                       "same generator, FP64 oracle (PyTorch-CPU autograd; C "
-                                       "neighbour lists); the reference's TensorFlow graph "
+                             "sample": "one full E+F per step of the 24,000-atom cube (the "
+                                       "GPU arm's workload), FP64 oracle (PyTorch-CPU autograd; "
+                                       "C neighbour lists); the reference's TensorFlow graph "
                                        "cannot run without TensorFlow"},
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -574,7 +643,7 @@ def main():
     e2e_ms = sum(e2e_t) / len(e2e_t)
     s.close()
     serving = None if args.no_serve else time_serving()
-    md_runs = None if args.no_md else time_md(model, torch)
+    md_runs = None if args.no_md else time_md(model, torch, oracle=not args.no_cpu)
     chno = time_chno512(args.steps, flush, torch)
     # BF16 variant
     _, _, _, model16 = build_workload("bf16")
@@ -584,10 +653,14 @@ def main():
     model16.close()
     plain = None
     if not args.no_plain:
-        pt, (Ep, Fp) = time_plain(model, W, w, max(2, min(args.steps, 3)), 2, torch)
-        plain = {"ms_per_step": sum(pt) / len(pt)}
+        pt, (Ep, Fp), pls, plg = time_plain(model, W, w, max(2, min(args.steps, 3)), 2, torch)
+        plain = {"ms_per_step": sum(pt) / len(pt), "lists_ms": sum(pls) / len(pls),
+                 "autograd_graph_ms": sum(plg) / len(plg)}
         plain["value"] = w.natoms / (plain["ms_per_step"] / 1000.0)
         plain["speedup_fused_vs_plain"] = plain["ms_per_step"] / ms
+        # the same lists in both arms: plain's graph + autograd against the
+        # fused evaluation without its own list stage
+        plain["speedup_fused_vs_plain_graph_only"] = plain["autograd_graph_ms"] / (ms - stages["nlist"])
     # roofline: the six network GEMM launches per E+F
     peak, hbm, src = _peaks()
     natoms = w.natoms
@@ -654,6 +727,7 @@ def main():
         if plain is not None:
             acc["plain_autograd"] = errors(Ep, Fp, ref, natoms)
         acc["activation"] = "relu"
+        acc["relu_decisions"] = relu_decisions(model, w, eles, W, ref)
         acc["fused_fp32_sigmoid_with_param"] = smooth_accuracy(w, eles, flush, torch)
         line["accuracy_vs_fp64_oracle"] = acc
     if ws > 1:

@@ -241,7 +241,13 @@ int tm_serve_read(tm_serve *sv, int mol, double *x, double *v, double *F);
  * device arena, or a serving process whose memory is budgeted up front. It
  * allocates nothing (no cudaMalloc/cudaFree, no allocating library routine);
  * its scratch is one file-scope device array sized for at most 32768 atoms
- * (about 2 MB, reserved on every GPU that loads the library until exit).
+ * (about 2 MB, held on every GPU that loads it until exit). With CUDA's lazy
+ * module loading (the default) that memory is committed by the first call of
+ * this entry point on each device, or by the first neighbour-list build
+ * there: make one small call before sizing a fixed arena from the free
+ * memory. The scratch's device address is looked up once per device, in the
+ * context current at that first call (the primary context); do not use this
+ * entry point after cudaDeviceReset in the same process.
  *
  * All array arguments are device pointers the caller allocated: x[natoms][3]
  * (Angstrom, FP64), elem[natoms] (element index, 0-based, sorted by Z as in the
@@ -270,6 +276,16 @@ int tm_nlist_build_static(const double *x, const int32_t *elem, int natoms, doub
 int tm_selftest_gemm(tm_ctx *ctx, int precision, int M, int N, int K, const float *A,
                      const float *B, float *C);
 /*
+ * Exercises the bounded waits of the tensor-core layer kernel: a 256 x 256 x 256
+ * selftest product in which the operand loads of one pipeline stage are never
+ * issued (nothing faults: the copy does not exist) and every wait is limited to
+ * wait_cycles SM cycles (1 .. 2^28). Returns TM_E_TIMEOUT when the waits ran out
+ * as designed: the kernel has then freed its tensor memory and returned, and the
+ * context (its status word cleared) runs the next call normally. No counterpart
+ * in the reference (it has no GPU kernels).
+ */
+int tm_selftest_gemm_timeout(tm_ctx *ctx, int precision, int64_t wait_cycles);
+/*
  * The polynomial the pair kernel evaluates erfc with on this model's DSF range
  * (erfc(x) = exp(-x^2) P(t), t = x * scale + offset in [-1, 1], x = alpha r
  * for r from the elu width to the Coulomb cutoff, in bohr): coeffs[11]
@@ -284,6 +300,23 @@ int tm_model_erfc_poly(const tm_model *m, float *coeffs, int *n, float *scale, f
  * TFSymSet_Scattered_Linear_WithEle_Release's SymList (RawSymFunc.py:2267-2309).
  */
 int tm_system_descriptors(tm_system *s, float *G_out);
+/*
+ * The outputs of hidden layer `layer` (0 .. n_hidden-1) of both networks from
+ * the last evaluation, out[2][natoms][hidden[layer]] (net 0 = energy, 1 =
+ * charge; atoms in input order): the activations h = act(z) of a hidden layer
+ * before the last, and w_out * act'(z) (the backward pass's seed) for the last
+ * one. Valid after an evaluation with TM_F_ENERGY_ONLY (the backward pass
+ * reuses these buffers). No counterpart in the reference (TensorFlow keeps
+ * its intermediate tensors internal).
+ */
+int tm_system_layer_outputs(tm_system *s, int layer, float *out);
+/*
+ * FP32 mode with relu: the number of hidden-unit pre-activations that the
+ * last evaluation recomputed in FP64 because they lay within the tensor-core
+ * error bound of the kink (0 in other modes). No counterpart in the reference
+ * (its FP64 TensorFlow graph has no such step).
+ */
+int tm_system_refined_units(tm_system *s, int64_t *n);
 /*
  * One energy(+force) evaluation of the resident positions with CUDA events on
  * the ctx stream between stages; stage_ms[7] = (lists, descriptors, network

@@ -1,11 +1,12 @@
 #!/bin/sh
 # Builds the reference's MolEmb extension from its own source tree into
-# oracle/_ref/ (git-ignored). Needs the reference tree at $TM_REFERENCE
-# (default /root/reference); where it is absent the script exits 0 and prints
-# why, and the oracle restatement is used alone.
+# oracle/_ref/ (git-ignored). Needs the reference tree at $TM_REFERENCE, or
+# else in a `reference` directory beside the repository checkout; where it is
+# absent the script exits 0 and prints why, and the oracle restatement is used
+# alone.
 set -e
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${TM_REFERENCE:-/root/reference}"
+REF="${TM_REFERENCE:-$(cd "$HERE/../.." && pwd)/reference}"
 SRC="$REF/C_API/MolEmb.cpp"
 if [ ! -f "$SRC" ]; then
   echo "build_ref: reference source not present ($SRC); skipping"

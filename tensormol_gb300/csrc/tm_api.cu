@@ -260,6 +260,25 @@ extern "C" int tm_model_create(tm_ctx* ctx, const tm_model_desc* d, tm_model** o
     k.sin_th[n] = (float)sin(th);
   }
   k.two_1mz = (float)pow(2.0, 1.0 - d->zeta);
+  auto lo_of = [](double v) { return (float)(v - (double)(float)v); };
+  for (int n = 0; n < k.nr; ++n) k.rs_r_lo[n] = lo_of(d->r_rc * n / k.nr);
+  for (int n = 0; n < 8; ++n) {
+    const double th = 2.0 * M_PI * n / 8.0;
+    k.rs_a_lo[n] = lo_of(d->a_rc * n / 8.0);
+    k.cos_th_lo[n] = lo_of(cos(th));
+    k.sin_th_lo[n] = lo_of(sin(th));
+  }
+  k.r_rc_hi = (float)d->r_rc;
+  k.r_rc_lo = lo_of(d->r_rc);
+  k.a_rc_hi = (float)d->a_rc;
+  k.a_rc_lo = lo_of(d->a_rc);
+  // 0.5 (cos(pi_tf r / Rc) + 1) = sin^2(pi_tf (Rc - r) / (2 Rc) + (pi - pi_tf) / 2);
+  // |pi - pi_tf| / 2 < 1.1e-13 is dropped
+  const double cr = 3.14159265359 / (2.0 * d->r_rc), ca = 3.14159265359 / (2.0 * d->a_rc);
+  k.cr_hi = (float)cr;
+  k.cr_lo = lo_of(cr);
+  k.ca_hi = (float)ca;
+  k.ca_lo = lo_of(ca);
   int p = 0;
   for (int a = 0; a < k.nele; ++a)
     for (int b = a; b < k.nele; ++b) {
@@ -369,6 +388,8 @@ extern "C" int tm_model_finalize(tm_model* m) {
     return m->layers[((size_t)net * nele + e) * (L + 1) + l];
   };
   int rc;
+  // relu kinks: FP32 mode recomputes near-kink units in FP64 (tm_gemm.cu)
+  m->kink = m->desc.precision == TM_PREC_FP32 && m->desc.activation == TM_ACT_RELU;
   for (int l = 0; l < L; ++l) {
     const int Kin = l == 0 ? Dp : H;
     std::vector<float> fwd((size_t)2 * nele * H * Kin, 0.f), bwd((size_t)2 * nele * Kin * H, 0.f);
@@ -386,6 +407,45 @@ extern "C" int tm_model_finalize(tm_model* m) {
         for (int o = 0; o < Lh.fan_out; ++o) bias[blk * H + o] = (float)Lh.b[o];
       }
     if ((rc = upload_split(m, fwd, m->w_fwd[l])) || (rc = upload_split(m, bwd, m->w_bwd[l]))) return rc;
+    if (m->kink) {
+      // the weights and biases as given (FP64) and the norm of each unit's
+      // weight vector, for the relu refinement (tm_gemm.cu)
+      std::vector<float2> w2((size_t)2 * nele * H * Kin, make_float2(0.f, 0.f)),
+          b2((size_t)2 * nele * H, make_float2(0.f, 0.f));
+      auto pair = [](double v) {
+        const float h = (float)v;
+        return make_float2(h, (float)(v - (double)h));
+      };
+      std::vector<float> wn((size_t)2 * nele * H, 0.f);
+      for (int net = 0; net < 2; ++net)
+        for (int e = 0; e < nele; ++e) {
+          const tm_layer_host& Lh = layer(net, e, l);
+          const size_t blk = (size_t)net * nele + e;
+          for (int o = 0; o < Lh.fan_out; ++o) {
+            double ss = 0.0;
+            for (int i = 0; i < Lh.fan_in; ++i) {
+              const double w = Lh.W[(size_t)i * Lh.fan_out + o];
+              w2[(blk * H + o) * Kin + i] = pair(w);
+              ss += w * w;
+            }
+            wn[blk * H + o] = (float)sqrt(ss);
+            b2[blk * H + o] = pair(Lh.b[o]);
+          }
+        }
+      if (m->kw2[l]) {   // finalized before: replace
+        tm_free(ctx, m->kw2[l], w2.size() * 8);
+        tm_free(ctx, m->kb2[l], b2.size() * 8);
+        tm_free(ctx, m->kwn[l], wn.size() * 4);
+      }
+      if ((rc = tm_alloc(ctx, (void**)&m->kw2[l], w2.size() * 8)) ||
+          (rc = tm_alloc(ctx, (void**)&m->kb2[l], b2.size() * 8)) ||
+          (rc = tm_alloc(ctx, (void**)&m->kwn[l], wn.size() * 4)))
+        return rc;
+      cudaMemcpyAsync(m->kw2[l], w2.data(), w2.size() * 8, cudaMemcpyHostToDevice, ctx->stream);
+      cudaMemcpyAsync(m->kb2[l], b2.data(), b2.size() * 8, cudaMemcpyHostToDevice, ctx->stream);
+      cudaMemcpyAsync(m->kwn[l], wn.data(), wn.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
+      if ((rc = tm_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "finalize"))) return rc;
+    }
     if ((rc = tm_alloc(ctx, (void**)&m->bias[l], bias.size() * 4))) return rc;
     cudaMemcpyAsync(m->bias[l], bias.data(), bias.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
     const int eb = (int)m->elem_size;
@@ -428,6 +488,11 @@ extern "C" int tm_model_destroy(tm_model* m) {
       tm_free(ctx, m->w_bwd[l][s], n);
     }
     tm_free(ctx, m->bias[l], (size_t)2 * nele * H * 4);
+    if (m->kw2[l]) {
+      tm_free(ctx, m->kw2[l], (size_t)2 * nele * H * Kin * 8);
+      tm_free(ctx, m->kb2[l], (size_t)2 * nele * H * 8);
+      tm_free(ctx, m->kwn[l], (size_t)2 * nele * H * 4);
+    }
   }
   tm_free(ctx, m->wout, (size_t)2 * nele * H * 4);
   tm_free(ctx, m->bout, (size_t)2 * nele * 8);
@@ -536,9 +601,11 @@ static int build_layout(tm_system* s, int N, int nmol, const int32_t* Z, const i
 // Zero the descriptor rows of the padding rows (atom_of_row < 0), so that
 // rows left from an earlier layout never reach the networks.
 __global__ void k_zero_pad_rows(const int32_t* __restrict__ atom_of_row, int Mpad, int Dp,
-                                float* __restrict__ g0, float* __restrict__ g1, int words) {
+                                float* __restrict__ g0, float* __restrict__ g1, int words,
+                                float* __restrict__ gnorm2) {
   const int r = blockIdx.x;
   if (r >= Mpad || atom_of_row[r] >= 0) return;
+  if (gnorm2 && threadIdx.x == 0) gnorm2[r] = 0.f;
   for (int c = threadIdx.x; c < words; c += blockDim.x) {
     g0[(size_t)r * words + c] = 0.f;
     if (g1) g1[(size_t)r * words + c] = 0.f;
@@ -606,7 +673,7 @@ static int upload_layout(tm_system* s, SysLayout& L) {
   const bool split = m->desc.precision == TM_PREC_FP32;
   const int words = (int)(m->k.Dp * m->elem_size / 4);
   k_zero_pad_rows<<<L.Mpad, 128, 0, st>>>(s->atom_of_row, L.Mpad, m->k.Dp, (float*)s->G[0],
-                                          split ? (float*)s->G[1] : nullptr, words);
+                                          split ? (float*)s->G[1] : nullptr, words, s->kink_g2);
   ctx->launches++;
   return tm_cuda_check(ctx, cudaGetLastError(), "system upload");
 }
@@ -692,6 +759,14 @@ static int system_alloc(tm_system* s, int N_cap, int nmol_cap, int Mpad_cap, int
   }
   A.get(&s->dEdG, sizeof(float) * 2 * Mp * Dp);
   A.get(&s->epart, sizeof(float) * 2 * Mp * (H / tm_gemm_bn(m->desc.precision)));
+  if (m->kink) {
+    const size_t parts = H / tm_gemm_bn(m->desc.precision);
+    A.get(&s->kink_g2, sizeof(float) * Mp);
+    A.get(&s->kink_h2[0], sizeof(float) * 2 * Mp * parts);
+    A.get(&s->kink_h2[1], sizeof(float) * 2 * Mp * parts);
+    A.get(&s->kink_mask, sizeof(uint32_t) * 2 * Mp * (H / 32));
+    A.get(&s->kink_count, sizeof(unsigned long long));
+  }
   A.get(&s->d_Eatom, sizeof(double) * N);
   A.get(&s->d_qraw, sizeof(float) * N);
   A.get(&s->d_q, sizeof(float) * N);
@@ -709,6 +784,8 @@ static int system_alloc(tm_system* s, int N_cap, int nmol_cap, int Mpad_cap, int
     cudaMemsetAsync(s->G[h], 0, Mp * Dp * es, st);
   }
   cudaMemsetAsync(s->d_x, 0, sizeof(double) * 3 * N, st);
+  if (s->kink_g2) cudaMemsetAsync(s->kink_g2, 0, sizeof(float) * Mp, st);
+  if (s->kink_count) cudaMemsetAsync(s->kink_count, 0, sizeof(unsigned long long), st);
   int rc;
   if ((rc = tm_cuda_check(ctx, cudaStreamSynchronize(st), "system alloc"))) return rc;
   const int eb = (int)es;
@@ -815,7 +892,8 @@ static void system_free(tm_system* s) {
                   s->d_cell_cnt, s->d_cell_start, s->d_cell_atoms, s->d_cell_of_atom, s->d_cnt_r,
                   s->d_cnt_a, s->d_nbr_r, s->d_nbr_a, s->d_rev_r, s->d_rev_a, s->d_sr, s->d_va,
                   s->dEdG, s->epart, s->d_Eatom, s->d_qraw, s->d_q, s->d_dEdq, s->d_fself,
-                  s->d_fcv, s->d_ecv, s->d_F, s->d_mol_E, s->d_mol_aux};
+                  s->d_fcv, s->d_ecv, s->d_F, s->d_mol_E, s->d_mol_aux, s->kink_g2, s->kink_h2[0],
+                  s->kink_h2[1], s->kink_mask, s->kink_count};
   for (void* p : ptrs)
     if (p) cudaFreeAsync(p, ctx->stream);
   for (int h = 0; h < 2; ++h) {
@@ -1059,6 +1137,65 @@ extern "C" int tm_selftest_gemm(tm_ctx* ctx, int prec, int M, int N, int K, cons
   if (!ctx || !A || !B || !C) return TM_E_ARG;
   if (prec != TM_PREC_FP32 && prec != TM_PREC_BF16) return tm_fail(ctx, TM_E_ARG, "precision");
   return tm_gemm_selftest(ctx, prec, M, N, K, A, B, C);
+}
+
+extern "C" int tm_selftest_gemm_timeout(tm_ctx* ctx, int prec, int64_t wait_cycles) {
+  if (!ctx || wait_cycles <= 0 || wait_cycles > (1LL << 28)) return TM_E_ARG;
+  if (prec != TM_PREC_FP32 && prec != TM_PREC_BF16) return tm_fail(ctx, TM_E_ARG, "precision");
+  const int M = 256, N = 256, K = 256;
+  std::vector<float> A((size_t)M * K, 0.5f), B((size_t)N * K, 0.25f), C((size_t)M * N, 0.f);
+  // the second operand stage of every CTA is withheld: the MMA issuer's wait on it
+  // runs out, then the producer's and the epilogue's waits do
+  return tm_gemm_selftest(ctx, prec, M, N, K, A.data(), B.data(), C.data(), wait_cycles, 1);
+}
+
+extern "C" int tm_system_layer_outputs(tm_system* s, int layer, float* out) {
+  if (!s || !out) return TM_E_ARG;
+  tm_ctx* ctx = s->ctx;
+  const tm_model* m = s->model;
+  const int L = m->nlayer, H = m->H;
+  if (layer < 0 || layer >= L) return tm_fail(ctx, TM_E_ARG, "layer index");
+  const int width = m->desc.hidden[layer];
+  void* const* buf = layer == L - 1 ? s->G3 : (layer == 0 ? s->H1 : s->H2);
+  const size_t n = (size_t)2 * s->Mpad * H;
+  const bool split = m->desc.precision == TM_PREC_FP32;
+  std::vector<float> hi(n), lo(split ? n : 0);
+  std::vector<uint16_t> b16(split ? 0 : n);
+  int rc;
+  if (split) {
+    if ((rc = tm_cuda_check(ctx, cudaMemcpyAsync(hi.data(), buf[0], n * 4, cudaMemcpyDeviceToHost, ctx->stream), "layer outputs")) ||
+        (rc = tm_cuda_check(ctx, cudaMemcpyAsync(lo.data(), buf[1], n * 4, cudaMemcpyDeviceToHost, ctx->stream), "layer outputs")))
+      return rc;
+  } else if ((rc = tm_cuda_check(ctx, cudaMemcpyAsync(b16.data(), buf[0], n * 2, cudaMemcpyDeviceToHost, ctx->stream), "layer outputs"))) {
+    return rc;
+  }
+  if ((rc = tm_sync_status(ctx, "layer outputs"))) return rc;
+  for (int net = 0; net < 2; ++net)
+    for (int i = 0; i < s->N; ++i) {
+      const size_t src = ((size_t)net * s->Mpad + s->row_of_atom_h[i]) * H;
+      float* dst = out + ((size_t)net * s->N + i) * width;
+      for (int c = 0; c < width; ++c) {
+        if (split) {
+          dst[c] = hi[src + c] + lo[src + c];
+        } else {
+          const uint32_t u = (uint32_t)b16[src + c] << 16;
+          memcpy(&dst[c], &u, 4);
+        }
+      }
+    }
+  return TM_OK;
+}
+
+extern "C" int tm_system_refined_units(tm_system* s, int64_t* n) {
+  if (!s || !n) return TM_E_ARG;
+  *n = 0;
+  if (!s->kink_count) return TM_OK;
+  unsigned long long c = 0;
+  int rc = tm_cuda_check(s->ctx, cudaMemcpyAsync(&c, s->kink_count, sizeof(c), cudaMemcpyDeviceToHost,
+                                                 s->ctx->stream), "refined units");
+  if (!rc) rc = tm_cuda_check(s->ctx, cudaStreamSynchronize(s->ctx->stream), "refined units");
+  *n = (int64_t)c;
+  return rc;
 }
 
 int tm_launch_descriptors_f32(tm_system* s, float* out);

@@ -51,6 +51,45 @@ __device__ __forceinline__ float ds_sub_shift(float ahi, float alo, float bhi, f
   return __fadd_rn(t, __fadd_rn(__fadd_rn(err, err2), __fsub_rn(__fsub_rn(alo, blo), slo)));
 }
 
+// Same, keeping the result as an unevaluated sum hi + lo (about 44 bits).
+__device__ __forceinline__ void ds_sub_shift2(float ahi, float alo, float bhi, float blo, float shi,
+                                              float slo, float& hi, float& lo) {
+  float s = __fsub_rn(ahi, bhi);
+  float bb = __fsub_rn(s, ahi);
+  float err = __fadd_rn(__fsub_rn(ahi, __fsub_rn(s, bb)), __fsub_rn(-bhi, bb));
+  float t = __fsub_rn(s, shi);
+  float tb = __fsub_rn(t, s);
+  float err2 = __fadd_rn(__fsub_rn(s, __fsub_rn(t, tb)), __fsub_rn(-shi, tb));
+  const float c = __fadd_rn(__fadd_rn(err, err2), __fsub_rn(__fsub_rn(alo, blo), slo));
+  hi = __fadd_rn(t, c);
+  lo = __fsub_rn(c, __fsub_rn(hi, t));
+}
+
+// ---------------------------------------------------------------------------
+// Error-free transformations for double-single (hi + lo) arithmetic: Knuth's
+// TwoSum, Dekker's FastTwoSum (|a| >= |b|) and the FMA form of TwoProduct.
+// The _rn intrinsics keep the compiler from contracting them into FMAs.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void tm_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ void tm_fast_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  e = __fsub_rn(b, __fsub_rn(s, a));
+}
+__device__ __forceinline__ void tm_two_prod(float a, float b, float& p, float& e) {
+  p = __fmul_rn(a, b);
+  e = __fmaf_rn(a, b, -p);
+}
+// sqrt of a double-single s = sh + sl >= 0 (one Newton correction)
+__device__ __forceinline__ void tm_ds_sqrt(float sh, float sl, float& rh, float& rl) {
+  if (sh <= 0.f) { rh = 0.f; rl = 0.f; return; }
+  rh = sqrtf(sh);
+  rl = __fmul_rn(__fadd_rn(__fmaf_rn(-rh, rh, sh), sl), __fdiv_rn(0.5f, rh));
+}
+
 // ---------------------------------------------------------------------------
 // The reference's membership test, C_API/MolEmb.cpp:1214-1218:
 //   dij = sqrt(dx*dx + dy*dy + dz*dz) + 1e-13;  accept if dij < rng

@@ -44,6 +44,8 @@ struct DescArgs {
   void* out0;
   void* out1;
   float* out_f32;       // optional plain fp32 rows [Mpad][Dp]
+  float* gnorm2;        // optional squared L2 norm of each row [Mpad] (the relu
+                        // refinement's error bound for the first layer)
   // adjoint
   const float* dEdG;    // [2*Mpad][Dp]
   const float* dEdq;    // [N]
@@ -63,6 +65,74 @@ __device__ __forceinline__ void nbr_vec(const DescArgs& a, float4 hi, float4 lo,
   dy = ds_sub_shift(hi.y, lo.y, hj.y, lj.y, a.sh_hi[r][1], a.sh_lo[r][1]);
   dz = ds_sub_shift(hi.z, lo.z, hj.z, lj.z, a.sh_hi[r][2], a.sh_lo[r][2]);
   el = __float_as_int(hj.w);
+}
+
+// the neighbour vector as double-single components (hi + lo)
+__device__ __forceinline__ void nbr_vec2(const DescArgs& a, float4 hi, float4 lo, uint32_t e,
+                                         float (&dh)[3], float (&dl)[3], int& el) {
+  const int j = (int)tm_atom(e);
+  const int r = tm_img(e);
+  const float4 hj = a.xhi[j], lj = a.xlo[j];
+  ds_sub_shift2(hi.x, lo.x, hj.x, lj.x, a.sh_hi[r][0], a.sh_lo[r][0], dh[0], dl[0]);
+  ds_sub_shift2(hi.y, lo.y, hj.y, lj.y, a.sh_hi[r][1], a.sh_lo[r][1], dh[1], dl[1]);
+  ds_sub_shift2(hi.z, lo.z, hj.z, lj.z, a.sh_hi[r][2], a.sh_lo[r][2], dh[2], dl[2]);
+  el = __float_as_int(hj.w);
+}
+
+// |d| of a double-single vector, as double-single
+__device__ __forceinline__ void ds_norm(const float (&dh)[3], const float (&dl)[3], float& rh,
+                                        float& rl) {
+  float sh, sl, p, e, t;
+  tm_two_prod(dh[0], dh[0], sh, sl);
+  sl = fmaf(2.f * dh[0], dl[0], sl);
+#pragma unroll
+  for (int c = 1; c < 3; ++c) {
+    tm_two_prod(dh[c], dh[c], p, e);
+    tm_two_sum(sh, p, sh, t);
+    sl += t + fmaf(2.f * dh[c], dl[c], e);
+  }
+  tm_fast_two_sum(sh, sl, sh, sl);
+  tm_ds_sqrt(sh, sl, rh, rl);
+}
+
+// fc(r) = 0.5 (cos(pi_tf r / Rc) + 1) = sin^2(c (Rc - r)) for r = rh + rl,
+// with c = c_hi + c_lo = pi_tf / (2 Rc): no cancellation near the cutoff and
+// the argument carried to about 44 bits (sin^2(b + bl) ~ s^2 + 2 s cos(b) bl)
+__device__ __forceinline__ float fcut_ds(float rh, float rl, float rc_hi, float rc_lo, float c_hi,
+                                         float c_lo) {
+  float dh, dl;
+  tm_two_sum(rc_hi, -rh, dh, dl);
+  dl += rc_lo - rl;
+  float bh, bl;
+  tm_two_prod(c_hi, dh, bh, bl);
+  bl += fmaf(c_hi, dl, c_lo * dh);
+  float sb, cb;
+  sincosf(bh, &sb, &cb);
+  return sb * fmaf(2.f * cb, bl, sb);
+}
+
+// (1 + c cos(th) + s sin(th))^8 for double-single c, s and constants, in
+// double-single (squarings by exact products)
+__device__ __forceinline__ float pow8_ds(float ch, float cl, float sh, float sl, float cth,
+                                        float cth_lo, float sth, float sth_lo) {
+  float p1, e1, p2, e2, th, tl;
+  tm_two_prod(ch, cth, p1, e1);
+  tm_two_prod(sh, sth, p2, e2);
+  tm_two_sum(p1, p2, th, tl);
+  tl += (e1 + e2) + (fmaf(ch, cth_lo, cl * cth) + fmaf(sh, sth_lo, sl * sth));
+  float xh, xl;
+  tm_two_sum(1.f, th, xh, xl);
+  xl += tl;
+  tm_fast_two_sum(xh, xl, xh, xl);
+  if (xh <= 0.f) return 0.f;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    float ph, pl;
+    tm_two_prod(xh, xh, ph, pl);
+    pl = fmaf(2.f * xh, xl, pl);
+    tm_fast_two_sum(ph, pl, xh, xl);
+  }
+  return xh + xl;
 }
 
 __device__ __forceinline__ float fcut(float r, float pi_tf, float rc) {
@@ -146,6 +216,42 @@ __device__ __forceinline__ void load_angular(const DescArgs& a, const tm_consts&
   __syncwarp();
 }
 
+// load_angular with double-single geometry (forward of the relu refinement):
+// unit vectors hi in ux/uy/uz and lo in vx/vy/vz, |d| hi in r and lo in fcd,
+// fc from the double-single distance
+__device__ __forceinline__ void load_angular_ds(const DescArgs& a, const tm_consts& k, int i,
+                                                float4 hi, float4 lo, int ca, WarpSmem& w,
+                                                int* seg, int lane) {
+  for (int e = 0; e <= k.nele; ++e) seg[e] = 0;
+  for (int base = 0; base < ca; base += 32) {
+    const int s = base + lane;
+    int el = -1;
+    if (s < ca) {
+      float dh[3], dl[3], rh, rl;
+      nbr_vec2(a, hi, lo, a.nbr_a[(size_t)i * a.KA + s], dh, dl, el);
+      ds_norm(dh, dl, rh, rl);
+      const float inv = __fdiv_rn(1.f, rh);
+      float uh[3], ul[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        uh[c] = __fmul_rn(dh[c], inv);
+        // (d - u r) / r with u = uh, r = rh + rl
+        ul[c] = (fmaf(-uh[c], rh, dh[c]) + fmaf(-uh[c], rl, dl[c])) * inv;
+      }
+      w.ux[s] = uh[0]; w.uy[s] = uh[1]; w.uz[s] = uh[2];
+      w.vx[s] = ul[0]; w.vy[s] = ul[1]; w.vz[s] = ul[2];
+      w.r[s] = rh;
+      w.fcd[s] = rl;
+      w.fc[s] = fcut_ds(rh, rl, k.a_rc_hi, k.a_rc_lo, k.ca_hi, k.ca_lo);
+    }
+    for (int e = 0; e < k.nele; ++e) seg[e] += __popc(__ballot_sync(TM_FULL, el == e));
+  }
+  int acc = 0;
+  for (int e = 0; e < k.nele; ++e) { int c = seg[e]; seg[e] = acc; acc += c; }
+  seg[k.nele] = acc;
+  __syncwarp();
+}
+
 // advance the (pa, pb) pair index by 4 in the enumeration order used for the
 // element pair (b outer, a inner; a < b when both atoms share an element)
 __device__ __forceinline__ void pair_advance(int& pa, int& pb, int na_, bool tri) {
@@ -168,6 +274,12 @@ __device__ __forceinline__ void pair_start(int t, int& pa, int& pb, int na_, boo
   }
 }
 
+// ACC: the relu refinement's form, every difference vector, distance, cutoff
+// function, angle term and Gaussian argument carried in double-single, so
+// that each term is within a few FP32 roundings of its FP64 value (the plain
+// form's FP32 distances put ~1e-7 relative error on the cutoff functions and
+// the angle powers). Rows are still FP32 sums.
+template <bool ACC>
 __global__ void __launch_bounds__(128) k_desc_fwd(const DescArgs a, const tm_consts k) {
   extern __shared__ float sh[];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -180,17 +292,25 @@ __global__ void __launch_bounds__(128) k_desc_fwd(const DescArgs a, const tm_con
   // ---- radial ----
   const int cr = a.cnt_r[i];
   const float rs_lane = k.rs_r[lane < k.nr ? lane : 0];
+  const float rs_lane_lo = k.rs_r_lo[lane < k.nr ? lane : 0];
   float racc = 0.f;
   int rel = -1;
   for (int base = 0; base < cr; base += 32) {
     const int s = base + lane;
-    float r = 0.f, f = 0.f;
+    float r = 0.f, rl = 0.f, f = 0.f;
     int el = 0;
     if (s < cr) {
-      float dx, dy, dz;
-      nbr_vec(a, hi, lo, a.nbr_r[(size_t)i * a.KR + s], dx, dy, dz, el);
-      r = sqrtf(dx * dx + dy * dy + dz * dz);
-      f = fcut(r, k.pi_tf, k.r_rc);
+      if constexpr (ACC) {
+        float dh[3], dl[3];
+        nbr_vec2(a, hi, lo, a.nbr_r[(size_t)i * a.KR + s], dh, dl, el);
+        ds_norm(dh, dl, r, rl);
+        f = fcut_ds(r, rl, k.r_rc_hi, k.r_rc_lo, k.cr_hi, k.cr_lo);
+      } else {
+        float dx, dy, dz;
+        nbr_vec(a, hi, lo, a.nbr_r[(size_t)i * a.KR + s], dx, dy, dz, el);
+        r = sqrtf(dx * dx + dy * dy + dz * dz);
+        f = fcut(r, k.pi_tf, k.r_rc);
+      }
     }
     // rows are sorted by element: accumulate in a register, flush to the
     // row when the element changes (at most nele flushes per centre)
@@ -204,7 +324,13 @@ __global__ void __launch_bounds__(128) k_desc_fwd(const DescArgs a, const tm_con
         racc = 0.f;
         rel = lq;
       }
-      const float t = rq - rs_lane;
+      float t;
+      if constexpr (ACC) {
+        const float rlq = __shfl_sync(TM_FULL, rl, q);
+        t = __fadd_rn(__fsub_rn(rq, rs_lane), __fsub_rn(rlq, rs_lane_lo));
+      } else {
+        t = rq - rs_lane;
+      }
       racc += expf(-k.eta * t * t) * fq;
     }
   }
@@ -212,9 +338,11 @@ __global__ void __launch_bounds__(128) k_desc_fwd(const DescArgs a, const tm_con
   // ---- angular ----
   const int ca = a.cnt_a[i];
   int seg[TM_MAX_ELE + 1];
-  load_angular(a, k, i, hi, lo, ca, w, seg, lane);
+  if constexpr (ACC) load_angular_ds(a, k, i, hi, lo, ca, w, seg, lane);
+  else load_angular(a, k, i, hi, lo, ca, w, seg, lane);
   const int grp = lane >> 3, q = lane & 7;
   const float cth = k.cos_th[q], sth = k.sin_th[q], rsq = k.rs_a[q];
+  const float cth_lo = k.cos_th_lo[q], sth_lo = k.sin_th_lo[q], rsq_lo = k.rs_a_lo[q];
   for (int ea = 0; ea < k.nele; ++ea) {
     for (int eb = ea; eb < k.nele; ++eb) {
       const int na_ = seg[ea + 1] - seg[ea], nb_ = seg[eb + 1] - seg[eb];
@@ -234,7 +362,44 @@ __global__ void __launch_bounds__(128) k_desc_fwd(const DescArgs a, const tm_con
         for (int h = 0; h < 2; ++h) {
           AF[h] = 0.f;
           B[h] = 0.f;
-          if (tb + 4 * h + grp < npair) {
+          if (ACC && tb + 4 * h + grp < npair) {
+            const int sa = seg[ea] + pa, sb = seg[eb] + pb;
+            // c = u_a . u_b and s = sqrt((1 - c)(1 + c)) in double-single (c is
+            // accurate to ~2^-44, so s is accurate even for nearly collinear triples)
+            float ch, cl, p, e, t;
+            tm_two_prod(w.ux[sa], w.ux[sb], ch, cl);
+            cl += fmaf(w.ux[sa], w.vx[sb], w.vx[sa] * w.ux[sb]);
+            tm_two_prod(w.uy[sa], w.uy[sb], p, e);
+            tm_two_sum(ch, p, ch, t);
+            cl += t + e + fmaf(w.uy[sa], w.vy[sb], w.vy[sa] * w.uy[sb]);
+            tm_two_prod(w.uz[sa], w.uz[sb], p, e);
+            tm_two_sum(ch, p, ch, t);
+            cl += t + e + fmaf(w.uz[sa], w.vz[sb], w.vz[sa] * w.uz[sb]);
+            tm_fast_two_sum(ch, cl, ch, cl);
+            float mh, ml, ph, pl, qh, ql, sh, sl;
+            tm_two_sum(1.f, -ch, mh, ml);
+            ml -= cl;
+            tm_two_sum(1.f, ch, ph, pl);
+            pl += cl;
+            tm_two_prod(mh, ph, qh, ql);
+            ql += fmaf(mh, pl, ml * ph);
+            tm_fast_two_sum(qh, ql, qh, ql);
+            tm_ds_sqrt(qh, ql, sh, sl);
+            float pw;
+            if (k.zeta_pow2) {
+              pw = pow8_ds(ch, cl, sh, sl, cth, cth_lo, sth, sth_lo);
+            } else {
+              float dp;
+              powz(fmaxf(0.f, 1.f + (ch * cth + sh * sth)), k, pw, dp);
+            }
+            AF[h] = k.two_1mz * pw * w.fc[sa] * w.fc[sb];
+            // (r_a + r_b) / 2 - Rs in double-single
+            float rh, rl2;
+            tm_two_sum(w.r[sa], w.r[sb], rh, rl2);
+            rl2 += w.fcd[sa] + w.fcd[sb];
+            const float u = __fadd_rn(__fsub_rn(0.5f * rh, rsq), __fsub_rn(0.5f * rl2, rsq_lo));
+            B[h] = expf(-k.eta * u * u);
+          } else if (!ACC && tb + 4 * h + grp < npair) {
             const int sa = seg[ea] + pa, sb = seg[eb] + pb;
             const float c = w.ux[sa] * w.ux[sb] + w.uy[sa] * w.uy[sb] + w.uz[sa] * w.uz[sb];
             // sin(theta) = |u_a x u_b|: well conditioned for nearly collinear triples,
@@ -299,6 +464,15 @@ __global__ void __launch_bounds__(128) k_desc_fwd(const DescArgs a, const tm_con
   if (a.out_f32) {
     float4* o = reinterpret_cast<float4*>(a.out_f32 + (size_t)row * k.Dp);
     for (int c = lane; c < k.Dp / 4; c += 32) o[c] = reinterpret_cast<const float4*>(w.row)[c];
+  }
+  if (a.gnorm2) {
+    float ss = 0.f;
+    for (int c = lane; c < k.Dp / 4; c += 32) {
+      const float4 v = reinterpret_cast<const float4*>(w.row)[c];
+      ss += v.x * v.x + v.y * v.y + v.z * v.z + v.w * v.w;
+    }
+    ss = warp_sum(ss);
+    if (lane == 0) a.gnorm2[row] = ss;
   }
 }
 
@@ -503,35 +677,33 @@ static DescArgs make_desc_args(tm_system* s) {
   a.cnt_r = s->d_cnt_r; a.cnt_a = s->d_cnt_a; a.rev_r = s->d_rev_r; a.rev_a = s->d_rev_a;
   a.row_of_atom = s->row_of_atom; a.N = s->N; a.KR = s->KR; a.KA = s->KA; a.Mpad = s->Mpad;
   a.prec = s->model->desc.precision;
-  a.out0 = s->G[0]; a.out1 = s->G[1]; a.out_f32 = nullptr;
+  a.out0 = s->G[0]; a.out1 = s->G[1]; a.out_f32 = nullptr; a.gnorm2 = s->kink_g2;
   a.dEdG = s->dEdG; a.dEdq = s->d_dEdq; a.fself = s->d_fself; a.sr = s->d_sr; a.va = s->d_va;
   tm_fill_shifts(s, a.sh_hi, a.sh_lo);
   return a;
 }
 
-int tm_launch_descriptors(tm_system* s) {
+static int launch_desc_fwd(tm_system* s, const DescArgs& a) {
   tm_ctx* ctx = s->ctx;
-  DescArgs a = make_desc_args(s);
   const tm_consts& k = s->model->k;
   const size_t shm = (size_t)4 * smem_floats(k.Dp, s->KA) * sizeof(float);
+  // the double-single form for the relu refinement (tm_gemm.cu)
+  const bool acc = s->model->kink;
   if (shm > 48 * 1024)
-    cudaFuncSetAttribute(k_desc_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-  k_desc_fwd<<<tm_div_up(s->N, 4), 128, shm, ctx->stream>>>(a, k);
+    cudaFuncSetAttribute(acc ? k_desc_fwd<true> : k_desc_fwd<false>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  if (acc) k_desc_fwd<true><<<tm_div_up(s->N, 4), 128, shm, ctx->stream>>>(a, k);
+  else k_desc_fwd<false><<<tm_div_up(s->N, 4), 128, shm, ctx->stream>>>(a, k);
   ctx->launches++;
   return tm_cuda_check(ctx, cudaGetLastError(), "descriptors");
 }
 
+int tm_launch_descriptors(tm_system* s) { return launch_desc_fwd(s, make_desc_args(s)); }
+
 int tm_launch_descriptors_f32(tm_system* s, float* out) {
-  tm_ctx* ctx = s->ctx;
   DescArgs a = make_desc_args(s);
   a.out_f32 = out;
-  const tm_consts& k = s->model->k;
-  const size_t shm = (size_t)4 * smem_floats(k.Dp, s->KA) * sizeof(float);
-  if (shm > 48 * 1024)
-    cudaFuncSetAttribute(k_desc_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-  k_desc_fwd<<<tm_div_up(s->N, 4), 128, shm, ctx->stream>>>(a, k);
-  ctx->launches++;
-  return tm_cuda_check(ctx, cudaGetLastError(), "descriptors");
+  return launch_desc_fwd(s, a);
 }
 
 namespace {

@@ -63,6 +63,20 @@ struct GemmArgs {
   const void* hprev1;
   tm_dev_status* st;
   int mtiles, ntiles;   // tiles per net along M and N
+  // relu refinement (FP32 forward layers with relu): a unit is flagged when
+  // |z| < kappa ||a_row|| ||w_unit||, a bound of the tensor-core error
+  const float* an2;     // squared norms of the input rows: an2_parts partial sums per row
+  int an2_parts;
+  int an2_net_stride;   // floats between the two nets' rows (0: shared input)
+  float* hn2_out;       // [2][Mpad][ntiles] partial squared norms of the outputs (or null)
+  const float* wnorm;   // [2][nele][N]
+  uint32_t* kmask;      // [2][Mpad][N/32]
+  float kappa;
+  // diagnostics of the bounded waits (tm_selftest_gemm_timeout): the wait
+  // limit in SM cycles (0: 2^28) and a producer iteration whose operand
+  // loads are withheld (-1: none), so that the MMA issuer's wait runs out
+  long long wait_limit;
+  int skip_it;
 };
 
 // ---- PTX wrappers ---------------------------------------------------------
@@ -88,11 +102,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* b, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait: false after about 2^32 SM cycles.
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
+// Bounded wait: false after `limit` SM cycles (2^28, about 0.13 s, unless a
+// diagnostic launch asks for less).
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, long long limit) {
   const long long t0 = clock64();
   while (!mbar_try_wait(b, parity)) {
-    if (clock64() - t0 > (1LL << 28)) return false;   // about 0.13 s
+    if (clock64() - t0 > limit) return false;
   }
   return true;
 }
@@ -248,6 +263,7 @@ template <int PREC, int EPI, int ACT>
 __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArgs g) {
   using C = Cfg<PREC>;
   constexpr int BN = C::BN;
+  constexpr bool KINK = PREC == TM_PREC_FP32 && ACT == TM_ACT_RELU && (EPI == EPI_FWD || EPI == EPI_FWD_LAST);
   // an earlier kernel of this context already failed: do nothing (every thread
   // reads the same word, written before this launch)
   if (*(volatile int*)&g.st->code != 0) return;
@@ -264,6 +280,7 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nk = g.K / C::BK;
+  const long long wlim = g.wait_limit > 0 ? g.wait_limit : (1LL << 28);
   const int per_net = g.mtiles * g.ntiles;
   const int total = 2 * per_net;
 
@@ -303,11 +320,12 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
         const int b_row = (net * g.nele + elem) * g.N + n_tile * BN;
         for (int kb = 0; kb < nk; ++kb, ++it) {
           const int s = it % C::NSTAGE;
-          if (it >= C::NSTAGE && !mbar_wait(&empty[s], ((it / C::NSTAGE) - 1) & 1)) {
+          if (it >= C::NSTAGE && !mbar_wait(&empty[s], ((it / C::NSTAGE) - 1) & 1, wlim)) {
             tm_flag(g.st, TM_E_TIMEOUT, t, 100);
             *abort_flag = 1;
             break;
           }
+          if (it == g.skip_it) continue;   // diagnostic: this stage never arrives
           uint8_t* st = smem + s * C::STAGE;
           mbar_expect_tx(&full[s], C::STAGE);
           const int x = kb * C::BK;
@@ -325,7 +343,7 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
       int it = 0, lt = 0;
       for (int t = blockIdx.x; t < total && !*abort_flag; t += gridDim.x, ++lt) {
         const int buf = lt & 1;
-        if (lt >= 2 && !mbar_wait(&acce[buf], ((lt >> 1) - 1) & 1)) {
+        if (lt >= 2 && !mbar_wait(&acce[buf], ((lt >> 1) - 1) & 1, wlim)) {
           tm_flag(g.st, TM_E_TIMEOUT, t, 103);
           *abort_flag = 1;
           break;
@@ -335,7 +353,7 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
         bool ok = true;
         for (int kb = 0; kb < nk; ++kb, ++it) {
           const int s = it % C::NSTAGE;
-          if (!mbar_wait(&full[s], (it / C::NSTAGE) & 1)) {
+          if (!mbar_wait(&full[s], (it / C::NSTAGE) & 1, wlim)) {
             tm_flag(g.st, TM_E_TIMEOUT, t, 101);
             *abort_flag = 1;
             ok = false;
@@ -380,7 +398,7 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
     int lt = 0;
     for (int t = blockIdx.x; t < total && eok; t += gridDim.x, ++lt) {
       const int buf = lt & 1;
-      if (!mbar_wait(&accf[buf], (lt >> 1) & 1)) {
+      if (!mbar_wait(&accf[buf], (lt >> 1) & 1, wlim)) {
         tm_flag(g.st, TM_E_TIMEOUT, t, 102);
         *abort_flag = 1;
         break;
@@ -395,6 +413,16 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
       const int pblk = (net * g.nele + elem) * g.N;
       const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(buf * C::ACC_COLS);
       float esum = 0.f;
+      // relu refinement: kappa * ||input row|| (flags |z| below it times ||w_unit||)
+      float kthr = 0.f, hss = 0.f;
+      if constexpr (KINK) {
+        if (g.kmask) {
+          const float* pa = g.an2 + (size_t)net * g.an2_net_stride + (size_t)row * g.an2_parts;
+          float ss = 0.f;
+          for (int q = 0; q < g.an2_parts; ++q) ss += pa[q];
+          kthr = g.kappa * sqrtf(ss);
+        }
+      }
       for (int c = 0; c < BN && eok; c += 32) {
         const int col = n_tile * BN + c;
         // BF16 (not dE/dG): one 64-column box covers two 32-column chunks
@@ -447,20 +475,28 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
         }
         float v[32];
         if (EPI == EPI_FWD || EPI == EPI_FWD_LAST) {
+          uint32_t km = 0;
 #pragma unroll
           for (int q = 0; q < 32; ++q) {
             const float z = __uint_as_float(r[q]) + bq[q];
+            if constexpr (KINK) {
+              if (fabsf(z) < kthr * __ldg(g.wnorm + pblk + col + q)) km |= 1u << q;
+            }
             if (EPI == EPI_FWD) {
               v[q] = act_f<ACT>(z, g.alpha);
+              if constexpr (KINK) hss = fmaf(v[q], v[q], hss);
             } else {
               esum += act_f<ACT>(z, g.alpha) * wq[q];
               v[q] = wq[q] * actd_z<ACT>(z, g.alpha);
             }
           }
+          if constexpr (KINK) {
+            if (g.kmask) g.kmask[((size_t)net * g.Mpad + row) * (g.N >> 5) + (col >> 5)] = km;
+          }
         } else if (EPI == EPI_BWD) {
           float h[32];
           if (box_start) {
-            if (!mbar_wait(&ebar[warp], eph & 1)) {
+            if (!mbar_wait(&ebar[warp], eph & 1, wlim)) {
               tm_flag(g.st, TM_E_TIMEOUT, t, 104);
               *abort_flag = 1;
               eok = false;
@@ -559,6 +595,9 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
         }
       }
       if (EPI == EPI_FWD_LAST) g.epart[orow * (g.N / BN) + n_tile] = esum;
+      if constexpr (KINK && EPI == EPI_FWD) {
+        if (g.hn2_out) g.hn2_out[orow * g.ntiles + n_tile] = hss;
+      }
       // this warp has read its 32 lanes of the accumulator: hand it back
       tc_fence_before();
       __syncwarp();
@@ -625,7 +664,144 @@ int dispatch(tm_ctx* ctx, int prec, int epi, const GemmArgs& g, int mtiles) {
                               : run_gemm_act<TM_PREC_BF16>(ctx, epi, g, mtiles);
 }
 
+// ---- relu refinement --------------------------------------------------------
+// The tensor core's FP32 accumulation truncates at every instruction, which
+// puts the pre-activation z of a unit up to about (K/8) 2^-23 sum|a||w| away
+// from its exact value. A relu unit whose z lies that close to zero can take
+// the other side of the kink, and its derivative (0 or 1) then differs from
+// the exact network's: the force jumps. The forward epilogue flags every unit
+// with |z| < kappa ||a|| ||w|| (Cauchy-Schwarz: ||a|| ||w|| >= sum|a||w|), and
+// this kernel recomputes the flagged ones from the layer's stored input
+// (hi + lo, an exact sum) and the weights and bias as given (FP64, held as
+// double-single pairs), with a double-single dot product (TwoProduct and
+// TwoSum per term, Ogita, Rump and Oishi 2005), then rewrites the unit's
+// output: h = relu(z) for a hidden layer, w_out * step(z) (the backward pass's
+// seed) for the last one. The energy of the last layer keeps the tensor-core z
+// of a flagged unit (a change below kappa ||a|| ||w|| |w_out|).
+struct KinkArgs {
+  const float* a_hi;
+  const float* a_lo;
+  int a_net_rows;         // 0: both nets read the same input rows (the descriptors)
+  int K;
+  const float2* w2;       // [2][nele][N][K] (hi, lo)
+  const float2* b2;       // [2][nele][N]
+  const float* wout;      // [2][nele][N]
+  const int32_t* tile_elem;
+  const uint32_t* kmask;  // [2][Mpad][N/32]
+  float* o_hi;
+  float* o_lo;            // [2*Mpad][N]
+  int N, Mpad, nele;
+  unsigned long long* count;
+};
+
+// One warp per (net, row). A row with flagged units reads its input once
+// into registers (KPL values per lane, all loads in flight together); each
+// flagged unit then streams its weight vector with independent loads.
+template <bool LAST, int KPL>
+__global__ void __launch_bounds__(256) k_kink_refine(const KinkArgs a) {
+  const int wg = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (wg >= 2 * a.Mpad) return;
+  const int net = wg / a.Mpad, r = wg - net * a.Mpad;
+  const int nw = a.N >> 5;
+  const uint32_t* mk = a.kmask + (size_t)wg * nw;
+  const uint32_t first = lane < nw ? mk[lane] : 0u;
+  if (nw <= 32 && !__any_sync(TM_FULL, first != 0u)) return;
+  const int elem = a.tile_elem[r / BM];
+  const size_t blk = (size_t)net * a.nele + elem;
+  const size_t arow = (size_t)net * a.a_net_rows + r;
+  const float* ah = a.a_hi + arow * a.K + lane;
+  const float* al = a.a_lo + arow * a.K + lane;
+  constexpr int KR = KPL > 0 ? KPL : 1;
+  float xh[KR], xl[KR];
+#pragma unroll
+  for (int q = 0; q < KPL; ++q) {
+    xh[q] = ah[q * 32];
+    xl[q] = al[q * 32];
+  }
+  int nref = 0;
+  for (int w0 = 0; w0 < nw; w0 += 32) {
+    const uint32_t mine = w0 == 0 ? first : (w0 + lane < nw ? mk[w0 + lane] : 0u);
+    uint32_t any = __ballot_sync(TM_FULL, mine != 0u);
+    while (any) {
+      const int src = __ffs(any) - 1;
+      any &= any - 1;
+      uint32_t bits = __shfl_sync(TM_FULL, mine, src);
+      while (bits) {
+        const int b = __ffs(bits) - 1;
+        bits &= bits - 1;
+        const int col = (w0 + src) * 32 + b;
+        const float2* wr = a.w2 + (blk * a.N + col) * a.K + lane;
+        float sh = 0.f, sl = 0.f;
+        if constexpr (KPL > 0) {
+          float2 wv[KPL];
+#pragma unroll
+          for (int q = 0; q < KPL; ++q) wv[q] = __ldg(wr + q * 32);
+#pragma unroll
+          for (int q = 0; q < KPL; ++q) {
+            float p, e, t;
+            tm_two_prod(xh[q], wv[q].x, p, e);
+            tm_two_sum(sh, p, sh, t);
+            sl += (t + e) + fmaf(xh[q], wv[q].y, xl[q] * wv[q].x);
+          }
+        } else {   // any K that is a multiple of 32: the input streamed as well
+#pragma unroll 8
+          for (int q = 0; q < a.K / 32; ++q) {
+            const float2 wq = __ldg(wr + q * 32);
+            const float x = ah[q * 32], xq = al[q * 32];
+            float p, e, t;
+            tm_two_prod(x, wq.x, p, e);
+            tm_two_sum(sh, p, sh, t);
+            sl += (t + e) + fmaf(x, wq.y, xq * wq.x);
+          }
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+          const float oh = __shfl_xor_sync(TM_FULL, sh, o), ol = __shfl_xor_sync(TM_FULL, sl, o);
+          float t;
+          tm_two_sum(sh, oh, sh, t);
+          sl += t + ol;
+        }
+        if (lane == 0) {
+          const float2 bb = a.b2[blk * a.N + col];
+          float t;
+          tm_two_sum(sh, bb.x, sh, t);
+          sl += t + bb.y;
+          const float z = sh + sl;
+          const float v = LAST ? (z > 0.f ? a.wout[blk * a.N + col] : 0.f) : (z > 0.f ? z : 0.f);
+          float hi, lo;
+          tm_tf32_split(v, hi, lo);
+          const size_t o = ((size_t)net * a.Mpad + r) * a.N + col;
+          a.o_hi[o] = hi;
+          a.o_lo[o] = lo;
+        }
+        ++nref;
+      }
+    }
+  }
+  if (lane == 0 && nref && a.count) atomicAdd(a.count, (unsigned long long)nref);
+}
+
+template <bool LAST>
+int launch_kink_refine(tm_ctx* ctx, const KinkArgs& ka) {
+  const int blocks = tm_div_up(2 * ka.Mpad * 32, 256);
+  switch (ka.K / 32) {
+    case 8: k_kink_refine<LAST, 8><<<blocks, 256, 0, ctx->stream>>>(ka); break;
+    case 16: k_kink_refine<LAST, 16><<<blocks, 256, 0, ctx->stream>>>(ka); break;
+    case 24: k_kink_refine<LAST, 24><<<blocks, 256, 0, ctx->stream>>>(ka); break;
+    case 32: k_kink_refine<LAST, 32><<<blocks, 256, 0, ctx->stream>>>(ka); break;
+    default: k_kink_refine<LAST, 0><<<blocks, 256, 0, ctx->stream>>>(ka); break;
+  }
+  ctx->launches++;
+  return tm_cuda_check(ctx, cudaGetLastError(), "relu refinement");
+}
+
 }  // namespace
+
+// kappa of the flag test for a reduction of length K: (K/8) 2^-23 for the
+// truncations of the main accumulator (one per 8-deep tf32 instruction) plus
+// 8 2^-23 for the split operands' residuals and the correction accumulator
+float tm_kink_kappa(int K) { return (float)((K / 8 + 8) * 0x1p-23); }
 
 int tm_gemm_bn(int prec) {
   return prec == TM_PREC_FP32 ? Cfg<TM_PREC_FP32>::BN : Cfg<TM_PREC_BF16>::BN;
@@ -682,6 +858,11 @@ static int mlp_layers(tm_system* s, bool forward, bool backward) {
   g.act = m->k.act;
   g.alpha = m->k.alpha_sig;
   g.st = ctx->d_status;
+  g.skip_it = -1;
+  const bool kink = m->kink && s->kink_mask;
+  const int nparts = H / tm_gemm_bn(prec);
+  if (forward && kink && s->kink_count)
+    cudaMemsetAsync(s->kink_count, 0, sizeof(unsigned long long), ctx->stream);
   for (int l = 0; forward && l < L; ++l) {
     const bool last = (l == L - 1);
     const CUtensorMap* const* A = l == 0 ? lv0 : lvH[l - 1];
@@ -700,8 +881,38 @@ static int mlp_layers(tm_system* s, bool forward, bool backward) {
     g.out1 = last ? s->G3[1] : bufH[l][1];
     g.o0 = last ? s->ts_G3[0] : *stH[l][0];
     g.o1 = last ? s->ts_G3[1] : *stH[l][1];
+    if (kink) {
+      g.kmask = s->kink_mask;
+      g.wnorm = m->kwn[l];
+      g.kappa = tm_kink_kappa(g.K);
+      g.an2 = l == 0 ? s->kink_g2 : s->kink_h2[(l - 1) & 1];
+      g.an2_parts = l == 0 ? 1 : nparts;
+      g.an2_net_stride = l == 0 ? 0 : s->Mpad * nparts;
+      g.hn2_out = last ? nullptr : s->kink_h2[l & 1];
+    }
     if ((rc = dispatch(ctx, prec, last ? EPI_FWD_LAST : EPI_FWD, g, mt))) return rc;
+    if (kink) {
+      KinkArgs ka;
+      ka.a_hi = static_cast<const float*>(l == 0 ? s->G[0] : bufH[l - 1][0]);
+      ka.a_lo = static_cast<const float*>(l == 0 ? s->G[1] : bufH[l - 1][1]);
+      ka.a_net_rows = l == 0 ? 0 : s->Mpad;
+      ka.K = g.K;
+      ka.w2 = m->kw2[l];
+      ka.b2 = m->kb2[l];
+      ka.wout = m->wout;
+      ka.tile_elem = s->tile_elem;
+      ka.kmask = s->kink_mask;
+      ka.o_hi = static_cast<float*>(last ? s->G3[0] : bufH[l][0]);
+      ka.o_lo = static_cast<float*>(last ? s->G3[1] : bufH[l][1]);
+      ka.N = H;
+      ka.Mpad = s->Mpad;
+      ka.nele = m->k.nele;
+      ka.count = s->kink_count;
+      if ((rc = last ? launch_kink_refine<true>(ctx, ka) : launch_kink_refine<false>(ctx, ka))) return rc;
+    }
   }
+  g.kmask = nullptr;
+  g.hn2_out = nullptr;
   if (!backward) return TM_OK;
   for (int l = L - 1; l >= 0; --l) {
     // A = g_{l+1} (level l+1 buffer), B = W_l as [Kin x Nout] rows
@@ -739,7 +950,7 @@ static int mlp_layers(tm_system* s, bool forward, bool backward) {
 // Stand-alone check of the tensor-core path: C[M,N] = A[M,K] B[N,K]^T with a
 // single element and net 0 (host fp32 in/out). Used by the GPU tests.
 int tm_gemm_selftest(tm_ctx* ctx, int prec, int M, int N, int K, const float* A, const float* B,
-                     float* Cout) {
+                     float* Cout, long long wait_limit, int skip_it) {
   const int BN = tm_gemm_bn(prec);
   if (M % BM || N % BN || K % 64) return tm_fail(ctx, TM_E_ARG, "selftest shape");
   const int eb = prec == TM_PREC_FP32 ? 4 : 2;
@@ -789,6 +1000,8 @@ int tm_gemm_selftest(tm_ctx* ctx, int prec, int M, int N, int K, const float* A,
     return rc;
   g.K = K; g.N = N; g.a_net_rows = M; g.nele = 1; g.tile_elem = dte; g.Mpad = M;
   g.out0 = dc; g.out1 = dc1; g.ldo = N; g.st = st;
+  g.wait_limit = wait_limit;
+  g.skip_it = skip_it;
   rc = dispatch(ctx, prec, EPI_OUT, g, M / BM);
   if (!rc) rc = tm_cuda_check(ctx, cudaMemcpyAsync(Cout, dc, nC * 4, cudaMemcpyDeviceToHost, sm), "selftest d2h");
   if (!rc) rc = tm_sync_status(ctx, "gemm selftest");

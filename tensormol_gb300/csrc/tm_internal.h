@@ -27,6 +27,11 @@ struct tm_consts {
   float pi_tf;                              // 3.14159265359 as in RawSymFunc.py
   float rs_r[32], rs_a[8], cos_th[8], sin_th[8];
   float two_1mz;                            // 2^(1 - zeta)
+  // low parts of the constants above (value - fp32(value)) and the cutoff
+  // functions' fc(r) = sin^2(c (Rc - r)), c = pi / (2 Rc), as hi + lo pairs:
+  // the double-single descriptor arithmetic of the relu refinement
+  float rs_r_lo[32], rs_a_lo[8], cos_th_lo[8], sin_th_lo[8];
+  float r_rc_hi, r_rc_lo, a_rc_hi, a_rc_lo, cr_hi, cr_lo, ca_hi, ca_lo;
   int elepair[TM_MAX_ELE][TM_MAX_ELE];      // unordered element pair -> index
   // Coulomb / vdW (atomic units, see params.coulomb_constants)
   float bohr, alpha, r_lr, r_sr, elu_shift, elu_a, zz, yy;
@@ -95,6 +100,13 @@ struct tm_model {
   CUtensorMap tm_wf[TM_MAX_HIDDEN][2];
   CUtensorMap tm_wb[TM_MAX_HIDDEN][2];
   size_t elem_size = 4;                // 4 (tf32 split) or 2 (bf16)
+  // relu refinement (FP32 precision with relu only): hidden pre-activations
+  // within the tensor-core error bound of zero are recomputed in FP64
+  bool kink = false;
+  float2* kw2[TM_MAX_HIDDEN] = {};     // [2][nele][H][Kin_l] W^T as given (FP64) held as
+                                       //   double-single pairs (hi, lo)
+  float2* kb2[TM_MAX_HIDDEN] = {};     // [2][nele][H] biases, likewise
+  float* kwn[TM_MAX_HIDDEN] = {};      // [2][nele][H] L2 norm of each W^T row (one output unit)
 };
 
 struct tm_system {
@@ -184,6 +196,14 @@ struct tm_system {
   void* G3[2] = {};
   float* dEdG = nullptr;               // [2*Mpad][Dp]
   float* epart = nullptr;              // [2][Mpad][H/tm_gemm_bn(precision)]
+  // relu refinement (tm_model::kink): squared row norms of each layer's input
+  // (the bound of the tensor-core error), flags of the units to recompute and
+  // the number recomputed by the last evaluation
+  float* kink_g2 = nullptr;            // [Mpad] descriptor rows
+  float* kink_h2[2] = {};              // [2][Mpad][H/BN] per-N-tile partial sums, two
+                                       //   buffers alternating between layers
+  uint32_t* kink_mask = nullptr;       // [2][Mpad][H/32]
+  unsigned long long* kink_count = nullptr;
   CUtensorMap tm_G[2], tm_H1[2], tm_H2[2], tm_G3[2];
   // 32-row boxes of the layer outputs for the GEMM epilogue's TMA stores (and
   // the backward pass's loads of the previous activation)
@@ -242,8 +262,9 @@ int tm_make_tmap(tm_ctx* ctx, CUtensorMap* map, void* base, int elem_bytes, uint
 int tm_launch_mlp(tm_system* s, bool backward);
 int tm_launch_mlp_backward_only(tm_system* s);
 int tm_gemm_bn(int prec);   // GEMM N tile of a precision mode (128 or 256)
+float tm_kink_kappa(int K); // relu refinement: flag bound per unit of ||a|| ||w||
 int tm_gemm_selftest(tm_ctx* ctx, int prec, int M, int N, int K, const float* A,
-                     const float* B, float* C);
+                     const float* B, float* C, long long wait_limit = 0, int skip_it = -1);
 // tm_coulomb.cu
 int tm_launch_mlp_finish(tm_system* s);
 int tm_launch_coulomb(tm_system* s, unsigned flags);

@@ -497,11 +497,14 @@ extern "C" int tm_md_run(tm_md* md, int nsteps, double skin, double* log) {
     }
     if (skin > 0.0) {
       // the next chunk: as long as the last one's displacement, scaled, allows
+      // (a one-step chunk measures no displacement), and at most twice as long
       const double per_step = disp / (n > 1 ? n - 1 : 1);
       int next = per_step > 0 ? (int)floor(0.5 * skin / (1.3 * per_step)) + 1 : kChunk;
+      if (next > 2 * n) next = 2 * n;
       chunk = next < 1 ? 1 : (next > kChunk ? kChunk : next);
     }
     start += n;
+    retries = 0;   // the replay limit is per chunk
   }
   if (exec) cudaGraphExecDestroy(exec);
   if (!rc && s->periodic && skin > 0.0) {   // hand back positions inside the cell

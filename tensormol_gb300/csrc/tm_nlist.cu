@@ -1336,7 +1336,12 @@ int tm_launch_export_ee(tm_system* s, int64_t* eep, int64_t cap) {
 // a library call cudaMalloc (a host MD engine or plugin that hands the GPU a
 // fixed arena, a serving process whose memory is budgeted up front): the
 // scratch of the cell-list build lives in one file-scope device array of fixed
-// size, reserved on every GPU that loads this library until the process exits.
+// size, held on every GPU that loads this code until the process exits. Under
+// CUDA's lazy module loading (the default) the array is committed when this
+// file's module first loads on a device: at the first call of this entry
+// point or the first neighbour-list build there. The device address is looked
+// up once per device, in the context current at that first call (the device's
+// primary context); it is not looked up again after cudaDeviceReset.
 // ---------------------------------------------------------------------------
 #define TM_STATIC_MAX_ATOMS 32768
 #define TM_STATIC_MAX_CELLS (2 * TM_STATIC_MAX_ATOMS + 64)
@@ -1415,6 +1420,8 @@ extern "C" int tm_nlist_build_static(const double* x, const int32_t* elem, int n
   if (natoms > TM_STATIC_MAX_ATOMS) return TM_E_ARG;          // beyond the fixed scratch
   if (!(a_rc > 0.0 && a_rc <= r_rc)) return TM_E_ARG;
   if ((size_t)4 * (KR + KA) * sizeof(uint64_t) > 200 * 1024) return TM_E_ARG;
+  // an error left by the caller's earlier work is not this call's: clear it
+  (void)cudaGetLastError();
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return TM_E_CUDA;
   // first call on this device: resolve the device address of the scratch
@@ -1433,11 +1440,11 @@ extern "C" int tm_nlist_build_static(const double* x, const int32_t* elem, int n
   k_grid_setup<<<1, 256, 0, st>>>(x, S->off, &S->grid, &S->ncell_m, r_rc, 0, 0.0, 0.0, 0.0, 0.0,
                                   2.0, 64.0, 0, 0, 0);
   k_grid_offsets<<<1, 256, 0, st>>>(&S->grid, &S->ncell_m, 1, &S->ncell, cap, &S->status);
-  cudaMemsetAsync(S->cell_cnt, 0, sizeof(int32_t) * (cap + 1), st);
+  if (cudaMemsetAsync(S->cell_cnt, 0, sizeof(int32_t) * (cap + 1), st) != cudaSuccess) return TM_E_CUDA;
   k_cell_count<<<tm_div_up(N, 256), 256, 0, st>>>(x, S->mol, &S->grid, S->cell_cnt, S->cell_of_atom,
                                                    N, cap, &S->status);
   k_scan_single<<<1, 1024, 0, st>>>(S->cell_cnt, S->cell_start, cap + 1);
-  cudaMemsetAsync(S->cell_cnt, 0, sizeof(int32_t) * (cap + 1), st);
+  if (cudaMemsetAsync(S->cell_cnt, 0, sizeof(int32_t) * (cap + 1), st) != cudaSuccess) return TM_E_CUDA;
   k_cell_fill<<<tm_div_up(N, 256), 256, 0, st>>>(S->cell_of_atom, S->cell_start, S->cell_cnt,
                                                   S->cell_atoms, N);
   k_cell_sort<<<tm_div_up(cap, 4), 128, 0, st>>>(S->cell_start, S->cell_atoms, S->sort_tmp, &S->ncell,
@@ -1453,8 +1460,10 @@ extern "C" int tm_nlist_build_static(const double* x, const int32_t* elem, int n
   a.ra2_hi = (float)(a_rc * a_rc) * (1.f + kBand);
   for (int q = 0; q < 9; ++q) a.lat[q] = 0.0;
   const size_t shm = (size_t)4 * (KR + KA) * sizeof(uint64_t);
-  if (shm > 48 * 1024)
-    cudaFuncSetAttribute(k_nbr_build<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  if (shm > 48 * 1024 &&
+      cudaFuncSetAttribute(k_nbr_build<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm) !=
+          cudaSuccess)
+    return TM_E_CUDA;
   k_nbr_build<false><<<tm_div_up(N, 4), 128, shm, st>>>(a);
   if (cudaGetLastError() != cudaSuccess) return TM_E_CUDA;
   // the counters the caller needs to size its rows, and the status word

@@ -195,6 +195,22 @@ class System:
         self.ctx.check(self.lib.tm_system_descriptors(self.h, _ptr(G)))
         return G
 
+    def layer_outputs(self, layer):
+        """[2, N, width] outputs of hidden layer ``layer`` of both networks
+        from the last evaluation (call after ``energy_force(x, False)``): the
+        activations, or for the last hidden layer w_out * act'(z)."""
+        width = int(self.model.p["HiddenLayers"][layer])
+        out = np.zeros((2, self.N, width), dtype=np.float32)
+        self.ctx.check(self.lib.tm_system_layer_outputs(self.h, int(layer), _ptr(out)))
+        return out
+
+    def refined_units(self):
+        """Hidden units the last evaluation recomputed in FP64 near the relu
+        kink (FP32 mode with relu; 0 otherwise)."""
+        n = ctypes.c_int64()
+        self.ctx.check(self.lib.tm_system_refined_units(self.h, ctypes.byref(n)))
+        return int(n.value)
+
     def export_ee(self):
         n = self.nlist_counts()["ee_pairs"]
         out = np.zeros((max(n, 1), 3), np.int64)

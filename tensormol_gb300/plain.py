@@ -45,7 +45,9 @@ class PlainAutograd:
         if act == "relu":
             self.act = torch.relu
         elif act == "sigmoid_with_param":
-            self.act = lambda z: torch.nn.functional.softplus(z, beta=a, threshold=1e30)
+            # log(1 + exp(a z)) / a; above a z = 20 it equals z to 2e-9 / a, and
+            # exp(a z) would overflow FP32 beyond a z = 88
+            self.act = lambda z: torch.nn.functional.softplus(z, beta=a, threshold=20.0)
         elif act == "tanh":
             self.act = torch.tanh
         elif act == "softplus":

@@ -1,7 +1,7 @@
 """Generates the golden fixtures in tests/golden/ from the reference's own code.
 
-Run here, where the reference tree is present (``TM_REFERENCE``, default
-/root/reference); the resulting .npz files are committed and travel with the
+Run where the reference tree is present (``TM_REFERENCE``, or a ``reference``
+directory beside the repository checkout; see ``refpath.py``); the resulting .npz files are committed and travel with the
 tests, so nothing at test time reads the reference tree.
 
 What is produced, per case (seeded inputs from ``tensormol_gb300.systems``):
@@ -37,7 +37,10 @@ sys.dont_write_bytecode = True
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("TM_REFERENCE", "/root/reference")
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+from refpath import reference_root  # noqa: E402
+
+REF = reference_root()
 sys.path.insert(0, REPO)
 
 from tensormol_gb300 import systems  # noqa: E402

@@ -37,7 +37,10 @@ import numpy as np
 sys.dont_write_bytecode = True
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.path.join(os.environ.get("TM_REFERENCE", "/root/reference"), "TensorMol")
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+from refpath import reference_root  # noqa: E402
+
+REF = os.path.join(reference_root(), "TensorMol")
 sys.path.insert(0, HERE)
 
 from numpy_tf import constant_tensor, tf  # noqa: E402

@@ -30,7 +30,10 @@ sys.dont_write_bytecode = True
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.path.join(os.environ.get("TM_REFERENCE", "/root/reference"), "TensorMol")
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+from refpath import reference_root  # noqa: E402
+
+REF = os.path.join(reference_root(), "TensorMol")
 sys.path.insert(0, REPO)
 
 from oracle import reference as orc  # noqa: E402

@@ -166,3 +166,42 @@ def test_pair_sums_out_of_range_are_reported(gpu):
     ref = orc.OpenSystemOracle(om, w.x, w.Z, w.offsets).terms(w.x)
     _check(out, ref, w.offsets)
     s.close()
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_bounded_wait_runs_out_and_the_context_recovers(gpu, prec):
+    """The tensor-core layer kernel's mbarrier waits are bounded. A selftest
+    product with one pipeline stage's operand loads withheld (never issued, so
+    nothing faults) and waits limited to 2^20 SM cycles must report
+    TM_E_TIMEOUT; the kernel frees its tensor memory on that path, so the next
+    launches on the same context (which allocate tensor memory again) and on a
+    fresh context compute the product correctly."""
+    import ctypes
+
+    from tensormol_gb300 import _lib
+    rng = np.random.default_rng(1)
+    M, N, K = 256, 512, 256
+    A = rng.normal(size=(M, K)).astype(np.float32)
+    B = (rng.normal(size=(N, K)) * 0.05).astype(np.float32)
+    ref = A.astype(np.float64) @ B.astype(np.float64).T
+    tol = 2e-5 if prec == 0 else 2e-2
+
+    def product(ctx):
+        C = np.zeros((M, N), np.float32)
+        ctx.check(ctx.lib.tm_selftest_gemm(ctx.h, prec, M, N, K, A.ctypes.data, B.ctypes.data,
+                                           C.ctypes.data))
+        return np.abs(C - ref).max() / np.abs(ref).max()
+
+    ctx = gpu.default_context()
+    rc = ctx.lib.tm_selftest_gemm_timeout(ctx.h, prec, ctypes.c_int64(1 << 20))
+    assert rc == _lib.ERROR_CODES["TM_E_TIMEOUT"], rc
+    buf = ctypes.create_string_buffer(256)
+    ctx.lib.tm_ctx_last_error(ctx.h, buf, 256)
+    assert b"device status 6" in buf.value, buf.value
+    for _ in range(2):
+        assert product(ctx) < tol
+    fresh = gpu.Context(0)
+    try:
+        assert product(fresh) < tol
+    finally:
+        fresh.close()

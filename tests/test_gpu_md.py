@@ -296,3 +296,27 @@ def test_skin_lists_follow_the_full_rebuild(gpu, periodic):
           % (np.abs(d).max(), np.abs(v_a - v_b).max()))
     assert np.abs(d).max() < 2e-5 and np.abs(v_a - v_b).max() < 2e-5
     np.testing.assert_allclose(l_a[:, 0], l_b[:, 0], rtol=0, atol=1e-8 * len(Z))   # Hartree
+
+
+def test_skin_replays_are_limited_per_chunk(gpu):
+    """A skin far below one step's displacement (0.002 A at 600 K) makes
+    nearly every chunk replay shorter until it is one step long: about 20
+    replays over 20 steps, every chunk completing on its retry. The replay
+    limit (16) applies to one chunk, so the run finishes, and its rows are
+    still exact: it follows the full-build run."""
+    model, md = gpu
+    w = systems.water_cluster_60(seed=0)
+    m, _ = _models(model, [1, 8])
+    v0 = systems.maxwell_boltzmann(w.Z, 600.0, seed=15)
+    out = []
+    for skin in (0.0, 0.002):
+        s = m.system(w.x, w.Z, w.offsets)
+        dyn = md.DeviceMD(s, "nve", dt=0.5, T=300.0)
+        dyn.set_velocities(v0)
+        log = dyn.run(20, skin=skin)
+        out.append((s.positions(), dyn.velocities(), log))
+        dyn.close()
+        s.close()
+    (x_a, v_a, l_a), (x_b, v_b, l_b) = out
+    assert np.abs(x_a - x_b).max() < 2e-5 and np.abs(v_a - v_b).max() < 2e-5
+    np.testing.assert_allclose(l_a[:, 0], l_b[:, 0], rtol=0, atol=1e-8 * len(w.Z))

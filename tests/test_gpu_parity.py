@@ -227,6 +227,67 @@ def test_energy_force_water24k_smooth(gpu):
     assert dE < E_TOL and dF < F_TOL, (dE, dF)
 
 
+def _oracle_preactivations(W, eles, Z, G):
+    """FP64 pre-activations z of every hidden layer, [layer][net] -> [N, width],
+    and sum|a||w| + |b| of each (the scale of any evaluation's rounding)."""
+    Z = np.asarray(Z)
+    nl = len(W["E"][eles[0]]) - 1
+    zs = [[None, None] for _ in range(nl)]
+    scale = [[None, None] for _ in range(nl)]
+    for ni, net in enumerate(("E", "Q")):
+        for li in range(nl):
+            width = np.asarray(W[net][eles[0]][li][0]).shape[1]
+            zs[li][ni] = np.zeros((len(Z), width))
+            scale[li][ni] = np.zeros((len(Z), width))
+        for e in eles:
+            idx = np.nonzero(Z == e)[0]
+            h = G[idx]
+            for li, (Wm, b) in enumerate(W[net][e][:-1]):
+                Wm = np.asarray(Wm, np.float64)
+                b = np.asarray(b, np.float64).reshape(-1)
+                z = h @ Wm + b
+                zs[li][ni][idx] = z
+                scale[li][ni][idx] = np.abs(h) @ np.abs(Wm) + np.abs(b)
+                h = np.maximum(z, 0.0)
+    return zs, scale
+
+
+def test_relu_decisions_water24k(gpu):
+    """24,000-atom cube with the reference's default relu. Every relu decision
+    of the fused FP32 path (the sign of each of the 73.7 M hidden
+    pre-activations, read from the layer outputs after an energy-only
+    evaluation) equals the FP64 oracle's, except at units whose exact
+    pre-activation lies within 2e-7 sum|a||w| of the kink: ties at the level
+    of FP32 rounding, which a plain FP32 graph of the same network flips too
+    (units out to 8e-8 measured). Without the near-kink recomputation the
+    tensor-core accumulation flipped units out to 1.3e-6. The energy stays
+    within 1e-5 eV/atom; each flipped tie moves the forces of its atom's
+    neighbourhood by up to ~0.1 eV/A, the same for any FP32 evaluation."""
+    w = systems.water_cube_24k(seed=1)
+    m, om = _model(gpu, [1, 8], "relu")
+    s = m.system(w.x, w.Z, w.offsets)
+    s.energy_force(w.x, False)
+    outs = [s.layer_outputs(l) for l in range(3)]
+    assert s.refined_units() > 0
+    W = systems.random_weights([1, 8], descriptor_width(2), seed=7)
+    ref = orc.OpenSystemOracle(om, w.x, w.Z, w.offsets).terms(w.x)
+    zs, scale = _oracle_preactivations(W, [1, 8], w.Z, ref["G"])
+    flips = []
+    for li in range(3):
+        for ni in range(2):
+            on = outs[li][ni] != 0 if li == 2 else outs[li][ni] > 0
+            bad = on != (zs[li][ni] > 0)
+            flips.extend((np.abs(zs[li][ni][bad]) / scale[li][ni][bad]).tolist())
+    print(f"relu decisions differing from FP64: {len(flips)} of "
+          f"{sum(o.size for o in outs)}; largest |z|/sum|a||w| among them: {max(flips, default=0):.2e}")
+    assert len(flips) <= 40
+    assert max(flips, default=0.0) < 2e-7
+    out = s.energy_force(w.x, True)
+    dE, dF = _errors(out, ref, w.natoms)
+    print(f"relu 24k: dE/atom={dE:.2e} eV  max|dF|={dF:.2e} eV/A")
+    assert dE < E_TOL
+
+
 def test_energy_force_chno128_smooth(gpu):
     b = systems.chno_batch(nmol=128, seed=3)
     m, om = _model(gpu, [1, 6, 7, 8], "sigmoid_with_param")
@@ -261,7 +322,7 @@ def test_energy_force_chno512_with_finite_differences(gpu):
         atoms = rng.choice(a1 - a0, 2, replace=False)
         fd = -om1.fd_gradient(b.x[a0:a1], atoms, h=1e-4) * JOULEPERHARTREE
         dfd = np.abs(out["force"][a0 + atoms] - fd).max() / JOULEPERHARTREE * EV_PER_HARTREE
-        assert dfd < 1e-3, (mol, dfd)
+        assert dfd < 1e-4, (mol, dfd)
 
 
 def test_autograd_function_gradient(gpu):
