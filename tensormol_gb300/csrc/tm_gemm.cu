@@ -201,25 +201,38 @@ __host__ __device__ constexpr uint32_t make_idesc(int ab_format, int M, int N) {
 // The activation is a template parameter: a run-time switch over all five
 // inlined into the 32-wide unrolled epilogue made the forward kernels
 // instruction-fetch bound.
+// The forward epilogue's activation h = act(z) and derivative act'(z) from
+// one exponential, with the hardware exp2/log2 approximations (__expf,
+// __logf: relative errors of a few 1e-7 on [1, 2] and below 1e-6 for exp's
+// argument range here; the absolute error of h stays below 1e-9, far under
+// the layer GEMM's). Four of the five activations spend most of the epilogue's
+// instructions on these functions, and the epilogue has one warp per
+// scheduler.
 template <int ACT>
-__device__ __forceinline__ float act_f(float z, float a) {
-  if constexpr (ACT == TM_ACT_RELU) return fmaxf(z, 0.f);
-  if constexpr (ACT == TM_ACT_SIGMOID_WITH_PARAM) {   // log(1 + exp(a z)) / a, Util.py:200-201
-    const float t = a * z;
-    return (fmaxf(t, 0.f) + log1pf(expf(-fabsf(t)))) / a;
+__device__ __forceinline__ void act_fwd(float z, float a, float& h, float& d) {
+  if constexpr (ACT == TM_ACT_RELU) {
+    h = fmaxf(z, 0.f);
+    d = z > 0.f ? 1.f : 0.f;
+  } else if constexpr (ACT == TM_ACT_SIGMOID_WITH_PARAM || ACT == TM_ACT_SOFTPLUS) {
+    // log(1 + exp(t)) / a = (max(t, 0) + log1p(exp(-|t|))) / a, t = a z;
+    // derivative sigmoid(t) = 1 / (1 + exp(-t))
+    const float t = ACT == TM_ACT_SOFTPLUS ? z : a * z;
+    const float e = __expf(-fabsf(t));
+    const float ope = 1.f + e;
+    const float l1p = ope == 1.f ? e : __logf(ope) * __fdividef(e, ope - 1.f);
+    h = ACT == TM_ACT_SOFTPLUS ? fmaxf(t, 0.f) + l1p : __fdividef(fmaxf(t, 0.f) + l1p, a);
+    d = __fdividef(t >= 0.f ? 1.f : e, ope);
+  } else if constexpr (ACT == TM_ACT_TANH) {
+    const float e = __expf(-2.f * fabsf(z));
+    const float th = __fdividef(1.f - e, 1.f + e);
+    h = copysignf(th, z);
+    d = 1.f - th * th;
+  } else {   // elu
+    h = z > 0.f ? z : expm1f(z);
+    d = z > 0.f ? 1.f : h + 1.f;
   }
-  if constexpr (ACT == TM_ACT_SOFTPLUS) return fmaxf(z, 0.f) + log1pf(expf(-fabsf(z)));
-  if constexpr (ACT == TM_ACT_TANH) return tanhf(z);
-  return z > 0.f ? z : expm1f(z);   // elu
 }
-template <int ACT>
-__device__ __forceinline__ float actd_z(float z, float a) {
-  if constexpr (ACT == TM_ACT_RELU) return z > 0.f ? 1.f : 0.f;
-  if constexpr (ACT == TM_ACT_SIGMOID_WITH_PARAM) return 1.f / (1.f + expf(-a * z));
-  if constexpr (ACT == TM_ACT_SOFTPLUS) return 1.f / (1.f + expf(-z));
-  if constexpr (ACT == TM_ACT_TANH) { const float t = tanhf(z); return 1.f - t * t; }
-  return z > 0.f ? 1.f : expf(z);
-}
+
 // derivative expressed through the activation's output h = act(z)
 template <int ACT>
 __device__ __forceinline__ float actd_h(float h, float a) {
@@ -247,6 +260,10 @@ struct Cfg {
   static constexpr int EPI_BYTES = 4 * 8192;
   static constexpr int SMEM = NSTAGE * STAGE + EPI_BYTES + 1024 + 256;   // + alignment, barriers
   static constexpr uint32_t IDESC = make_idesc(PREC == TM_PREC_FP32 ? 2 : 1, BM, BN);
+  // FP32: B hi and lo are adjacent 128-row tiles in a stage, i.e. one 256-row
+  // operand, so A_hi [B_hi; B_lo] is a single N = 256 instruction writing the
+  // main and the correction accumulator (adjacent in tensor memory)
+  static constexpr uint32_t IDESC2 = make_idesc(2, BM, 2 * BN);
 };
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* b) {
@@ -370,9 +387,10 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
             const uint64_t ad0 = sw128_desc(a0 + kk * 32), bd0 = sw128_desc(b0 + kk * 32);
             const uint32_t acc = (kb | kk) ? 1u : 0u;
             if (PREC == TM_PREC_FP32) {
-              const uint64_t ad1 = sw128_desc(a1 + kk * 32), bd1 = sw128_desc(b1 + kk * 32);
-              umma_tf32(d, ad0, bd0, C::IDESC, acc);
-              umma_tf32(d + BN, ad0, bd1, C::IDESC, acc);
+              const uint64_t ad1 = sw128_desc(a1 + kk * 32);
+              // A_hi B_hi -> main, A_hi B_lo -> correction (one instruction: A_hi is
+              // read once), then A_lo B_hi -> correction
+              umma_tf32(d, ad0, bd0, C::IDESC2, acc);
               umma_tf32(d + BN, ad1, bd0, C::IDESC, 1u);
             } else {
               umma_f16(d, ad0, bd0, C::IDESC, acc);
@@ -482,12 +500,14 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
             if constexpr (KINK) {
               if (fabsf(z) < kthr * __ldg(g.wnorm + pblk + col + q)) km |= 1u << q;
             }
+            float h, dz;
+            act_fwd<ACT>(z, g.alpha, h, dz);
             if (EPI == EPI_FWD) {
-              v[q] = act_f<ACT>(z, g.alpha);
+              v[q] = h;
               if constexpr (KINK) hss = fmaf(v[q], v[q], hss);
             } else {
-              esum += act_f<ACT>(z, g.alpha) * wq[q];
-              v[q] = wq[q] * actd_z<ACT>(z, g.alpha);
+              esum += h * wq[q];
+              v[q] = wq[q] * dz;
             }
           }
           if constexpr (KINK) {
