@@ -123,9 +123,12 @@ int tm_model_destroy(tm_model *m);
  * A batch of molecules in CSR order: atoms of molecule m are
  * mol_offsets[m] .. mol_offsets[m+1]-1. Replaces the padded
  * [nmol, MaxNAtoms] feed of EvalBPDirectEEUpdateSet (TFMolManage.py:1260-1276).
- * cell: NULL for open boundaries, else 9 doubles of lattice vectors (rows);
- * only orthorhombic cells with every edge >= 2 * the largest cutoff are
- * accepted. Z is host memory.
+ * cell: NULL for open boundaries, else 9 doubles of lattice vectors (rows,
+ * any shape, Periodic.py:12-24) whose three plane spacings (volume / area of
+ * the opposite faces) are all at least twice the largest cutoff, so that at
+ * most one image of an atom is within a cutoff of another (TM_E_ARG
+ * otherwise); positions are expected inside the cell (ModuloLattice,
+ * Periodic.py:87-100). Z is host memory.
  */
 int tm_system_create(tm_model *m, int natoms, int nmol, const int32_t *Z,
                      const int64_t *mol_offsets, const double *cell, tm_system **out);
@@ -310,6 +313,13 @@ int tm_system_descriptors(tm_system *s, float *G_out);
  * its intermediate tensors internal).
  */
 int tm_system_layer_outputs(tm_system *s, int layer, float *out);
+/*
+ * The network layers of the last evaluation run again (forward, then backward,
+ * from the same descriptor rows) with CUDA events around each tensor-core
+ * layer launch only: ms[2 * n_hidden] = forward layers 0 .. n_hidden-1, then
+ * backward layers n_hidden-1 .. 0, in ms. No counterpart in the reference.
+ */
+int tm_system_profile_layers(tm_system *s, float *ms);
 /*
  * FP32 mode with relu: the number of hidden-unit pre-activations that the
  * last evaluation recomputed in FP64 because they lay within the tensor-core

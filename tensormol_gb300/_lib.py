@@ -36,7 +36,7 @@ EXPORTS = [
     "tm_system_export_nlist", "tm_system_export_ee", "tm_energy_force",
     "tm_md_create", "tm_md_destroy", "tm_md_set_velocities", "tm_md_get_velocities", "tm_md_run",
     "tm_selftest_gemm", "tm_selftest_gemm_timeout", "tm_model_erfc_poly", "tm_system_descriptors", "tm_energy_force_profile",
-    "tm_system_refined_units", "tm_system_layer_outputs",
+    "tm_system_refined_units", "tm_system_layer_outputs", "tm_system_profile_layers",
     "tm_nlist_build_static",
     "tm_serve_create", "tm_serve_destroy", "tm_serve_info", "tm_serve_layout", "tm_serve_step",
     "tm_serve_read",
@@ -106,6 +106,7 @@ def _declare(lib):
         "tm_energy_force_profile": (I, [P, U, P]),
         "tm_system_refined_units": (I, [P, P]),
         "tm_system_layer_outputs": (I, [P, I, P]),
+        "tm_system_profile_layers": (I, [P, P]),
         "tm_nlist_build_static": (I, [P, P, I, D, D, P, P, I, P, P, I, P, P]),
         "tm_serve_create": (I, [P, I, I, D, PP]),
         "tm_serve_destroy": (I, [P]),

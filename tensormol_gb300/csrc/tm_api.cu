@@ -3,6 +3,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
+
+#include <cmath>
 #include <string.h>
 
 #include <algorithm>
@@ -585,7 +587,7 @@ static int build_layout(tm_system* s, int N, int nmol, const int32_t* Z, const i
   if (s->periodic) {
     long nc = 1, ne = 1;
     for (int d = 0; d < 3; ++d) {
-      nc *= (long)floor(s->lat[4 * d] / k.r_rc_d);
+      nc *= (long)floor(s->hpl[d] / k.r_rc_d);
       ne *= s->ee_dims[d];
     }
     L.ncell_cap = (int)nc;
@@ -816,26 +818,54 @@ extern "C" int tm_system_create(tm_model* m, int N, int nmol, const int32_t* Z,
   const tm_consts& k = m->k;
   if (cell) {
     for (int q = 0; q < 9; ++q) s->lat[q] = cell[q];
-    if (cell[1] != 0 || cell[2] != 0 || cell[3] != 0 || cell[5] != 0 || cell[6] != 0 || cell[7] != 0) {
-      delete s;
-      return tm_fail(ctx, TM_E_UNSUPPORTED, "only orthorhombic cells are supported");
-    }
     if (nmol != 1) { delete s; return tm_fail(ctx, TM_E_ARG, "a periodic system is one molecule"); }
-    const double Lmin = std::min(cell[0], std::min(cell[4], cell[8]));
-    const double rmax = std::max(k.r_rc_d, k.ree_d);
-    if (Lmin < 2.0 * rmax) {
+    // any three lattice vectors (Periodic.py:12-24): the cells of both grids
+    // are slices between lattice planes, binned by each atom's distance from
+    // the planes through the origin (its coordinate along the plane normals)
+    const double* a0 = cell;
+    const double* a1 = cell + 3;
+    const double* a2 = cell + 6;
+    auto cross = [](const double* u, const double* v, double* w) {
+      w[0] = u[1] * v[2] - u[2] * v[1];
+      w[1] = u[2] * v[0] - u[0] * v[2];
+      w[2] = u[0] * v[1] - u[1] * v[0];
+    };
+    double c[3][3];
+    cross(a1, a2, c[0]);
+    cross(a2, a0, c[1]);
+    cross(a0, a1, c[2]);
+    const double vol = a0[0] * c[0][0] + a0[1] * c[0][1] + a0[2] * c[0][2];
+    if (!(std::fabs(vol) > 0.0) || !std::isfinite(vol)) {
       delete s;
-      return tm_fail(ctx, TM_E_ARG, "cell edges must be at least twice the largest cutoff");
+      return tm_fail(ctx, TM_E_ARG, "lattice vectors are linearly dependent");
     }
-    // With edges >= 2 * cutoff, a +-R cell search (R = ceil(cutoff / cell
-    // edge) <= ceil(n / 2) <= n) wraps at most once per axis and reaches each
-    // (cell, image) at most once; the exact distance test keeps the one image
-    // within the cutoff.
+    s->ortho = cell[1] == 0 && cell[2] == 0 && cell[3] == 0 && cell[5] == 0 && cell[6] == 0 &&
+               cell[7] == 0 && cell[0] > 0 && cell[4] > 0 && cell[8] > 0;
+    for (int d = 0; d < 3; ++d) {
+      const double cn = std::sqrt(c[d][0] * c[d][0] + c[d][1] * c[d][1] + c[d][2] * c[d][2]);
+      const double sg = vol > 0 ? 1.0 : -1.0;
+      for (int e = 0; e < 3; ++e) {
+        s->nrm[3 * d + e] = s->ortho ? (e == d ? 1.0 : 0.0) : sg * c[d][e] / cn;
+        s->binv[3 * e + d] = c[d][e] / vol;
+      }
+      s->hpl[d] = s->ortho ? cell[4 * d] : std::fabs(vol) / cn;
+    }
+    const double hmin = std::min(s->hpl[0], std::min(s->hpl[1], s->hpl[2]));
+    const double rmax = std::max(k.r_rc_d, k.ree_d);
+    if (hmin < 2.0 * rmax) {
+      delete s;
+      return tm_fail(ctx, TM_E_ARG, "the spacing of every pair of opposite cell faces must be at "
+                                    "least twice the largest cutoff");
+    }
+    // With plane spacings >= 2 * cutoff, every nonzero lattice vector is at
+    // least 2 * cutoff long, so at most one image of an atom lies within the
+    // cutoff of another, and a +-R cell search (R = ceil(cutoff / cell
+    // spacing) <= n / 2) wraps at most once per axis and reaches each
+    // (cell, image) at most once; the exact distance test keeps that image.
     s->periodic = true;
-    // Coulomb grid: floor(L / size) cells per edge, about 24 atoms per cell
-    const double vol = cell[0] * cell[4] * cell[8];
-    const double cs = std::max(2.0, cbrt(24.0 * vol / N));
-    for (int d = 0; d < 3; ++d) s->ee_dims[d] = std::max(1, std::min(4096, (int)floor(cell[4 * d] / cs)));
+    // Coulomb grid: floor(h / size) cells per plane spacing, ~24 atoms per cell
+    const double cs = std::max(2.0, cbrt(24.0 * std::fabs(vol) / N));
+    for (int d = 0; d < 3; ++d) s->ee_dims[d] = std::max(1, std::min(4096, (int)floor(s->hpl[d] / cs)));
   }
   SysLayout L;
   int rc = build_layout(s, N, nmol, Z, off, L);
@@ -1184,6 +1214,12 @@ extern "C" int tm_system_layer_outputs(tm_system* s, int layer, float* out) {
       }
     }
   return TM_OK;
+}
+
+extern "C" int tm_system_profile_layers(tm_system* s, float* ms) {
+  if (!s || !ms) return TM_E_ARG;
+  if (!s->nlist_valid) return tm_fail(s->ctx, TM_E_STATE, "evaluate the system first");
+  return tm_profile_layers(s, ms);
 }
 
 extern "C" int tm_system_refined_units(tm_system* s, int64_t* n) {

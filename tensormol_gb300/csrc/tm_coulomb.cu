@@ -141,6 +141,8 @@ struct CoulArgs {
   float pre2;               // candidate-vs-centre-box screen: ree^2 (1 + 2e-5)
   float inv_bohr, inv_b2, inv_vdw_width, c_lin;   // 1/bohr, 1/bohr^2, 1/width, zz/R_lr + yy
   double lat[9];
+  int ortho;                // periodic: orthorhombic cell
+  double cu[9];             // periodic, not orthorhombic: grid-cell edges a_d / n_d (rows)
   float sh_hi[27][3];
   float sh_lo[27][3];
 };
@@ -327,6 +329,11 @@ __device__ __forceinline__ void coulomb_drain(const CoulArgs& a, const StageSmem
   }
 }
 
+// TRIC: a periodic cell that is not orthorhombic (grid cells are slices
+// between lattice planes, spanned by the edges a_d / n_d in a.cu; a cell
+// offset (ox, oy, oz) moves by ox u0 + oy u1 + oz u2, and the gaps along the
+// three plane normals bound the distance by their maximum).
+template <bool TRIC>
 __global__ void __launch_bounds__(128, 6) k_coulomb(const CoulArgs a, const tm_consts k) {
   __shared__ StageSmem stage[4];
   __shared__ float tab[2][TM_MAX_ELE * TM_MAX_ELE];   // sqrt(C6_i C6_j), R0_i + R0_j
@@ -392,7 +399,16 @@ __global__ void __launch_bounds__(128, 6) k_coulomb(const CoulArgs a, const tm_c
     const int ti = t0 + lane;
     const bool have = ti < t1;
     float4 pi = a.exhi[have ? ti : t0];
-    if (have) pi.z += (float)((a.cell_of[a.eatom[ti]] - head - z0) * g.cz);
+    if (have) {
+      const int dzc = a.cell_of[a.eatom[ti]] - head - z0;
+      if constexpr (TRIC) {
+        pi.x += (float)(dzc * a.cu[6]);
+        pi.y += (float)(dzc * a.cu[7]);
+        pi.z += (float)(dzc * a.cu[8]);
+      } else {
+        pi.z += (float)(dzc * g.cz);
+      }
+    }
     const float qi = a.exlo[have ? ti : t0].w;
     const int ei = __float_as_int(pi.w);
     const float* s6row = tab[0] + ei * k.nele;
@@ -418,7 +434,9 @@ __global__ void __launch_bounds__(128, 6) k_coulomb(const CoulArgs a, const tm_c
       const float offx = (float)(ox * g.cx), offy = (float)(oy * g.cy);
       for (int zc = (col == 0 ? z0 : z0 - Rz); zc <= z1 + Rz; ++zc) {
         const float gapz = fmaxf(0.f, (float)(max(z0 - zc, zc - z1) - 1)) * cz;
-        if (gapx * gapx + gapy * gapy + gapz * gapz > a.reach2) continue;
+        if (TRIC ? fmaxf(gapx * gapx, fmaxf(gapy * gapy, gapz * gapz)) > a.reach2
+                 : gapx * gapx + gapy * gapy + gapz * gapz > a.reach2)
+          continue;
         int jx = ix + ox, jy = iy + oy, jz = zc, sx = 0, sy = 0, sz = 0;
         if (a.periodic) {
           if (jx < 0) { jx += g.nx; sx = -1; } else if (jx >= g.nx) { jx -= g.nx; sx = 1; }
@@ -429,7 +447,14 @@ __global__ void __launch_bounds__(128, 6) k_coulomb(const CoulArgs a, const tm_c
         }
         const int cj = g.cell_off + (jx * g.ny + jy) * g.nz + jz;
         const uint32_t rcode = (uint32_t)(9 * (sx + 1) + 3 * (sy + 1) + (sz + 1)) << 27;
-        const float offz = (float)((zc - z0) * g.cz);
+        float3 off;
+        if constexpr (TRIC) {
+          off.x = (float)(ox * a.cu[0] + oy * a.cu[3] + (zc - z0) * a.cu[6]);
+          off.y = (float)(ox * a.cu[1] + oy * a.cu[4] + (zc - z0) * a.cu[7]);
+          off.z = (float)(ox * a.cu[2] + oy * a.cu[5] + (zc - z0) * a.cu[8]);
+        } else {
+          off = make_float3(offx, offy, (float)((zc - z0) * g.cz));
+        }
         const int kadd = col == 0 ? (sz > 0 ? ncolumn : 0) : -1;
         const int u1 = a.cell_start[cj + 1];
         for (int u0 = a.cell_start[cj]; u0 < u1; u0 += 32) {
@@ -441,7 +466,7 @@ __global__ void __launch_bounds__(128, 6) k_coulomb(const CoulArgs a, const tm_c
           float qj = 0.f;
           if (t < u1) {
             const float4 pr = a.exhi[t];
-            pj = make_float4(pr.x + offx, pr.y + offy, pr.z + offz, pr.w);
+            pj = make_float4(pr.x + off.x, pr.y + off.y, pr.z + off.z, pr.w);
             qj = a.exlo[t].w;
             const float ex = fmaxf(0.f, fmaxf(bx0 - pj.x, pj.x - bx1));
             const float ey = fmaxf(0.f, fmaxf(by0 - pj.y, pj.y - by1));
@@ -597,9 +622,15 @@ int tm_launch_coulomb(tm_system* s, unsigned flags) {
   a.inv_vdw_width = (float)(1.0 / (double)k.vdw_width);
   a.c_lin = (float)((double)k.zz / (double)k.r_lr + (double)k.yy);
   for (int q = 0; q < 9; ++q) a.lat[q] = s->lat[q];
+  a.ortho = s->ortho ? 1 : 0;
+  for (int d = 0; d < 3; ++d)   // the periodic Coulomb grid has ee_dims cells per lattice vector
+    for (int e = 0; e < 3; ++e) a.cu[3 * d + e] = s->periodic ? s->lat[3 * d + e] / s->ee_dims[d] : 0.0;
   tm_fill_shifts(s, a.sh_hi, a.sh_lo);
   cudaMemsetAsync(s->d_cacc, 0, sizeof(unsigned long long) * 5 * (size_t)s->N, ctx->stream);
-  k_coulomb<<<tm_div_up(a.blk_cap * TM_EE_SPLIT, 4), 128, 0, ctx->stream>>>(a, k);
+  if (s->periodic && !s->ortho)
+    k_coulomb<true><<<tm_div_up(a.blk_cap * TM_EE_SPLIT, 4), 128, 0, ctx->stream>>>(a, k);
+  else
+    k_coulomb<false><<<tm_div_up(a.blk_cap * TM_EE_SPLIT, 4), 128, 0, ctx->stream>>>(a, k);
   k_coulomb_finish<<<tm_div_up(s->N, 256), 256, 0, ctx->stream>>>(a);
   ctx->launches += 2;
   k_chunk_sum2<<<s->nchunk, 256, 0, ctx->stream>>>(s->d_chunk, s->d_ecv, s->d_dEdq, s->d_q,

@@ -849,12 +849,28 @@ int tm_make_tmap(tm_ctx* ctx, CUtensorMap* map, void* base, int elem_bytes, uint
 //   fwd 0..L-1 (last one: energy dot product + g_L = w_out * act'(z_L)),
 //   bwd L-1..1 (g_{l-1} = (g_l W_l^T) * act'(z_{l-1}), in place over h_{l-1}),
 //   bwd 0 (dE/dG = g_1 W_1^T, FP32).
-static int mlp_layers(tm_system* s, bool forward, bool backward);
+// ev (optional): 2 events per layer GEMM launch, recorded around it (forward
+// layers first, then backward), for tm_system_profile_layers.
+static int mlp_layers(tm_system* s, bool forward, bool backward, cudaEvent_t* ev = nullptr);
 
 int tm_launch_mlp(tm_system* s, bool backward) { return mlp_layers(s, true, backward); }
 int tm_launch_mlp_backward_only(tm_system* s) { return mlp_layers(s, false, true); }
 
-static int mlp_layers(tm_system* s, bool forward, bool backward) {
+int tm_profile_layers(tm_system* s, float* ms) {
+  tm_ctx* ctx = s->ctx;
+  const int L = s->model->nlayer;
+  std::vector<cudaEvent_t> ev(4 * L);
+  for (auto& e : ev) cudaEventCreate(&e);
+  int rc = mlp_layers(s, true, true, ev.data());
+  if (!rc) rc = tm_cuda_check(ctx, cudaEventSynchronize(ev[4 * L - 1]), "profile layers");
+  if (!rc)
+    for (int q = 0; q < 2 * L; ++q) cudaEventElapsedTime(&ms[q], ev[2 * q], ev[2 * q + 1]);
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (!rc) rc = tm_sync_status(ctx, "profile layers");
+  return rc;
+}
+
+static int mlp_layers(tm_system* s, bool forward, bool backward, cudaEvent_t* ev) {
   tm_model* m = s->model;
   tm_ctx* ctx = s->ctx;
   const int L = m->nlayer;
@@ -910,7 +926,9 @@ static int mlp_layers(tm_system* s, bool forward, bool backward) {
       g.an2_net_stride = l == 0 ? 0 : s->Mpad * nparts;
       g.hn2_out = last ? nullptr : s->kink_h2[l & 1];
     }
+    if (ev) cudaEventRecord(ev[2 * l], ctx->stream);
     if ((rc = dispatch(ctx, prec, last ? EPI_FWD_LAST : EPI_FWD, g, mt))) return rc;
+    if (ev) cudaEventRecord(ev[2 * l + 1], ctx->stream);
     if (kink) {
       KinkArgs ka;
       ka.a_hi = static_cast<const float*>(l == 0 ? s->G[0] : bufH[l - 1][0]);
@@ -954,14 +972,18 @@ static int mlp_layers(tm_system* s, bool forward, bool backward) {
       g.out1 = bufH[l - 1][1];
       g.o0 = *stH[l - 1][0];
       g.o1 = *stH[l - 1][1];
+      if (ev) cudaEventRecord(ev[2 * (2 * L - 1 - l)], ctx->stream);
       if ((rc = dispatch(ctx, prec, EPI_BWD, g, mt))) return rc;
+      if (ev) cudaEventRecord(ev[2 * (2 * L - 1 - l) + 1], ctx->stream);
     } else {
       g.N = Dp;
       g.ldo = Dp;
       g.out0 = s->dEdG;
       g.out1 = nullptr;
       g.o0 = s->ts_dEdG;
+      if (ev) cudaEventRecord(ev[2 * (2 * L - 1)], ctx->stream);
       if ((rc = dispatch(ctx, prec, EPI_OUT, g, mt))) return rc;
+      if (ev) cudaEventRecord(ev[2 * (2 * L - 1) + 1], ctx->stream);
     }
   }
   return TM_OK;

@@ -117,6 +117,14 @@ struct tm_system {
   int Mpad_cap = 0, nchunk_cap = 0, ncell_alloc = 0, ecell_alloc = 0;
   bool periodic = false;
   double lat[9] = {0};
+  // general cells: unit normals of the three lattice planes (rows; plane d is
+  // spanned by the other two lattice vectors, a_d . n_d > 0), their spacings,
+  // and B^-1 (fractional f = x B^-1, f_d = sum_i x_i binv[3 i + d]); open
+  // systems keep the identity normals, which bin by Cartesian coordinate
+  double nrm[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  double hpl[3] = {0, 0, 0};
+  double binv[9] = {0};
+  bool ortho = true;                   // orthorhombic (or open)
   std::vector<int32_t> Z;              // host
   std::vector<int64_t> off;            // host
   std::vector<int32_t> elem_h;         // element index per atom
@@ -261,6 +269,7 @@ int tm_make_tmap(tm_ctx* ctx, CUtensorMap* map, void* base, int elem_bytes, uint
                  uint64_t cols, uint32_t box_rows);
 int tm_launch_mlp(tm_system* s, bool backward);
 int tm_launch_mlp_backward_only(tm_system* s);
+int tm_profile_layers(tm_system* s, float* ms);   // [2 * nlayer] ms
 int tm_gemm_bn(int prec);   // GEMM N tile of a precision mode (128 or 256)
 float tm_kink_kappa(int K); // relu refinement: flag bound per unit of ||a|| ||w||
 int tm_gemm_selftest(tm_ctx* ctx, int prec, int M, int N, int K, const float* A,
@@ -271,3 +280,13 @@ int tm_launch_coulomb(tm_system* s, unsigned flags);
 int tm_launch_finish(tm_system* s, unsigned flags);
 
 static inline int tm_div_up(int a, int b) { return (a + b - 1) / b; }
+
+// Nine doubles by value (a lattice, its inverse, or plane normals) for kernels.
+struct tm_mat3 {
+  double v[9];
+};
+static inline tm_mat3 tm_mat3_of(const double* p) {
+  tm_mat3 m;
+  for (int q = 0; q < 9; ++q) m.v[q] = p[q];
+  return m;
+}

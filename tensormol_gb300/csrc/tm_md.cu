@@ -80,16 +80,30 @@ __global__ void k_vv_vel(double* __restrict__ v, double* __restrict__ a, const d
   a[q] = an;
 }
 
-__global__ void k_wrap(double* __restrict__ x, double Lx, double Ly, double Lz, int N) {
+// Positions into the cell (ModuloLattice, Periodic.py:87-100): orthorhombic
+// cells per axis, others through fractional coordinates f = x B^-1, f - floor(f).
+__global__ void k_wrap(double* __restrict__ x, const tm_mat3 lat, const tm_mat3 binv, int ortho,
+                       int N) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
-  const double L[3] = {Lx, Ly, Lz};
-  for (int d = 0; d < 3; ++d) {
-    double v = x[3 * i + d];
-    v = v - L[d] * floor(v / L[d]);
-    if (v >= L[d]) v -= L[d];
-    x[3 * i + d] = v;
+  if (ortho) {
+    const double L[3] = {lat.v[0], lat.v[4], lat.v[8]};
+    for (int d = 0; d < 3; ++d) {
+      double v = x[3 * i + d];
+      v = v - L[d] * floor(v / L[d]);
+      if (v >= L[d]) v -= L[d];
+      x[3 * i + d] = v;
+    }
+    return;
   }
+  const double p[3] = {x[3 * i], x[3 * i + 1], x[3 * i + 2]};
+  double f[3];
+  for (int d = 0; d < 3; ++d) {
+    f[d] = p[0] * binv.v[d] + p[1] * binv.v[3 + d] + p[2] * binv.v[6 + d];
+    f[d] -= floor(f[d]);
+    if (f[d] >= 1.0) f[d] -= 1.0;
+  }
+  for (int d = 0; d < 3; ++d) x[3 * i + d] = f[0] * lat.v[d] + f[1] * lat.v[3 + d] + f[2] * lat.v[6 + d];
 }
 
 // Nose: x, v(dt/2) (SimpleMD.py:117-118)
@@ -350,7 +364,7 @@ static int md_step(tm_md* md, double* dlog, int* dstep) {
   if (md->kind == TM_MD_NVE) {
     k_vv_pos<<<gb, 256, 0, st>>>(s->d_x, md->v, md->a, dt, n3);
     ctx->launches++;
-    if (wrap) { k_wrap<<<tm_div_up(N, 256), 256, 0, st>>>(s->d_x, s->lat[0], s->lat[4], s->lat[8], N); ctx->launches++; }
+    if (wrap) { k_wrap<<<tm_div_up(N, 256), 256, 0, st>>>(s->d_x, tm_mat3_of(s->lat), tm_mat3_of(s->binv), s->ortho, N); ctx->launches++; }
     if ((rc = tm_energy_force_device(s, flags))) return rc;
     k_vv_vel<<<gb, 256, 0, st>>>(md->v, md->a, s->d_F, md->m, dt, n3);
     ctx->launches++;
@@ -359,7 +373,7 @@ static int md_step(tm_md* md, double* dlog, int* dstep) {
     ke_into(md, md->v, S_KE2);
     k_nose_pos<<<gb, 256, 0, st>>>(s->d_x, md->v, md->a, md->vh, md->sc, dt, n3);
     ctx->launches++;
-    if (wrap) { k_wrap<<<tm_div_up(N, 256), 256, 0, st>>>(s->d_x, s->lat[0], s->lat[4], s->lat[8], N); ctx->launches++; }
+    if (wrap) { k_wrap<<<tm_div_up(N, 256), 256, 0, st>>>(s->d_x, tm_mat3_of(s->lat), tm_mat3_of(s->binv), s->ortho, N); ctx->launches++; }
     ke_into(md, md->vh, S_KE2B);
     if ((rc = tm_energy_force_device(s, flags))) return rc;
     k_nose_eta<<<1, 1, 0, st>>>(md->sc, md->Qnose, md->kT, (double)N, dt);
@@ -373,7 +387,7 @@ static int md_step(tm_md* md, double* dlog, int* dstep) {
     k_kick<<<gb, 256, 0, st>>>(md->v, md->a, 0.5 * dt, n3);
     k_drift<<<gb, 256, 0, st>>>(s->d_x, md->v, dt, n3);
     ctx->launches += 4;
-    if (wrap) { k_wrap<<<tm_div_up(N, 256), 256, 0, st>>>(s->d_x, s->lat[0], s->lat[4], s->lat[8], N); ctx->launches++; }
+    if (wrap) { k_wrap<<<tm_div_up(N, 256), 256, 0, st>>>(s->d_x, tm_mat3_of(s->lat), tm_mat3_of(s->binv), s->ortho, N); ctx->launches++; }
     if ((rc = tm_energy_force_device(s, flags))) return rc;
     k_accel<<<gb, 256, 0, st>>>(md->a, s->d_F, md->m, n3);
     k_kick<<<gb, 256, 0, st>>>(md->v, md->a, 0.5 * dt, n3);
@@ -508,7 +522,7 @@ extern "C" int tm_md_run(tm_md* md, int nsteps, double skin, double* log) {
   }
   if (exec) cudaGraphExecDestroy(exec);
   if (!rc && s->periodic && skin > 0.0) {   // hand back positions inside the cell
-    k_wrap<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_x, s->lat[0], s->lat[4], s->lat[8], s->N);
+    k_wrap<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_x, tm_mat3_of(s->lat), tm_mat3_of(s->binv), s->ortho, s->N);
     ctx->launches++;
   }
   s->need_sticky = false;

@@ -220,15 +220,22 @@ __device__ __forceinline__ int cell_coord(double v, double o, double c, int n) {
   return q < 0 ? 0 : (q >= n ? n - 1 : q);
 }
 
+// nrm: rows are the directions the cells are sliced along (the lattice
+// planes' unit normals of a periodic cell, whose cell spacings g.c* are
+// measured along them; the identity for open systems and orthorhombic cells,
+// for which the coordinate is the Cartesian one exactly)
 __global__ void k_cell_count(const double* __restrict__ x, const int32_t* __restrict__ mol,
                              const tm_grid* __restrict__ grid, int32_t* __restrict__ cnt,
-                             int32_t* __restrict__ cell_of, int N, int cap, tm_dev_status* st) {
+                             int32_t* __restrict__ cell_of, int N, int cap, tm_dev_status* st,
+                             const tm_mat3 nrm) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   const tm_grid g = grid[mol[i]];
-  int ix = cell_coord(x[3 * i], g.ox, g.cx, g.nx);
-  int iy = cell_coord(x[3 * i + 1], g.oy, g.cy, g.ny);
-  int iz = cell_coord(x[3 * i + 2], g.oz, g.cz, g.nz);
+  const double xi = x[3 * i], yi = x[3 * i + 1], zi = x[3 * i + 2];
+  const double* n = nrm.v;
+  int ix = cell_coord(xi * n[0] + yi * n[1] + zi * n[2], g.ox, g.cx, g.nx);
+  int iy = cell_coord(xi * n[3] + yi * n[4] + zi * n[5], g.oy, g.cy, g.ny);
+  int iz = cell_coord(xi * n[6] + yi * n[7] + zi * n[8], g.oz, g.cz, g.nz);
   int c = g.cell_off + (ix * g.ny + iy) * g.nz + iz;
   if (c < 0 || c >= cap) {   // cannot happen for a valid grid; never index out of range
     tm_flag(st, TM_E_CAPACITY, i, 2);
@@ -289,10 +296,13 @@ __global__ void __launch_bounds__(128) k_cell_sort(const int32_t* __restrict__ s
 // Coulomb-grid packing: atoms in cell order with their positions relative to
 // the origin of their own cell (FP64 difference rounded once to FP32; w =
 // element). The charge (olo.w) is written after the charge network.
+// A periodic cell's grid cell (ix, iy, iz) has its origin at
+// ix a0/nx + iy a1/ny + iz a2/nz (lat: the lattice vectors as rows).
 __global__ void k_ee_pack(const int32_t* __restrict__ order, const double* __restrict__ x,
                           const int32_t* __restrict__ elem, const int32_t* __restrict__ mol,
                           const tm_grid* __restrict__ grid, const int32_t* __restrict__ cell_of,
-                          int32_t* __restrict__ pos, float4* __restrict__ ohi, int N) {
+                          int32_t* __restrict__ pos, float4* __restrict__ ohi, int N,
+                          const tm_mat3 lat) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= N) return;
   const int a = order[p];
@@ -300,8 +310,18 @@ __global__ void k_ee_pack(const int32_t* __restrict__ order, const double* __res
   const tm_grid g = grid[mol[a]];
   const int lc = cell_of[a] - g.cell_off;
   const int iz = lc % g.nz, iy = (lc / g.nz) % g.ny, ix = lc / (g.nz * g.ny);
-  ohi[p] = make_float4((float)(x[3 * a] - (g.ox + ix * g.cx)), (float)(x[3 * a + 1] - (g.oy + iy * g.cy)),
-                       (float)(x[3 * a + 2] - (g.oz + iz * g.cz)), __int_as_float(elem[a]));
+  double o[3];
+  if (g.periodic) {
+    const double* L = lat.v;
+    for (int d = 0; d < 3; ++d)
+      o[d] = ix * (L[d] / g.nx) + iy * (L[3 + d] / g.ny) + iz * (L[6 + d] / g.nz);
+  } else {
+    o[0] = g.ox + ix * g.cx;
+    o[1] = g.oy + iy * g.cy;
+    o[2] = g.oz + iz * g.cz;
+  }
+  ohi[p] = make_float4((float)(x[3 * a] - o[0]), (float)(x[3 * a + 1] - o[1]),
+                       (float)(x[3 * a + 2] - o[2]), __int_as_float(elem[a]));
 }
 
 // Centre blocks of the pair-term kernel: runs of up to 32 consecutive atoms
@@ -910,6 +930,8 @@ struct FiltArgs {
   double rr, ra;
   float rr2_lo, rr2_hi, ra2_lo, ra2_hi;
   double lat[9];
+  double binv[9];
+  int ortho;
   float sh_hi[27][3], sh_lo[27][3];
 };
 
@@ -968,14 +990,22 @@ __global__ void __launch_bounds__(128) k_nbr_filter(const FiltArgs a) {
     a.cnt_r[i] = min(nr, a.KR);
     a.cnt_a[i] = min(na, a.KA);
     double d2 = 0.0;
-    for (int d = 0; d < 3; ++d) {
-      double u = a.x[3 * i + d] - a.x0[3 * i + d];
-      if (a.periodic) {   // wrapped into the cell since the build: nearest image
+    double u[3];
+    for (int d = 0; d < 3; ++d) u[d] = a.x[3 * i + d] - a.x0[3 * i + d];
+    if (a.periodic && a.ortho) {   // wrapped into the cell since the build: nearest image
+      for (int d = 0; d < 3; ++d) {
         const double L = a.lat[4 * d];
-        u -= L * rint(u / L);
+        u[d] -= L * rint(u[d] / L);
       }
-      d2 += u * u;
+    } else if (a.periodic) {       // the same in fractional coordinates
+      double f[3];
+      for (int d = 0; d < 3; ++d) {
+        f[d] = u[0] * a.binv[d] + u[1] * a.binv[3 + d] + u[2] * a.binv[6 + d];
+        f[d] -= rint(f[d]);
+      }
+      for (int d = 0; d < 3; ++d) u[d] = f[0] * a.lat[d] + f[1] * a.lat[3 + d] + f[2] * a.lat[6 + d];
     }
+    for (int d = 0; d < 3; ++d) d2 += u[d] * u[d];
     atomicMax(a.disp, (unsigned long long)__double_as_longlong(d2));
   }
 }
@@ -993,7 +1023,11 @@ int launch_filter(tm_system* s) {
   a.rr2_hi = (float)(k.r_rc_d * k.r_rc_d) * (1.f + kBand);
   a.ra2_lo = (float)(k.a_rc_d * k.a_rc_d) * (1.f - kBand);
   a.ra2_hi = (float)(k.a_rc_d * k.a_rc_d) * (1.f + kBand);
-  for (int q = 0; q < 9; ++q) a.lat[q] = s->lat[q];
+  for (int q = 0; q < 9; ++q) {
+    a.lat[q] = s->lat[q];
+    a.binv[q] = s->binv[q];
+  }
+  a.ortho = s->ortho ? 1 : 0;
   tm_fill_shifts(s, a.sh_hi, a.sh_lo);
   k_nbr_filter<<<tm_div_up(s->N, 4), 128, 0, ctx->stream>>>(a);
   ctx->launches++;
@@ -1019,7 +1053,7 @@ static int launch_ee_grid(tm_system* s) {
   int rc;
   k_grid_from_chunks<<<tm_div_up(s->nmol, 4), 128, 0, st>>>(
       s->d_cbox, s->d_mol_chunk, s->d_off, s->d_egrid, s->d_encell_m, s->nmol, 2.0,
-      s->periodic ? 1 : 0, s->lat[0], s->lat[4], s->lat[8], 24.0, 0.125, 8.0, s->ee_dims[0],
+      s->periodic ? 1 : 0, s->hpl[0], s->hpl[1], s->hpl[2], 24.0, 0.125, 8.0, s->ee_dims[0],
       s->ee_dims[1], s->ee_dims[2], s->nmol == 1 ? s->d_encell : nullptr, s->ecell_cap,
       ctx->d_status);
   if (s->nmol > 1) {
@@ -1030,7 +1064,7 @@ static int launch_ee_grid(tm_system* s) {
   cudaMemsetAsync(s->d_ecell_cnt, 0, sizeof(int32_t) * (s->ecell_cap + 1), st);
   k_cell_count<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_x, s->d_mol, s->d_egrid, s->d_ecell_cnt,
                                                       s->d_ecell_of_atom, s->N, s->ecell_cap,
-                                                      ctx->d_status);
+                                                      ctx->d_status, tm_mat3_of(s->nrm));
   ctx->launches += 2;
   if ((rc = scan_exclusive<int32_t>(ctx, s->d_ecell_cnt, s->d_ecell_start, s->ecell_cap + 1,
                                     nullptr, s->d_scan_tmp2)))
@@ -1042,7 +1076,7 @@ static int launch_ee_grid(tm_system* s) {
                                                             s->d_sort_tmp2, s->d_encell, s->ecell_cap);
   k_ee_pack<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_ecell_atoms, s->d_x, s->d_elem, s->d_mol,
                                                   s->d_egrid, s->d_ecell_of_atom, s->d_epos,
-                                                  s->d_exhi, s->N);
+                                                  s->d_exhi, s->N, tm_mat3_of(s->lat));
   cudaMemsetAsync(s->d_neblk, 0, sizeof(int32_t), st);
   k_ee_blocks<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_ecell_atoms, s->d_mol, s->d_egrid,
                                                     s->d_ecell_of_atom, s->d_ecell_start,
@@ -1091,7 +1125,7 @@ static int launch_nbr_rows(tm_system* s) {
   int rc;
   k_grid_from_chunks<<<tm_div_up(s->nmol, 4), 128, 0, st>>>(
       s->d_cbox, s->d_mol_chunk, s->d_off, s->d_grid, s->d_ncell_m, s->nmol, k.r_rc_d + s->skin,
-      s->periodic ? 1 : 0, s->lat[0], s->lat[4], s->lat[8], 0.0, 2.0, 64.0, 0, 0, 0,
+      s->periodic ? 1 : 0, s->hpl[0], s->hpl[1], s->hpl[2], 0.0, 2.0, 64.0, 0, 0, 0,
       s->nmol == 1 ? s->d_ncell : nullptr, s->ncell_cap, ctx->d_status);
   ctx->launches++;
   if (s->nmol > 1) {
@@ -1102,7 +1136,7 @@ static int launch_nbr_rows(tm_system* s) {
   cudaMemsetAsync(s->d_cell_cnt, 0, sizeof(int32_t) * (s->ncell_cap + 1), st);
   k_cell_count<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_x, s->d_mol, s->d_grid, s->d_cell_cnt,
                                                       s->d_cell_of_atom, s->N, s->ncell_cap,
-                                                      ctx->d_status);
+                                                      ctx->d_status, tm_mat3_of(s->nrm));
   ctx->launches++;
   if ((rc = scan_exclusive<int32_t>(ctx, s->d_cell_cnt, s->d_cell_start, s->ncell_cap + 1,
                                     nullptr, s->d_scan_tmp)))
@@ -1170,7 +1204,7 @@ int tm_launch_nlist_filter(tm_system* s) {
                                                         s->d_elem, s->d_mol, s->d_off, s->N);
   k_ee_pack<<<tm_div_up(s->N, 256), 256, 0, st>>>(s->d_ecell_atoms, s->d_x, s->d_elem, s->d_mol,
                                                   s->d_egrid, s->d_ecell_of_atom, s->d_epos,
-                                                  s->d_exhi, s->N);
+                                                  s->d_exhi, s->N, tm_mat3_of(s->lat));
   ctx->launches += 2;
   s->nlist_valid = true;
   return tm_cuda_check(ctx, cudaGetLastError(), "nlist filter");
@@ -1441,8 +1475,9 @@ extern "C" int tm_nlist_build_static(const double* x, const int32_t* elem, int n
                                   2.0, 64.0, 0, 0, 0);
   k_grid_offsets<<<1, 256, 0, st>>>(&S->grid, &S->ncell_m, 1, &S->ncell, cap, &S->status);
   if (cudaMemsetAsync(S->cell_cnt, 0, sizeof(int32_t) * (cap + 1), st) != cudaSuccess) return TM_E_CUDA;
+  const double ident[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};   // open boundary: Cartesian bins
   k_cell_count<<<tm_div_up(N, 256), 256, 0, st>>>(x, S->mol, &S->grid, S->cell_cnt, S->cell_of_atom,
-                                                   N, cap, &S->status);
+                                                   N, cap, &S->status, tm_mat3_of(ident));
   k_scan_single<<<1, 1024, 0, st>>>(S->cell_cnt, S->cell_start, cap + 1);
   if (cudaMemsetAsync(S->cell_cnt, 0, sizeof(int32_t) * (cap + 1), st) != cudaSuccess) return TM_E_CUDA;
   k_cell_fill<<<tm_div_up(N, 256), 256, 0, st>>>(S->cell_of_atom, S->cell_start, S->cell_cnt,

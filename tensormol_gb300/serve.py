@@ -53,6 +53,7 @@ class Request:
         self.rid = Request._next
         Request._next += 1
         self.steps_done = 0
+        self.overtaken = 0        # times a later request was admitted first
         self.energies = []        # per step: (Etotal, Ebp, Ecc, Evdw) Hartree
         self.x = self.v = self.F = None
         self.t_submit = self.t_admit = self.t_done = None
@@ -69,9 +70,22 @@ class Request:
 class Server:
     """Continuous batching over one tm_serve. ``max_atoms``/``max_mols`` bound
     the batch; ``capacity_for_budget`` derives ``max_atoms`` from an HBM byte
-    budget."""
+    budget.
 
-    def __init__(self, model, max_atoms=65536, max_mols=512, dt=0.5):
+    admission: "fifo" admits strictly in arrival order (a request that does not
+    fit blocks the ones behind it); "first_fit" looks at up to ``lookahead``
+    waiting requests in arrival order and admits every one that fits, so a
+    large request at the head does not leave the batch half empty, but a
+    request that has been overtaken ``max_overtakes`` times stops later ones
+    from passing it until it is admitted (no request waits forever)."""
+
+    def __init__(self, model, max_atoms=65536, max_mols=512, dt=0.5, admission="fifo",
+                 lookahead=64, max_overtakes=8):
+        if admission not in ("fifo", "first_fit"):
+            raise ValueError("admission must be 'fifo' or 'first_fit'")
+        self.admission = admission
+        self.lookahead = int(lookahead)
+        self.max_overtakes = int(max_overtakes)
         self.model = model
         self.ctx = model.ctx
         self.lib = model.lib
@@ -122,21 +136,21 @@ class Server:
             self.active = []
             return
         Z = np.concatenate([r.Z for r in reqs]).astype(np.int32)
+        counts = np.fromiter((r.natoms for r in reqs), dtype=np.int64, count=nmol)
         offs = np.zeros(nmol + 1, dtype=np.int64)
-        offs[1:] = np.cumsum([r.natoms for r in reqs])
-        mode = np.array([_lib.TM_SERVE[r.kind] for r in reqs], dtype=np.int32)
-        src = np.empty(int(offs[-1]), dtype=np.int32)
-        k = 0
-        xn, vn = [], []
-        for q, r in enumerate(reqs):
-            a, b = offs[q], offs[q + 1]
-            if r.rid in old_off:
-                src[a:b] = old_off[r.rid] + np.arange(r.natoms, dtype=np.int32)
-            else:
-                src[a:b] = -(k + 1 + np.arange(r.natoms, dtype=np.int32))
-                k += r.natoms
-                xn.append(r.x0)
-                vn.append(r.v0)
+        np.cumsum(counts, out=offs[1:])
+        mode = np.fromiter((_lib.TM_SERVE[r.kind] for r in reqs), dtype=np.int32, count=nmol)
+        # gather map, vectorised: kept rows point at their old index, the k-th
+        # new row is -(k+1) (new rows numbered in layout order)
+        is_new = np.fromiter((r.rid not in old_off for r in reqs), dtype=bool, count=nmol)
+        new_counts = np.where(is_new, counts, 0)
+        new_start = np.cumsum(new_counts) - new_counts
+        base = np.where(is_new, -1 - new_start,
+                        np.fromiter((old_off.get(r.rid, 0) for r in reqs), dtype=np.int64, count=nmol))
+        local = np.arange(int(offs[-1]), dtype=np.int64) - np.repeat(offs[:-1], counts)
+        src = (np.repeat(base, counts) + np.where(np.repeat(is_new, counts), -local, local)).astype(np.int32)
+        xn = [r.x0 for r in admit]
+        vn = [r.v0 for r in admit]
         xn = np.ascontiguousarray(np.concatenate(xn)) if xn else None
         vn = np.ascontiguousarray(np.concatenate(vn)) if vn else None
         self.ctx.check(self.lib.tm_serve_layout(self.h, nmol, _p(Z), _p(offs), _p(mode), _p(src),
@@ -147,16 +161,42 @@ class Server:
         atoms = sum(r.natoms for r in keep)
         slots = len(keep)
         admit = []
-        while self.pending:
-            r = self.pending[0]
+        if self.admission == "fifo":
+            while self.pending:
+                r = self.pending[0]
+                if r.natoms > self.max_atoms:
+                    raise ValueError(f"request of {r.natoms} atoms exceeds the capacity {self.max_atoms}")
+                if atoms + r.natoms > self.max_atoms or slots + 1 > self.max_mols:
+                    break
+                self.pending.pop(0)
+                atoms += r.natoms
+                slots += 1
+                admit.append(r)
+            return admit
+        rest, skipped = [], []
+        last_admitted = -1
+        blocked = False       # a request overtaken too often holds back later ones
+        for i, r in enumerate(self.pending):
             if r.natoms > self.max_atoms:
                 raise ValueError(f"request of {r.natoms} atoms exceeds the capacity {self.max_atoms}")
-            if atoms + r.natoms > self.max_atoms or slots + 1 > self.max_mols:
-                break
-            self.pending.pop(0)
-            atoms += r.natoms
-            slots += 1
-            admit.append(r)
+            fits = atoms + r.natoms <= self.max_atoms and slots + 1 <= self.max_mols
+            if fits and not blocked and i < self.lookahead:
+                atoms += r.natoms
+                slots += 1
+                admit.append(r)
+                last_admitted = i
+                continue
+            if not fits and not blocked and i < self.lookahead:
+                if r.overtaken >= self.max_overtakes:
+                    blocked = True
+                else:
+                    skipped.append((i, r))
+            rest.append(r)
+        # a request counts as overtaken when one behind it got in
+        for i, r in skipped:
+            if i < last_admitted:
+                r.overtaken += 1
+        self.pending = rest
         return admit
 
     # -- one step -------------------------------------------------------------
@@ -190,13 +230,13 @@ class Server:
                 if not np.all(np.isfinite(x)):
                     r.error = "non-finite positions"
         natoms = 0
-        for q, r in enumerate(self.active):
+        for r, e, fm in zip(self.active, E, fmax):   # rows of fresh arrays: no copies
             r.steps_done += 1
-            r.energies.append(E[q].copy())
+            r.energies.append(e)
             natoms += r.natoms
             if r.kind == "opt":
                 # the force of the positions just evaluated (the step's x)
-                r.fmax_last = fmax[q] / JOULEPERHARTREE * EV_PER_HARTREE
+                r.fmax_last = fm / JOULEPERHARTREE * EV_PER_HARTREE
                 r.converged = r.fmax_last <= r.fmax
         for q, r in enumerate(self.active):
             if r.done:

@@ -62,6 +62,8 @@ class _FakeLib:
             if md == _lib.TM_SERVE["md"]:
                 self.x[a:b, 0] += 1.0
             E[q] = (b - a, 0, 0, 0)
+        if fmax is not None:     # optimisation requests: converged at once
+            _arr(fmax, ctypes.c_double, len(self.mode))[:] = 0.0
         return 0
 
     def tm_serve_read(self, h, q, x, v, F):
@@ -118,3 +120,63 @@ def test_admission_is_fifo_within_capacity():
     assert all(r.done for r in (a, b, c))
     assert max(srv.step_atoms) <= 30
     assert a.t_admit <= b.t_admit <= c.t_admit
+
+
+def test_first_fit_admission_fills_the_batch_and_bounds_overtaking():
+    m = _Model()
+    srv = serve.Server(m, max_atoms=30, max_mols=4, admission="first_fit", max_overtakes=2)
+    a, b, c = _req(20, "md", 2), _req(15, "md", 2), _req(5, "md", 2)
+    for r in (a, b, c):
+        srv.submit(r)
+    srv.step()
+    # b (15) does not fit beside a (20); c (5) does and goes ahead of it
+    assert [r.rid for r in srv.active] == [a.rid, c.rid]
+    assert b.overtaken == 1
+    srv.drain()
+    assert all(r.done for r in (a, b, c)) and max(srv.step_atoms) <= 30
+
+
+def test_first_fit_stops_overtaking_a_request_that_waited_long_enough():
+    m = _Model()
+    srv = serve.Server(m, max_atoms=30, max_mols=8, admission="first_fit", max_overtakes=1)
+    big = _req(20, "md", 50)
+    srv.submit(big)
+    srv.step()                                 # big runs for 50 steps
+    head = _req(15, "md", 1)                   # cannot fit beside big
+    srv.submit(head)
+    small = [_req(6, "md", 1) for _ in range(3)]
+    for r in small:
+        srv.submit(r)
+    srv.step()                                 # small[0] overtakes head
+    assert head.overtaken == 1
+    admitted = {r.rid for r in srv.active}
+    assert small[0].rid in admitted and small[1].rid not in admitted
+    srv.step()                                 # head may not be overtaken again
+    admitted = {r.rid for r in srv.active}
+    assert small[1].rid not in admitted and small[2].rid not in admitted
+    srv.drain()
+    assert head.t_admit <= small[1].t_admit and head.t_admit <= small[2].t_admit
+
+
+def test_vectorised_gather_map_matches_the_rule():
+    m = _Model()
+    srv = serve.Server(m, max_atoms=200, max_mols=8)
+    reqs = [_req(n, "md", s, k) for k, (n, s) in enumerate([(7, 1), (3, 5), (11, 2), (4, 4)])]
+    for r in reqs[:3]:
+        srv.submit(r)
+    srv.step()
+    srv.submit(reqs[3])
+    srv.drain()
+    for r in reqs:
+        np.testing.assert_array_equal(r.x[:, 1], r.x0[:, 1])
+
+
+def test_optimisation_requests_retire_on_convergence():
+    m = _Model()
+    srv = serve.Server(m, max_atoms=100, max_mols=4, admission="first_fit")
+    a, b = _req(6, "opt", 200), _req(8, "md", 3)
+    srv.submit(a)
+    srv.submit(b)
+    srv.drain()
+    assert a.converged and a.steps_done == 1 and a.fmax_last == 0.0
+    assert b.steps_done == 3
