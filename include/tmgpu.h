@@ -124,11 +124,17 @@ int tm_model_destroy(tm_model *m);
  * mol_offsets[m] .. mol_offsets[m+1]-1. Replaces the padded
  * [nmol, MaxNAtoms] feed of EvalBPDirectEEUpdateSet (TFMolManage.py:1260-1276).
  * cell: NULL for open boundaries, else 9 doubles of lattice vectors (rows,
- * any shape, Periodic.py:12-24) whose three plane spacings (volume / area of
- * the opposite faces) are all at least twice the largest cutoff, so that at
- * most one image of an atom is within a cutoff of another (TM_E_ARG
- * otherwise); positions are expected inside the cell (ModuloLattice,
- * Periodic.py:87-100). Z is host memory.
+ * any shape, Periodic.py:12-24); positions are expected inside the cell
+ * (ModuloLattice, Periodic.py:87-100). When a plane spacing of the cell
+ * (volume / area of the opposite faces) is below twice the largest cutoff,
+ * several images of an atom reach another (the reference tessellates more
+ * shells, Periodic.py:143-147): such a cell is evaluated as the smallest
+ * supercell (at most 4096 copies) whose spacings reach twice the cutoff, and
+ * tm_energy_force returns the energy per cell and the cell's own atoms'
+ * forces, charges and per-atom energies; list export, the images-fixed force
+ * (TM_F_REFERENCE_PERIODIC_FORCE) and MD of such a cell return
+ * TM_E_UNSUPPORTED. Linearly dependent lattice vectors give TM_E_ARG.
+ * Z is host memory.
  */
 int tm_system_create(tm_model *m, int natoms, int nmol, const int32_t *Z,
                      const int64_t *mol_offsets, const double *cell, tm_system **out);

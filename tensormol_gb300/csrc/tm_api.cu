@@ -853,9 +853,39 @@ extern "C" int tm_system_create(tm_model* m, int N, int nmol, const int32_t* Z,
     const double hmin = std::min(s->hpl[0], std::min(s->hpl[1], s->hpl[2]));
     const double rmax = std::max(k.r_rc_d, k.ree_d);
     if (hmin < 2.0 * rmax) {
+      // a small cell: evaluated as the smallest supercell whose plane
+      // spacings are at least twice the largest cutoff
+      int rep[3];
+      long K = 1;
+      for (int d = 0; d < 3; ++d) {
+        rep[d] = std::max(1, (int)std::ceil(2.0 * rmax / s->hpl[d] * (1.0 + 1e-12)));
+        K *= rep[d];
+      }
+      if (K > 4096 || (long)N * K >= (1L << 26)) {
+        delete s;
+        return tm_fail(ctx, TM_E_ARG, "cell too small for its cutoffs (more than 4096 copies)");
+      }
+      std::vector<double> sup(9);
+      for (int d = 0; d < 3; ++d)
+        for (int e = 0; e < 3; ++e) sup[3 * d + e] = rep[d] * cell[3 * d + e];
+      std::vector<int32_t> Zs((size_t)N * K);
+      for (long c = 0; c < K; ++c)
+        for (int a = 0; a < N; ++a) Zs[c * N + a] = Z[a];
+      const int64_t offs[2] = {0, (int64_t)N * K};
       delete s;
-      return tm_fail(ctx, TM_E_ARG, "the spacing of every pair of opposite cell faces must be at "
-                                    "least twice the largest cutoff");
+      tm_system* sup_s = nullptr;
+      int rc = tm_system_create(m, (int)(N * K), 1, Zs.data(), offs, sup.data(), &sup_s);
+      if (rc) return rc;
+      for (int d = 0; d < 3; ++d) sup_s->rep[d] = rep[d];
+      sup_s->K = (int)K;
+      sup_s->N_user = N;
+      for (int q = 0; q < 9; ++q) sup_s->user_lat[q] = cell[q];
+      if ((rc = tm_alloc(ctx, (void**)&sup_s->d_xuser, sizeof(double) * 3 * (size_t)N))) {
+        tm_system_destroy(sup_s);
+        return rc;
+      }
+      *out = sup_s;
+      return TM_OK;
     }
     // With plane spacings >= 2 * cutoff, every nonzero lattice vector is at
     // least 2 * cutoff long, so at most one image of an atom lies within the
@@ -867,6 +897,9 @@ extern "C" int tm_system_create(tm_model* m, int N, int nmol, const int32_t* Z,
     const double cs = std::max(2.0, cbrt(24.0 * std::fabs(vol) / N));
     for (int d = 0; d < 3; ++d) s->ee_dims[d] = std::max(1, std::min(4096, (int)floor(s->hpl[d] / cs)));
   }
+  s->N_user = N;
+  if (cell)
+    for (int q = 0; q < 9; ++q) s->user_lat[q] = cell[q];
   SysLayout L;
   int rc = build_layout(s, N, nmol, Z, off, L);
   if (!rc) rc = system_alloc(s, N, nmol, L.Mpad, L.nchunk, L.ncell_cap, L.ecell_cap);
@@ -922,7 +955,7 @@ static void system_free(tm_system* s) {
                   s->d_cell_cnt, s->d_cell_start, s->d_cell_atoms, s->d_cell_of_atom, s->d_cnt_r,
                   s->d_cnt_a, s->d_nbr_r, s->d_nbr_a, s->d_rev_r, s->d_rev_a, s->d_sr, s->d_va,
                   s->dEdG, s->epart, s->d_Eatom, s->d_qraw, s->d_q, s->d_dEdq, s->d_fself,
-                  s->d_fcv, s->d_ecv, s->d_F, s->d_mol_E, s->d_mol_aux, s->kink_g2, s->kink_h2[0],
+                  s->d_fcv, s->d_ecv, s->d_F, s->d_mol_E, s->d_mol_aux, s->d_xuser, s->kink_g2, s->kink_h2[0],
                   s->kink_h2[1], s->kink_mask, s->kink_count};
   for (void* p : ptrs)
     if (p) cudaFreeAsync(p, ctx->stream);
@@ -946,12 +979,48 @@ extern "C" int tm_system_destroy(tm_system* s) {
   return TM_OK;
 }
 
-extern "C" int tm_system_natoms(const tm_system* s) { return s ? s->N : -1; }
+// Small cells: copy c = (c0 r1 + c1) r2 + c2 of atom a at x_a + c0 a0 + c1 a1
+// + c2 a2, formed left to right as the reference's tessellation forms images
+// (Periodic.py:170-173).
+__global__ void k_replicate(const double* __restrict__ xu, double* __restrict__ X, int N, int r1,
+                            int r2, int K, const tm_mat3 lat) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= N * K) return;
+  const int c = q / N, a = q - c * N;
+  const int c0 = c / (r1 * r2), c1 = (c / r2) % r1, c2 = c % r2;
+  for (int d = 0; d < 3; ++d)
+    X[3 * q + d] = tm_image_coord(xu[3 * a + d], c0, c1, c2, lat.v[d], lat.v[3 + d], lat.v[6 + d]);
+}
+
+// per-cell totals of a replicated system: the supercell's energies and dipole / K
+__global__ void k_per_cell(double* __restrict__ mol_E, double* __restrict__ mol_aux, double invK) {
+  const int t = threadIdx.x;
+  if (t < 4) mol_E[t] *= invK;
+  if (t >= 4 && t < 7) mol_aux[2 + t - 4] *= invK;
+}
+
+static int user_natoms(const tm_system* s) { return s->K > 1 ? s->N_user : s->N; }
+
+// positions of a replicated system: the caller's cell into d_xuser, then the copies
+static int replicate_positions(tm_system* s, const double* x, cudaMemcpyKind kind) {
+  tm_ctx* ctx = s->ctx;
+  int rc = tm_cuda_check(ctx, cudaMemcpyAsync(s->d_xuser, x, sizeof(double) * 3 * s->N_user, kind,
+                                              ctx->stream), "positions");
+  if (rc) return rc;
+  k_replicate<<<tm_div_up(s->N, 256), 256, 0, ctx->stream>>>(s->d_xuser, s->d_x, s->N_user, s->rep[1],
+                                                             s->rep[2], s->K, tm_mat3_of(s->user_lat));
+  ctx->launches++;
+  return tm_cuda_check(ctx, cudaGetLastError(), "replicate");
+}
+
+extern "C" int tm_system_natoms(const tm_system* s) { return s ? user_natoms(s) : -1; }
 
 extern "C" int tm_system_set_positions(tm_system* s, const double* x, int on_device) {
   if (!s || !x) return TM_E_ARG;
   tm_ctx* ctx = s->ctx;
   s->nlist_valid = false;
+  if (s->K > 1)
+    return replicate_positions(s, x, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice);
   return tm_cuda_check(ctx, cudaMemcpyAsync(s->d_x, x, sizeof(double) * 3 * s->N,
                                             on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                                             ctx->stream),
@@ -961,7 +1030,7 @@ extern "C" int tm_system_set_positions(tm_system* s, const double* x, int on_dev
 extern "C" int tm_system_get_positions(tm_system* s, double* x, int on_device) {
   if (!s || !x) return TM_E_ARG;
   tm_ctx* ctx = s->ctx;
-  int rc = tm_cuda_check(ctx, cudaMemcpyAsync(x, s->d_x, sizeof(double) * 3 * s->N,
+  int rc = tm_cuda_check(ctx, cudaMemcpyAsync(x, s->d_x, sizeof(double) * 3 * user_natoms(s),
                                               on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
                                               ctx->stream),
                          "positions");
@@ -983,6 +1052,8 @@ extern "C" int tm_system_build_nlist(tm_system* s) {
 
 extern "C" int tm_system_nlist_counts(tm_system* s, int64_t counts[4]) {
   if (!s || !counts) return TM_E_ARG;
+  if (s->K > 1)
+    return tm_fail(s->ctx, TM_E_UNSUPPORTED, "list export of a cell below twice the cutoff");
   if (!s->nlist_valid) return tm_fail(s->ctx, TM_E_STATE, "neighbour lists not built");
   return tm_count_nlist(s, counts);
 }
@@ -990,6 +1061,8 @@ extern "C" int tm_system_nlist_counts(tm_system* s, int64_t counts[4]) {
 extern "C" int tm_system_export_nlist(tm_system* s, int64_t* radp, int64_t* angt, int64_t* mil_j,
                                       int64_t* mil_jk, int on_device) {
   if (!s) return TM_E_ARG;
+  if (s->K > 1)
+    return tm_fail(s->ctx, TM_E_UNSUPPORTED, "list export of a cell below twice the cutoff");
   tm_ctx* ctx = s->ctx;
   if (!s->nlist_valid) return tm_fail(ctx, TM_E_STATE, "neighbour lists not built");
   int64_t c[4];
@@ -1018,6 +1091,8 @@ extern "C" int tm_system_export_nlist(tm_system* s, int64_t* radp, int64_t* angt
 
 extern "C" int tm_system_export_ee(tm_system* s, int64_t* eep, int64_t cap, int on_device) {
   if (!s || !eep) return TM_E_ARG;
+  if (s->K > 1)
+    return tm_fail(s->ctx, TM_E_UNSUPPORTED, "list export of a cell below twice the cutoff");
   tm_ctx* ctx = s->ctx;
   if (!s->nlist_valid) return tm_fail(ctx, TM_E_STATE, "neighbour lists not built");
   if (on_device) return tm_launch_export_ee(s, eep, cap);
@@ -1122,12 +1197,18 @@ extern "C" int tm_energy_force(tm_system* s, const double* x, unsigned flags, do
   tm_ctx* ctx = s->ctx;
   const bool dev = flags & TM_F_DEVICE_IO;
   int rc;
+  if (s->K > 1 && (flags & TM_F_REFERENCE_PERIODIC_FORCE))
+    return tm_fail(ctx, TM_E_UNSUPPORTED, "the images-fixed force of a cell below twice the cutoff");
   if (x) {
-    if ((rc = tm_cuda_check(ctx, cudaMemcpyAsync(s->d_x, x, sizeof(double) * 3 * s->N,
-                                                 dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
-                                                 ctx->stream),
-                            "x")))
+    if (s->K > 1) {
+      if ((rc = replicate_positions(s, x, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice)))
+        return rc;
+    } else if ((rc = tm_cuda_check(ctx, cudaMemcpyAsync(s->d_x, x, sizeof(double) * 3 * s->N,
+                                                        dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                                        ctx->stream),
+                                   "x"))) {
       return rc;
+    }
     if (!(flags & TM_F_REUSE_NLIST)) s->nlist_valid = false;
   }
   for (int attempt = 0;; ++attempt) {
@@ -1139,21 +1220,27 @@ extern "C" int tm_energy_force(tm_system* s, const double* x, unsigned flags, do
   }
   const cudaMemcpyKind kind = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
   cudaStream_t st = ctx->stream;
+  // a replicated cell: copy 0's per-atom results, the supercell's totals / K
+  const int Nu = user_natoms(s);
+  if (s->K > 1) {
+    k_per_cell<<<1, 32, 0, st>>>(s->d_mol_E, s->d_mol_aux, 1.0 / s->K);
+    ctx->launches++;
+  }
   if (E_out) cudaMemcpyAsync(E_out, s->d_mol_E, sizeof(double) * 4 * s->nmol, kind, st);
-  if (F_out && !(flags & TM_F_ENERGY_ONLY)) cudaMemcpyAsync(F_out, s->d_F, sizeof(double) * 3 * s->N, kind, st);
-  if (Eatom_out) cudaMemcpyAsync(Eatom_out, s->d_Eatom, sizeof(double) * s->N, kind, st);
+  if (F_out && !(flags & TM_F_ENERGY_ONLY)) cudaMemcpyAsync(F_out, s->d_F, sizeof(double) * 3 * Nu, kind, st);
+  if (Eatom_out) cudaMemcpyAsync(Eatom_out, s->d_Eatom, sizeof(double) * Nu, kind, st);
   if (q_out || dipole_out) {
     // q (float) and dipole (aux[2..4]) are converted on the host side
-    std::vector<float> qf(s->N);
+    std::vector<float> qf(Nu);
     std::vector<double> aux((size_t)8 * s->nmol);
-    cudaMemcpyAsync(qf.data(), s->d_q, sizeof(float) * s->N, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(qf.data(), s->d_q, sizeof(float) * Nu, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(aux.data(), s->d_mol_aux, sizeof(double) * 8 * s->nmol, cudaMemcpyDeviceToHost, st);
     if ((rc = tm_sync_status(ctx, "energy_force"))) return rc;
-    std::vector<double> qd(s->N), dip((size_t)3 * s->nmol);
-    for (int i = 0; i < s->N; ++i) qd[i] = qf[i];
+    std::vector<double> qd(Nu), dip((size_t)3 * s->nmol);
+    for (int i = 0; i < Nu; ++i) qd[i] = qf[i];
     for (int m = 0; m < s->nmol; ++m)
       for (int d = 0; d < 3; ++d) dip[3 * m + d] = aux[8 * m + 2 + d];
-    if (q_out) cudaMemcpy(q_out, qd.data(), sizeof(double) * s->N, dev ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost);
+    if (q_out) cudaMemcpy(q_out, qd.data(), sizeof(double) * Nu, dev ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost);
     if (dipole_out) cudaMemcpy(dipole_out, dip.data(), sizeof(double) * 3 * s->nmol, dev ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost);
   }
   return tm_sync_status(ctx, "energy_force");
@@ -1200,10 +1287,11 @@ extern "C" int tm_system_layer_outputs(tm_system* s, int layer, float* out) {
     return rc;
   }
   if ((rc = tm_sync_status(ctx, "layer outputs"))) return rc;
+  const int Nu = user_natoms(s);
   for (int net = 0; net < 2; ++net)
-    for (int i = 0; i < s->N; ++i) {
+    for (int i = 0; i < Nu; ++i) {
       const size_t src = ((size_t)net * s->Mpad + s->row_of_atom_h[i]) * H;
-      float* dst = out + ((size_t)net * s->N + i) * width;
+      float* dst = out + ((size_t)net * Nu + i) * width;
       for (int c = 0; c < width; ++c) {
         if (split) {
           dst[c] = hi[src + c] + lo[src + c];
@@ -1258,7 +1346,7 @@ extern "C" int tm_system_descriptors(tm_system* s, float* G_out) {
     rc = tm_cuda_check(ctx, cudaMemcpyAsync(rows.data(), dev, rows.size() * 4, cudaMemcpyDeviceToHost, ctx->stream), "G");
     if (!rc) rc = tm_sync_status(ctx, "descriptors");
     if (!rc)
-      for (int i = 0; i < s->N; ++i)
+      for (int i = 0; i < user_natoms(s); ++i)
         memcpy(G_out + (size_t)i * D, rows.data() + (size_t)s->row_of_atom_h[i] * Dp, sizeof(float) * D);
   }
   tm_free(ctx, dev, sizeof(float) * (size_t)s->Mpad * Dp);

@@ -125,6 +125,15 @@ struct tm_system {
   double hpl[3] = {0, 0, 0};
   double binv[9] = {0};
   bool ortho = true;                   // orthorhombic (or open)
+  // a cell smaller than twice the largest cutoff across some plane spacing is
+  // evaluated as a supercell of rep[0] x rep[1] x rep[2] copies (lat is then
+  // the supercell's lattice, user_lat the cell's): the caller's N_user atoms
+  // are copy 0, the others follow copy-major (atom a of copy c at c N_user + a)
+  int rep[3] = {1, 1, 1};
+  int K = 1;                           // number of copies
+  int N_user = 0;
+  double user_lat[9] = {0};
+  double* d_xuser = nullptr;           // [N_user][3] caller positions (replicated systems)
   std::vector<int32_t> Z;              // host
   std::vector<int64_t> off;            // host
   std::vector<int32_t> elem_h;         // element index per atom

@@ -256,6 +256,9 @@ extern "C" int tm_md_create(tm_system* s, int kind, double dt, double T, int cha
   if (!s || dt <= 0 || T < 0) return TM_E_ARG;
   tm_ctx* ctx = s->ctx;
   if (kind < TM_MD_NVE || kind > TM_MD_NHC) return tm_fail(ctx, TM_E_ARG, "md kind");
+  // a cell below twice the cutoff is evaluated as a supercell whose copies
+  // would drift apart in a trajectory (their FP32 sums run in different orders)
+  if (s->K > 1) return tm_fail(ctx, TM_E_UNSUPPORTED, "MD of a cell below twice the cutoff");
   if (kind == TM_MD_NHC && (chain < 1 || chain > 10)) return tm_fail(ctx, TM_E_ARG, "chain length 1..10");
   tm_md* md = new tm_md();
   md->s = s;

@@ -4,8 +4,9 @@ twice the 9 A Coulomb cutoff. Lists bit-exact against the oracle's 27-image
 tessellation; FP32 energies within 1e-5 eV/atom and forces within 1e-4 eV/A of
 the FP64 oracle (conservative force and the reference's own, images held
 fixed); skin lists in a device MD run follow a full rebuild every step (the
-positions are wrapped through fractional coordinates). A cell whose plane
-spacing is below twice the largest cutoff is rejected with TM_E_ARG.
+positions are wrapped through fractional coordinates). Lattice vectors without
+volume are rejected with TM_E_ARG (cells below twice the cutoff are covered in
+test_gpu_periodic_small.py).
 """
 import numpy as np
 import pytest
@@ -99,12 +100,12 @@ def test_triclinic_skin_lists_follow_the_full_rebuild(tric):
     np.testing.assert_allclose(l_a[:, 0], l_b[:, 0], rtol=0, atol=1e-8 * len(b.Z))
 
 
-def test_cells_below_twice_the_cutoff_are_rejected(tric):
+def test_degenerate_lattices_are_rejected(tric):
     from tensormol_gb300 import _lib
     model, md, b, B, x, p, W = tric
     m = model.BPEEModel([1, 8], W, params=p, precision="fp32")
-    thin = B.copy()
-    thin[2] = [0.1 * L, -0.2 * L, 15.0]                 # plane spacing 15 A < 18 A
+    flat = B.copy()
+    flat[2] = B[0] + B[1]                                # no volume
     with pytest.raises(_lib.TmError) as err:
-        m.system(orc.modulo_lattice(x, thin), b.Z, None, thin)
+        m.system(x, b.Z, None, flat)
     assert err.value.code == _lib.ERROR_CODES["TM_E_ARG"]
