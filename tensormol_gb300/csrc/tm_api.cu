@@ -760,9 +760,9 @@ static int system_alloc(tm_system* s, int N_cap, int nmol_cap, int Mpad_cap, int
     A.get(&s->G3[h], 2 * Mp * H * es);
   }
   A.get(&s->dEdG, sizeof(float) * 2 * Mp * Dp);
-  A.get(&s->epart, sizeof(float) * 2 * Mp * (H / tm_gemm_bn(m->desc.precision)));
+  A.get(&s->epart, sizeof(float) * 2 * Mp * tm_gemm_row_parts(m->desc.precision, H));
   if (m->kink) {
-    const size_t parts = H / tm_gemm_bn(m->desc.precision);
+    const size_t parts = tm_gemm_row_parts(m->desc.precision, H);
     A.get(&s->kink_g2, sizeof(float) * Mp);
     A.get(&s->kink_h2[0], sizeof(float) * 2 * Mp * parts);
     A.get(&s->kink_h2[1], sizeof(float) * 2 * Mp * parts);

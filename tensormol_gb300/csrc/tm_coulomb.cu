@@ -586,7 +586,7 @@ void tm_fill_shifts(const tm_system* s, float hi[27][3], float lo[27][3]);
 int tm_launch_mlp_finish(tm_system* s) {
   tm_ctx* ctx = s->ctx;
   tm_model* m = s->model;
-  const int nsplit = m->H / tm_gemm_bn(m->desc.precision);
+  const int nsplit = tm_gemm_row_parts(m->desc.precision, m->H);
   k_mlp_finish<<<s->nchunk, 256, 0, ctx->stream>>>(s->d_chunk, s->epart, m->bout, s->row_of_atom,
                                                    s->d_elem, nsplit, s->Mpad, m->k.nele,
                                                    s->d_Eatom, s->d_qraw, s->d_part);

@@ -55,7 +55,7 @@ struct GemmArgs {
   float alpha;
   const float* bias;   // [2][nele][N]
   const float* wout;   // [2][nele][N]
-  float* epart;        // [2][Mpad][N/BN], BN of the precision mode
+  float* epart;        // [2][Mpad][2 N/BN]: per (N tile, column half), BN of the precision mode
   void* out0;
   void* out1;
   int ldo;
@@ -68,7 +68,7 @@ struct GemmArgs {
   const float* an2;     // squared norms of the input rows: an2_parts partial sums per row
   int an2_parts;
   int an2_net_stride;   // floats between the two nets' rows (0: shared input)
-  float* hn2_out;       // [2][Mpad][ntiles] partial squared norms of the outputs (or null)
+  float* hn2_out;       // [2][Mpad][2 ntiles] partial squared norms of the outputs (or null)
   const float* wnorm;   // [2][nele][N]
   uint32_t* kmask;      // [2][Mpad][N/32]
   float kappa;
@@ -255,10 +255,12 @@ struct Cfg {
   static constexpr int B_TILE = BN * 128;             // 16 KB (tf32) or 32 KB (bf16)
   static constexpr int STAGE = NSPLIT * (A_TILE + B_TILE);   // 64 KB or 48 KB
   static constexpr int NSTAGE = PREC == TM_PREC_FP32 ? 3 : 4;
-  // epilogue staging per epilogue warp (8 KB): FP32, a 32 x 32 hi and lo box;
-  // BF16, a 32-row x 64-column box (and an FP32 32 x 32 box for dE/dG)
-  static constexpr int EPI_BYTES = 4 * 8192;
+  // epilogue staging per epilogue warp (4 KB): FP32, a 32 x 32 box (hi parts,
+  // then lo parts); BF16, a 32-row x 64-column box (or a 32 x 32 FP32 box for dE/dG)
+  static constexpr int EPI_WB = 4096;
+  static constexpr int EPI_BYTES = 8 * EPI_WB;
   static constexpr int SMEM = NSTAGE * STAGE + EPI_BYTES + 1024 + 256;   // + alignment, barriers
+  static_assert((2 * NSTAGE + 4 + 8) * 8 + 8 <= 256, "barrier block");
   static constexpr uint32_t IDESC = make_idesc(PREC == TM_PREC_FP32 ? 2 : 1, BM, BN);
   // FP32: B hi and lo are adjacent 128-row tiles in a stage, i.e. one 256-row
   // operand, so A_hi [B_hi; B_lo] is a single N = 256 instruction writing the
@@ -270,6 +272,21 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* b) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
 }
 
+// Epilogue warps of one instantiation: eight (two per tensor-memory lane
+// quarter, each with half of the tile's columns), except for the FP32 backward
+// pass, whose four warps bring the previous activation's hi and lo parts in
+// with one bulk tensor load into an 8 KB box each (the same shared memory).
+template <int PREC, int EPI>
+struct EpiShape {
+  static constexpr int WARPS =
+      (PREC == TM_PREC_FP32 && EPI == EPI_BWD && Cfg<PREC>::EPI_BYTES < 8 * 8192) ? 4 : 8;
+  static constexpr int WB = Cfg<PREC>::EPI_BYTES / WARPS;   // staging bytes per warp
+  static constexpr int THREADS = 32 * (WARPS + 2);
+  // FP32: hi and lo boxes side by side (8 KB per warp), else one 4 KB box
+  // that takes the hi parts, then the lo parts
+  static constexpr bool PAIRBOX = PREC == TM_PREC_FP32 && WB >= 8192;
+};
+
 // Persistent, warp-specialised layer kernel. Each CTA walks tiles
 // t = blockIdx.x, blockIdx.x + gridDim.x, ... in (net, m_tile, n_tile) order
 // (n fastest, so the N-tiles of one M-tile run on neighbouring CTAs and share
@@ -277,7 +294,7 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* b) {
 // tile boundaries; the MMA issuer alternates between two 256-column TMEM
 // tile buffers, so the epilogue of tile t overlaps the MMAs of tile t + 1.
 template <int PREC, int EPI, int ACT>
-__global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArgs g) {
+__global__ void __launch_bounds__(EpiShape<PREC, EPI>::THREADS, 1) k_gemm(const __grid_constant__ GemmArgs g) {
   using C = Cfg<PREC>;
   constexpr int BN = C::BN;
   constexpr bool KINK = PREC == TM_PREC_FP32 && ACT == TM_ACT_RELU && (EPI == EPI_FWD || EPI == EPI_FWD_LAST);
@@ -291,8 +308,13 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
   uint64_t* empty = full + C::NSTAGE;
   uint64_t* accf = empty + C::NSTAGE;   // [2] accumulator ready
   uint64_t* acce = accf + 2;            // [2] accumulator drained
-  uint64_t* ebar = acce + 2;            // [4] epilogue loads (one per epilogue warp)
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(ebar + 4);
+  uint64_t* ebar = acce + 2;            // [8] previous-activation loads (FP32 backward),
+                                        // one per epilogue warp
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(ebar + 8);
+  constexpr int EW = EpiShape<PREC, EPI>::WARPS;
+  constexpr bool BOXLOAD = PREC == TM_PREC_FP32 && EPI == EPI_BWD;
+  constexpr bool PAIRBOX = EpiShape<PREC, EPI>::PAIRBOX;
+  static_assert(!BOXLOAD || PAIRBOX, "the FP32 backward pass loads hi and lo boxes together");
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -308,9 +330,9 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&accf[b], 1);
-      mbar_init(&acce[b], 4);   // one arrival per epilogue warp
+      mbar_init(&acce[b], EW);   // one arrival per epilogue warp
     }
-    for (int w = 0; w < 4; ++w) mbar_init(&ebar[w], 1);
+    for (int w = 0; w < 8; ++w) mbar_init(&ebar[w], 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -326,7 +348,7 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (warp == 4) {
+  if (warp == EW) {
     if (lane == 0) {
       int it = 0;
       for (int t = blockIdx.x; t < total && !*abort_flag; t += gridDim.x) {
@@ -355,7 +377,7 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
         }
       }
     }
-  } else if (warp == 5) {
+  } else if (warp == EW + 1) {
     if (lane == 0) {
       int it = 0, lt = 0;
       for (int t = blockIdx.x; t < total && !*abort_flag; t += gridDim.x, ++lt) {
@@ -403,15 +425,21 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
       }
     }
   } else {
-    // ---- epilogue: warps 0..3, thread = accumulator row ----
-    // Each warp stages its 32 rows in shared memory in the TMA 128-byte-swizzle
-    // layout (16-byte piece q of row r at piece q ^ (r & 7): conflict-free for
-    // a row per lane) and writes them with bulk tensor stores: FP32 32 columns
-    // per box (hi and lo parts), BF16 64 columns per box (two 32-column
-    // chunks); the backward pass brings the previous activation in the same way.
-    float* ebh = reinterpret_cast<float*>(smem + C::NSTAGE * C::STAGE + warp * 8192);
-    float* ebl = ebh + 1024;
-    int eph = 0;   // uses of this warp's load barrier
+    // ---- epilogue: warps 0..7, thread = accumulator row ----
+    // Two warps per tensor-memory lane quarter (warp w reads lanes 32 (w % 4)
+    // ...), each taking half of the tile's columns: the epilogue's arithmetic
+    // (activation, split, staging) outweighs the MMAs with one warp per
+    // scheduler. Each warp stages 32 rows x 32 columns in shared memory in the
+    // TMA 128-byte-swizzle layout (16-byte piece q of row r at piece q ^ (r &
+    // 7): conflict-free for a row per lane) and writes them with bulk tensor
+    // stores: FP32 hi then lo parts through one 4 KB box, BF16 64 columns per
+    // box (two 32-column chunks). The backward pass reads the previous
+    // activation of its rows with vector loads.
+    const int quad = warp & 3, half = EW == 8 ? warp >> 2 : 0;
+    constexpr int HALF = EW == 8 ? BN / 2 : BN;   // columns per warp
+    float* ebox = reinterpret_cast<float*>(smem + C::NSTAGE * C::STAGE + warp * EpiShape<PREC, EPI>::WB);
+    float* ebl = ebox + 1024;   // FP32 with 8 KB per warp: the lo box
+    int eph = 0;                // uses of this warp's load barrier
     bool eok = true;
     int lt = 0;
     for (int t = blockIdx.x; t < total && eok; t += gridDim.x, ++lt) {
@@ -425,11 +453,13 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
       const int net = t / per_net, rem = t % per_net;
       const int m_tile = rem / g.ntiles, n_tile = rem % g.ntiles;
       const int elem = g.tile_elem[m_tile];
-      const int row = m_tile * BM + warp * 32 + lane;          // row in this net
+      const int row = m_tile * BM + quad * 32 + lane;          // row in this net
       const size_t orow = (size_t)net * g.Mpad + row;
-      const int orow0 = net * g.Mpad + m_tile * BM + warp * 32;   // first row of this warp
+      const int orow0 = net * g.Mpad + m_tile * BM + quad * 32;   // first row of this warp
       const int pblk = (net * g.nele + elem) * g.N;
-      const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(buf * C::ACC_COLS);
+      const int part = 2 * n_tile + half;                      // this warp's share of the row
+      (void)part;
+      const uint32_t tbase = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * C::ACC_COLS);
       float esum = 0.f;
       // relu refinement: kappa * ||input row|| (flags |z| below it times ||w_unit||)
       float kthr = 0.f, hss = 0.f;
@@ -441,7 +471,7 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
           kthr = g.kappa * sqrtf(ss);
         }
       }
-      for (int c = 0; c < BN && eok; c += 32) {
+      for (int c = half * HALF; c < (half + 1) * HALF && eok; c += 32) {
         const int col = n_tile * BN + c;
         // BF16 (not dE/dG): one 64-column box covers two 32-column chunks
         const bool box_start = PREC == TM_PREC_FP32 || EPI == EPI_OUT || (c & 32) == 0;
@@ -450,37 +480,61 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
           // the staging box is free once the previous stores have read it
           if (lane == 0) bulk_wait_read();
           __syncwarp();
-          if constexpr (EPI == EPI_BWD) {
+          if constexpr (BOXLOAD) {
             if (lane == 0) {
-              if constexpr (PREC == TM_PREC_FP32) {
-                mbar_expect_tx(&ebar[warp], 8192);
-                tma_load_2d(ebh, &g.o0, col, orow0, &ebar[warp]);
-                tma_load_2d(ebl, &g.o1, col, orow0, &ebar[warp]);
-              } else {
-                mbar_expect_tx(&ebar[warp], 4096);
-                tma_load_2d(ebh, &g.o0, col, orow0, &ebar[warp]);
+              mbar_expect_tx(&ebar[warp], 8192);
+              tma_load_2d(ebox, &g.o0, col, orow0, &ebar[warp]);
+              tma_load_2d(ebl, &g.o1, col, orow0, &ebar[warp]);
+            }
+          }
+        }
+        // the previous activation of these 32 columns (backward), then bias
+        // and output weights (same for every row): loads issued before the
+        // tensor-memory reads
+        float h[32];
+        if constexpr (EPI == EPI_BWD && !BOXLOAD) {
+          if constexpr (PREC == TM_PREC_FP32) {
+            const float4* ph = reinterpret_cast<const float4*>(
+                static_cast<const float*>(g.hprev0) + orow * g.ldo + col);
+            const float4* pl = reinterpret_cast<const float4*>(
+                static_cast<const float*>(g.hprev1) + orow * g.ldo + col);
+            float4 a[8], b[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) { a[q] = ph[q]; b[q] = pl[q]; }
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              h[4 * q] = a[q].x + b[q].x;
+              h[4 * q + 1] = a[q].y + b[q].y;
+              h[4 * q + 2] = a[q].z + b[q].z;
+              h[4 * q + 3] = a[q].w + b[q].w;
+            }
+          } else {
+            const uint4* ph = reinterpret_cast<const uint4*>(
+                static_cast<const __nv_bfloat16*>(g.hprev0) + orow * g.ldo + col);
+            uint4 u[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) u[q] = ph[q];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              const uint32_t w[4] = {u[q].x, u[q].y, u[q].z, u[q].w};
+#pragma unroll
+              for (int e = 0; e < 4; ++e) {
+                const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w[e]));
+                h[8 * q + 2 * e] = f.x;
+                h[8 * q + 2 * e + 1] = f.y;
               }
             }
           }
         }
-        // bias and output weights of these 32 columns (same for every row):
-        // vector loads issued before the tensor-memory reads
-        float bq[32], wq[32];
-        if (EPI == EPI_FWD || EPI == EPI_FWD_LAST) {
-          const float4* b4 = reinterpret_cast<const float4*>(g.bias + pblk + col);
-#pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            const float4 u = __ldg(b4 + q);
-            bq[4 * q] = u.x; bq[4 * q + 1] = u.y; bq[4 * q + 2] = u.z; bq[4 * q + 3] = u.w;
-          }
-        }
-        if (EPI == EPI_FWD_LAST) {
-          const float4* w4 = reinterpret_cast<const float4*>(g.wout + pblk + col);
-#pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            const float4 u = __ldg(w4 + q);
-            wq[4 * q] = u.x; wq[4 * q + 1] = u.y; wq[4 * q + 2] = u.z; wq[4 * q + 3] = u.w;
-          }
+        // bias, output weight and (relu refinement) unit norm of these 32
+        // columns, the same for every row: lane q holds column q's values and
+        // the loop takes them by shuffle (one coalesced load each, issued
+        // before the tensor-memory reads; 32-float register copies spill)
+        float b_l = 0.f, w_l = 0.f, wn_l = 0.f;
+        if (EPI == EPI_FWD || EPI == EPI_FWD_LAST) b_l = __ldg(g.bias + pblk + col + lane);
+        if (EPI == EPI_FWD_LAST) w_l = __ldg(g.wout + pblk + col + lane);
+        if constexpr (KINK) {
+          if (g.kmask) wn_l = __ldg(g.wnorm + pblk + col + lane);
         }
         uint32_t r[32];
         tmem_ld32(tbase + (uint32_t)c, r);
@@ -496,35 +550,33 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
           uint32_t km = 0;
 #pragma unroll
           for (int q = 0; q < 32; ++q) {
-            const float z = __uint_as_float(r[q]) + bq[q];
+            const float z = __uint_as_float(r[q]) + __shfl_sync(TM_FULL, b_l, q);
             if constexpr (KINK) {
-              if (fabsf(z) < kthr * __ldg(g.wnorm + pblk + col + q)) km |= 1u << q;
+              if (fabsf(z) < kthr * __shfl_sync(TM_FULL, wn_l, q)) km |= 1u << q;
             }
-            float h, dz;
-            act_fwd<ACT>(z, g.alpha, h, dz);
+            float hz, dz;
+            act_fwd<ACT>(z, g.alpha, hz, dz);
             if (EPI == EPI_FWD) {
-              v[q] = h;
+              v[q] = hz;
               if constexpr (KINK) hss = fmaf(v[q], v[q], hss);
             } else {
-              esum += h * wq[q];
-              v[q] = wq[q] * dz;
+              const float wq = __shfl_sync(TM_FULL, w_l, q);
+              esum += hz * wq;
+              v[q] = wq * dz;
             }
           }
           if constexpr (KINK) {
             if (g.kmask) g.kmask[((size_t)net * g.Mpad + row) * (g.N >> 5) + (col >> 5)] = km;
           }
         } else if (EPI == EPI_BWD) {
-          float h[32];
-          if (box_start) {
+          if constexpr (BOXLOAD) {
             if (!mbar_wait(&ebar[warp], eph & 1, wlim)) {
               tm_flag(g.st, TM_E_TIMEOUT, t, 104);
               *abort_flag = 1;
               eok = false;
             }
             ++eph;
-          }
-          if constexpr (PREC == TM_PREC_FP32) {
-            const float4* sh = reinterpret_cast<const float4*>(ebh) + lane * 8;
+            const float4* sh = reinterpret_cast<const float4*>(ebox) + lane * 8;
             const float4* sl = reinterpret_cast<const float4*>(ebl) + lane * 8;
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
@@ -534,21 +586,7 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
               h[4 * q + 2] = a.z + b.z;
               h[4 * q + 3] = a.w + b.w;
             }
-          } else {
-            // bf16 box: 16-byte piece p (8 values) of row r at p ^ (r & 7)
-            const uint4* sh = reinterpret_cast<const uint4*>(ebh) + lane * 8;
-            const int p0 = (c & 32) ? 4 : 0;
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              const uint4 u = sh[(p0 + q) ^ (lane & 7)];
-              const uint32_t w[4] = {u.x, u.y, u.z, u.w};
-#pragma unroll
-              for (int e = 0; e < 4; ++e) {
-                const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w[e]));
-                h[8 * q + 2 * e] = f.x;
-                h[8 * q + 2 * e + 1] = f.y;
-              }
-            }
+            __syncwarp();   // every lane has read the boxes before they take the outputs
           }
 #pragma unroll
           for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]) * actd_h<ACT>(h[q], g.alpha);
@@ -556,51 +594,81 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
 #pragma unroll
           for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]);
         }
+        float4* dh = reinterpret_cast<float4*>(ebox) + lane * 8;
         if constexpr (PREC == TM_PREC_FP32) {
-          float4* dh = reinterpret_cast<float4*>(ebh) + lane * 8;
-          float4* dl = reinterpret_cast<float4*>(ebl) + lane * 8;
+          if constexpr (EPI == EPI_OUT) {   // one FP32 output
 #pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            float4 hh, ll;
-            if (EPI == EPI_OUT) {   // one FP32 output
-              hh = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-            } else {
+            for (int q = 0; q < 8; ++q)
+              dh[q ^ (lane & 7)] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+          } else if constexpr (PAIRBOX) {   // hi and lo boxes side by side
+            float4* dl = reinterpret_cast<float4*>(ebl) + lane * 8;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              float4 hh, ll;
               tm_tf32_split(v[4 * q], hh.x, ll.x);
               tm_tf32_split(v[4 * q + 1], hh.y, ll.y);
               tm_tf32_split(v[4 * q + 2], hh.z, ll.z);
               tm_tf32_split(v[4 * q + 3], hh.w, ll.w);
+              dh[q ^ (lane & 7)] = hh;
               dl[q ^ (lane & 7)] = ll;
             }
-            dh[q ^ (lane & 7)] = hh;
+          } else {                          // hi parts now, lo parts after them
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              float4 hh;
+              hh.x = tm_tf32_rn(v[4 * q]);
+              hh.y = tm_tf32_rn(v[4 * q + 1]);
+              hh.z = tm_tf32_rn(v[4 * q + 2]);
+              hh.w = tm_tf32_rn(v[4 * q + 3]);
+              dh[q ^ (lane & 7)] = hh;
+            }
           }
           fence_async_smem();
           __syncwarp();
           if (lane == 0) {
-            tma_store_2d(&g.o0, col, orow0, ebh);
-            if (EPI != EPI_OUT) tma_store_2d(&g.o1, col, orow0, ebl);
+            tma_store_2d(&g.o0, col, orow0, ebox);
+            if (PAIRBOX && EPI != EPI_OUT) tma_store_2d(&g.o1, col, orow0, ebl);
             bulk_commit();
+          }
+          if constexpr (EPI != EPI_OUT && !PAIRBOX) {
+            if (lane == 0) bulk_wait_read();
+            __syncwarp();
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              float4 ll;
+              ll.x = tm_tf32_rn(v[4 * q] - tm_tf32_rn(v[4 * q]));
+              ll.y = tm_tf32_rn(v[4 * q + 1] - tm_tf32_rn(v[4 * q + 1]));
+              ll.z = tm_tf32_rn(v[4 * q + 2] - tm_tf32_rn(v[4 * q + 2]));
+              ll.w = tm_tf32_rn(v[4 * q + 3] - tm_tf32_rn(v[4 * q + 3]));
+              dh[q ^ (lane & 7)] = ll;
+            }
+            fence_async_smem();
+            __syncwarp();
+            if (lane == 0) {
+              tma_store_2d(&g.o1, col, orow0, ebox);
+              bulk_commit();
+            }
           }
         } else if (EPI == EPI_OUT) {
           // FP32 dE/dG through a 32 x 32 FP32 box
-          float4* dh = reinterpret_cast<float4*>(ebh) + lane * 8;
 #pragma unroll
           for (int q = 0; q < 8; ++q)
             dh[q ^ (lane & 7)] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
           fence_async_smem();
           __syncwarp();
           if (lane == 0) {
-            tma_store_2d(&g.o0, col, orow0, ebh);   // the FP32 map of dE/dG
+            tma_store_2d(&g.o0, col, orow0, ebox);   // the FP32 map of dE/dG
             bulk_commit();
           }
         } else {
-          uint4* dh = reinterpret_cast<uint4*>(ebh) + lane * 8;
+          uint4* db = reinterpret_cast<uint4*>(ebox) + lane * 8;
           const int p0 = (c & 32) ? 4 : 0;
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
             __nv_bfloat162 b[4];
 #pragma unroll
             for (int e = 0; e < 4; ++e) b[e] = __floats2bfloat162_rn(v[8 * q + 2 * e], v[8 * q + 2 * e + 1]);
-            dh[(p0 + q) ^ (lane & 7)] =
+            db[(p0 + q) ^ (lane & 7)] =
                 make_uint4(*reinterpret_cast<uint32_t*>(&b[0]), *reinterpret_cast<uint32_t*>(&b[1]),
                            *reinterpret_cast<uint32_t*>(&b[2]), *reinterpret_cast<uint32_t*>(&b[3]));
           }
@@ -608,17 +676,17 @@ __global__ void __launch_bounds__(192, 1) k_gemm(const __grid_constant__ GemmArg
             fence_async_smem();
             __syncwarp();
             if (lane == 0) {
-              tma_store_2d(&g.o0, col - 32, orow0, ebh);
+              tma_store_2d(&g.o0, col - 32, orow0, ebox);
               bulk_commit();
             }
           }
         }
       }
-      if (EPI == EPI_FWD_LAST) g.epart[orow * (g.N / BN) + n_tile] = esum;
+      if (EPI == EPI_FWD_LAST) g.epart[orow * (2 * g.ntiles) + part] = esum;
       if constexpr (KINK && EPI == EPI_FWD) {
-        if (g.hn2_out) g.hn2_out[orow * g.ntiles + n_tile] = hss;
+        if (g.hn2_out) g.hn2_out[orow * (2 * g.ntiles) + part] = hss;
       }
-      // this warp has read its 32 lanes of the accumulator: hand it back
+      // this warp has read its lanes and columns of the accumulator: hand them back
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&acce[buf]);
@@ -652,7 +720,7 @@ int launch_gemm(tm_ctx* ctx, const GemmArgs& g0, int mtiles) {
   g.ntiles = ntiles;
   const int total = 2 * mtiles * ntiles;
   const int grid = total < ctx->num_sms ? total : ctx->num_sms;
-  k_gemm<PREC, EPI, ACT><<<grid, 192, C::SMEM, ctx->stream>>>(g);
+  k_gemm<PREC, EPI, ACT><<<grid, EpiShape<PREC, EPI>::THREADS, C::SMEM, ctx->stream>>>(g);
   ctx->launches++;
   return tm_cuda_check(ctx, cudaGetLastError(), "gemm");
 }
@@ -827,6 +895,10 @@ int tm_gemm_bn(int prec) {
   return prec == TM_PREC_FP32 ? Cfg<TM_PREC_FP32>::BN : Cfg<TM_PREC_BF16>::BN;
 }
 
+// partial row sums a layer launch writes per row (energy, squared norms): one
+// per N tile and column half
+int tm_gemm_row_parts(int prec, int H) { return 2 * (H / tm_gemm_bn(prec)); }
+
 int tm_make_tmap(tm_ctx* ctx, CUtensorMap* map, void* base, int elem_bytes, uint64_t rows,
                  uint64_t cols, uint32_t box_rows) {
   if (!ctx->encode) return tm_fail(ctx, TM_E_CUDA, "cuTensorMapEncodeTiled unavailable");
@@ -896,7 +968,7 @@ static int mlp_layers(tm_system* s, bool forward, bool backward, cudaEvent_t* ev
   g.st = ctx->d_status;
   g.skip_it = -1;
   const bool kink = m->kink && s->kink_mask;
-  const int nparts = H / tm_gemm_bn(prec);
+  const int nparts = tm_gemm_row_parts(prec, H);
   if (forward && kink && s->kink_count)
     cudaMemsetAsync(s->kink_count, 0, sizeof(unsigned long long), ctx->stream);
   for (int l = 0; forward && l < L; ++l) {

@@ -212,12 +212,12 @@ struct tm_system {
   void* H2[2] = {};
   void* G3[2] = {};
   float* dEdG = nullptr;               // [2*Mpad][Dp]
-  float* epart = nullptr;              // [2][Mpad][H/tm_gemm_bn(precision)]
+  float* epart = nullptr;              // [2][Mpad][tm_gemm_row_parts(precision, H)]
   // relu refinement (tm_model::kink): squared row norms of each layer's input
   // (the bound of the tensor-core error), flags of the units to recompute and
   // the number recomputed by the last evaluation
   float* kink_g2 = nullptr;            // [Mpad] descriptor rows
-  float* kink_h2[2] = {};              // [2][Mpad][H/BN] per-N-tile partial sums, two
+  float* kink_h2[2] = {};              // [2][Mpad][row parts] partial sums, two
                                        //   buffers alternating between layers
   uint32_t* kink_mask = nullptr;       // [2][Mpad][H/32]
   unsigned long long* kink_count = nullptr;
@@ -280,6 +280,7 @@ int tm_launch_mlp(tm_system* s, bool backward);
 int tm_launch_mlp_backward_only(tm_system* s);
 int tm_profile_layers(tm_system* s, float* ms);   // [2 * nlayer] ms
 int tm_gemm_bn(int prec);   // GEMM N tile of a precision mode (128 or 256)
+int tm_gemm_row_parts(int prec, int H);   // partial sums per row of one layer launch
 float tm_kink_kappa(int K); // relu refinement: flag bound per unit of ||a|| ||w||
 int tm_gemm_selftest(tm_ctx* ctx, int prec, int M, int N, int K, const float* A,
                      const float* B, float* C, long long wait_limit = 0, int skip_it = -1);
