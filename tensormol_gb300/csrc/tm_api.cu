@@ -768,6 +768,8 @@ static int system_alloc(tm_system* s, int N_cap, int nmol_cap, int Mpad_cap, int
     A.get(&s->kink_h2[1], sizeof(float) * 2 * Mp * parts);
     A.get(&s->kink_mask, sizeof(uint32_t) * 2 * Mp * (H / 32));
     A.get(&s->kink_count, sizeof(unsigned long long));
+    A.get(&s->kink_rows, sizeof(uint32_t) * 2 * Mp * parts);
+    A.get(&s->kink_nrows, sizeof(uint32_t) * TM_KINK_LAYERS);
   }
   A.get(&s->d_Eatom, sizeof(double) * N);
   A.get(&s->d_qraw, sizeof(float) * N);
@@ -956,7 +958,7 @@ static void system_free(tm_system* s) {
                   s->d_cnt_a, s->d_nbr_r, s->d_nbr_a, s->d_rev_r, s->d_rev_a, s->d_sr, s->d_va,
                   s->dEdG, s->epart, s->d_Eatom, s->d_qraw, s->d_q, s->d_dEdq, s->d_fself,
                   s->d_fcv, s->d_ecv, s->d_F, s->d_mol_E, s->d_mol_aux, s->d_xuser, s->kink_g2, s->kink_h2[0],
-                  s->kink_h2[1], s->kink_mask, s->kink_count};
+                  s->kink_h2[1], s->kink_mask, s->kink_count, s->kink_rows, s->kink_nrows};
   for (void* p : ptrs)
     if (p) cudaFreeAsync(p, ctx->stream);
   for (int h = 0; h < 2; ++h) {

@@ -71,6 +71,8 @@ struct GemmArgs {
   float* hn2_out;       // [2][Mpad][2 ntiles] partial squared norms of the outputs (or null)
   const float* wnorm;   // [2][nele][N]
   uint32_t* kmask;      // [2][Mpad][N/32]
+  uint32_t* krows;      // entries orow * parts + part with a flagged unit, appended
+  uint32_t* knrows;     // number of entries (zeroed before the launch)
   float kappa;
   // diagnostics of the bounded waits (tm_selftest_gemm_timeout): the wait
   // limit in SM cycles (0: 2^28) and a producer iteration whose operand
@@ -463,6 +465,7 @@ __global__ void __launch_bounds__(EpiShape<PREC, EPI>::THREADS, 1) k_gemm(const 
       float esum = 0.f;
       // relu refinement: kappa * ||input row|| (flags |z| below it times ||w_unit||)
       float kthr = 0.f, hss = 0.f;
+      uint32_t kany = 0;   // flags of this thread's row in this warp's columns
       if constexpr (KINK) {
         if (g.kmask) {
           const float* pa = g.an2 + (size_t)net * g.an2_net_stride + (size_t)row * g.an2_parts;
@@ -567,6 +570,7 @@ __global__ void __launch_bounds__(EpiShape<PREC, EPI>::THREADS, 1) k_gemm(const 
           }
           if constexpr (KINK) {
             if (g.kmask) g.kmask[((size_t)net * g.Mpad + row) * (g.N >> 5) + (col >> 5)] = km;
+            kany |= km;
           }
         } else if (EPI == EPI_BWD) {
           if constexpr (BOXLOAD) {
@@ -683,6 +687,17 @@ __global__ void __launch_bounds__(EpiShape<PREC, EPI>::THREADS, 1) k_gemm(const 
         }
       }
       if (EPI == EPI_FWD_LAST) g.epart[orow * (2 * g.ntiles) + part] = esum;
+      if constexpr (KINK) {
+        // (row, column part) entries with flagged units, for the refinement:
+        // one atomic per warp
+        const uint32_t bal = __ballot_sync(TM_FULL, kany != 0u);
+        if (bal && g.kmask) {
+          uint32_t base = 0;
+          if (lane == 0) base = atomicAdd(g.knrows, (uint32_t)__popc(bal));
+          base = __shfl_sync(TM_FULL, base, 0);
+          if (kany) g.krows[base + __popc(bal & ((1u << lane) - 1u))] = (uint32_t)(orow * (2 * g.ntiles) + part);
+        }
+      }
       if constexpr (KINK && EPI == EPI_FWD) {
         if (g.hn2_out) g.hn2_out[orow * (2 * g.ntiles) + part] = hss;
       }
@@ -776,40 +791,44 @@ struct KinkArgs {
   const float* wout;      // [2][nele][N]
   const int32_t* tile_elem;
   const uint32_t* kmask;  // [2][Mpad][N/32]
+  const uint32_t* rows;   // entries orow * parts + part (appended by the layer kernel)
+  const uint32_t* nrows;
+  int parts, part_cols;   // column parts per row and their width
   float* o_hi;
   float* o_lo;            // [2*Mpad][N]
   int N, Mpad, nele;
   unsigned long long* count;
 };
 
-// One warp per (net, row). A row with flagged units reads its input once
-// into registers (KPL values per lane, all loads in flight together); each
-// flagged unit then streams its weight vector with independent loads.
+// Persistent warps over the entries (row, column part) that the layer kernel
+// flagged. An entry reads its row's input once into registers (KPL values per
+// lane, all loads in flight together); each flagged unit of the part then
+// streams its weight vector with independent loads.
 template <bool LAST, int KPL>
 __global__ void __launch_bounds__(256) k_kink_refine(const KinkArgs a) {
-  const int wg = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
-  if (wg >= 2 * a.Mpad) return;
-  const int net = wg / a.Mpad, r = wg - net * a.Mpad;
-  const int nw = a.N >> 5;
-  const uint32_t* mk = a.kmask + (size_t)wg * nw;
-  const uint32_t first = lane < nw ? mk[lane] : 0u;
-  if (nw <= 32 && !__any_sync(TM_FULL, first != 0u)) return;
-  const int elem = a.tile_elem[r / BM];
-  const size_t blk = (size_t)net * a.nele + elem;
-  const size_t arow = (size_t)net * a.a_net_rows + r;
-  const float* ah = a.a_hi + arow * a.K + lane;
-  const float* al = a.a_lo + arow * a.K + lane;
-  constexpr int KR = KPL > 0 ? KPL : 1;
-  float xh[KR], xl[KR];
-#pragma unroll
-  for (int q = 0; q < KPL; ++q) {
-    xh[q] = ah[q * 32];
-    xl[q] = al[q * 32];
-  }
+  const int nwarps = (int)((gridDim.x * (size_t)blockDim.x) >> 5);
+  const int n = (int)*a.nrows;
   int nref = 0;
-  for (int w0 = 0; w0 < nw; w0 += 32) {
-    const uint32_t mine = w0 == 0 ? first : (w0 + lane < nw ? mk[w0 + lane] : 0u);
+  for (int e = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5); e < n; e += nwarps) {
+    const uint32_t ent = a.rows[e];
+    const int orow = (int)(ent / (uint32_t)a.parts), part = (int)(ent % (uint32_t)a.parts);
+    const int net = orow / a.Mpad, r = orow - net * a.Mpad;
+    const int c0 = part * a.part_cols;
+    const uint32_t* mk = a.kmask + (size_t)orow * (a.N >> 5) + (c0 >> 5);
+    const uint32_t mine = lane < (a.part_cols >> 5) ? mk[lane] : 0u;   // one flag word per lane
+    const int elem = a.tile_elem[r / BM];
+    const size_t blk = (size_t)net * a.nele + elem;
+    const size_t arow = (size_t)net * a.a_net_rows + r;
+    const float* ah = a.a_hi + arow * a.K + lane;
+    const float* al = a.a_lo + arow * a.K + lane;
+    constexpr int KR = KPL > 0 ? KPL : 1;
+    float xh[KR], xl[KR];
+#pragma unroll
+    for (int q = 0; q < KPL; ++q) {
+      xh[q] = ah[q * 32];
+      xl[q] = al[q * 32];
+    }
     uint32_t any = __ballot_sync(TM_FULL, mine != 0u);
     while (any) {
       const int src = __ffs(any) - 1;
@@ -818,7 +837,7 @@ __global__ void __launch_bounds__(256) k_kink_refine(const KinkArgs a) {
       while (bits) {
         const int b = __ffs(bits) - 1;
         bits &= bits - 1;
-        const int col = (w0 + src) * 32 + b;
+        const int col = c0 + src * 32 + b;
         const float2* wr = a.w2 + (blk * a.N + col) * a.K + lane;
         float sh = 0.f, sl = 0.f;
         if constexpr (KPL > 0) {
@@ -827,20 +846,20 @@ __global__ void __launch_bounds__(256) k_kink_refine(const KinkArgs a) {
           for (int q = 0; q < KPL; ++q) wv[q] = __ldg(wr + q * 32);
 #pragma unroll
           for (int q = 0; q < KPL; ++q) {
-            float p, e, t;
-            tm_two_prod(xh[q], wv[q].x, p, e);
+            float p, e2, t;
+            tm_two_prod(xh[q], wv[q].x, p, e2);
             tm_two_sum(sh, p, sh, t);
-            sl += (t + e) + fmaf(xh[q], wv[q].y, xl[q] * wv[q].x);
+            sl += (t + e2) + fmaf(xh[q], wv[q].y, xl[q] * wv[q].x);
           }
         } else {   // any K that is a multiple of 32: the input streamed as well
 #pragma unroll 8
           for (int q = 0; q < a.K / 32; ++q) {
             const float2 wq = __ldg(wr + q * 32);
             const float x = ah[q * 32], xq = al[q * 32];
-            float p, e, t;
-            tm_two_prod(x, wq.x, p, e);
+            float p, e2, t;
+            tm_two_prod(x, wq.x, p, e2);
             tm_two_sum(sh, p, sh, t);
-            sl += (t + e) + fmaf(x, wq.y, xq * wq.x);
+            sl += (t + e2) + fmaf(x, wq.y, xq * wq.x);
           }
         }
 #pragma unroll
@@ -872,7 +891,7 @@ __global__ void __launch_bounds__(256) k_kink_refine(const KinkArgs a) {
 
 template <bool LAST>
 int launch_kink_refine(tm_ctx* ctx, const KinkArgs& ka) {
-  const int blocks = tm_div_up(2 * ka.Mpad * 32, 256);
+  const int blocks = 4 * ctx->num_sms;   // persistent: a few thousand entries per layer
   switch (ka.K / 32) {
     case 8: k_kink_refine<LAST, 8><<<blocks, 256, 0, ctx->stream>>>(ka); break;
     case 16: k_kink_refine<LAST, 16><<<blocks, 256, 0, ctx->stream>>>(ka); break;
@@ -969,8 +988,10 @@ static int mlp_layers(tm_system* s, bool forward, bool backward, cudaEvent_t* ev
   g.skip_it = -1;
   const bool kink = m->kink && s->kink_mask;
   const int nparts = tm_gemm_row_parts(prec, H);
-  if (forward && kink && s->kink_count)
+  if (forward && kink && s->kink_count) {
     cudaMemsetAsync(s->kink_count, 0, sizeof(unsigned long long), ctx->stream);
+    cudaMemsetAsync(s->kink_nrows, 0, sizeof(uint32_t) * TM_KINK_LAYERS, ctx->stream);
+  }
   for (int l = 0; forward && l < L; ++l) {
     const bool last = (l == L - 1);
     const CUtensorMap* const* A = l == 0 ? lv0 : lvH[l - 1];
@@ -997,6 +1018,8 @@ static int mlp_layers(tm_system* s, bool forward, bool backward, cudaEvent_t* ev
       g.an2_parts = l == 0 ? 1 : nparts;
       g.an2_net_stride = l == 0 ? 0 : s->Mpad * nparts;
       g.hn2_out = last ? nullptr : s->kink_h2[l & 1];
+      g.krows = s->kink_rows;
+      g.knrows = s->kink_nrows + l;
     }
     if (ev) cudaEventRecord(ev[2 * l], ctx->stream);
     if ((rc = dispatch(ctx, prec, last ? EPI_FWD_LAST : EPI_FWD, g, mt))) return rc;
@@ -1018,6 +1041,10 @@ static int mlp_layers(tm_system* s, bool forward, bool backward, cudaEvent_t* ev
       ka.Mpad = s->Mpad;
       ka.nele = m->k.nele;
       ka.count = s->kink_count;
+      ka.rows = s->kink_rows;
+      ka.nrows = s->kink_nrows + l;
+      ka.parts = nparts;
+      ka.part_cols = H / nparts;
       if ((rc = last ? launch_kink_refine<true>(ctx, ka) : launch_kink_refine<false>(ctx, ka))) return rc;
     }
   }

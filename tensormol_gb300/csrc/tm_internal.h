@@ -14,6 +14,7 @@
 #define TM_MAX_ELE 8
 #define TM_MAX_HIDDEN 4
 #define TM_BN 256          // padding of the hidden width H and descriptor width Dp
+#define TM_KINK_LAYERS 8   // entry counters of the relu refinement (one per forward layer)
 #define TM_BM 128          // GEMM M tile (rows per element are padded to this)
 #define TM_EE_SPLIT 25     // warps sharing one centre block's half stencil (one
                            // (x, y) column each at a 3-cell reach)
@@ -220,6 +221,8 @@ struct tm_system {
   float* kink_h2[2] = {};              // [2][Mpad][row parts] partial sums, two
                                        //   buffers alternating between layers
   uint32_t* kink_mask = nullptr;       // [2][Mpad][H/32]
+  uint32_t* kink_rows = nullptr;       // [2][Mpad][row parts] (row, part) entries with flags
+  uint32_t* kink_nrows = nullptr;      // [TM_KINK_LAYERS] entries per forward layer
   unsigned long long* kink_count = nullptr;
   CUtensorMap tm_G[2], tm_H1[2], tm_H2[2], tm_G3[2];
   // 32-row boxes of the layer outputs for the GEMM epilogue's TMA stores (and
