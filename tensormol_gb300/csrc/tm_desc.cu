@@ -262,6 +262,15 @@ __device__ __forceinline__ void pair_advance(int& pa, int& pb, int na_, bool tri
     while (pa >= na_ && na_ > 0) { pa -= na_; ++pb; }
   }
 }
+// the same by `step` pairs
+__device__ __forceinline__ void pair_advance_by(int& pa, int& pb, int na_, bool tri, int step) {
+  pa += step;
+  if (tri) {
+    while (pa >= pb && pb > 0) { pa -= pb; ++pb; }
+  } else {
+    while (pa >= na_ && na_ > 0) { pa -= na_; ++pb; }
+  }
+}
 __device__ __forceinline__ void pair_start(int t, int& pa, int& pb, int na_, bool tri) {
   if (tri) {
     int b = 1, acc = 0;
@@ -353,16 +362,18 @@ __global__ void __launch_bounds__(128) k_desc_fwd(const DescArgs a, const tm_con
       float acc[8];
 #pragma unroll
       for (int n = 0; n < 8; ++n) acc[n] = 0.f;
-      int pa, pb;
-      pair_start(grp, pa, pb, na_, tri);
-      // two triples per group per iteration (independent chains for latency)
-      for (int tb = 0; tb < npair; tb += 8) {
-        float AF[2], B[2];
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          AF[h] = 0.f;
-          B[h] = 0.f;
-          if (ACC && tb + 4 * h + grp < npair) {
+      if constexpr (ACC) {
+        // The double-single quantities of a triple that do not depend on the
+        // angle bin or shell (cos and sin of the angle, the cutoff factors,
+        // the mean distance) are computed once, by one lane per triple for 32
+        // triples a round; each group of 8 lanes then takes its triples' values
+        // by shuffle (the same triples in the same order as below, so the
+        // rows are the same bit for bit).
+        int pa, pb;
+        pair_start(lane, pa, pb, na_, tri);
+        for (int tb = 0; tb < npair; tb += 32) {
+          float tch = 0.f, tcl = 0.f, tsh = 0.f, tsl = 0.f, tfa = 0.f, tfb = 0.f, trh = 0.f, trl = 0.f;
+          if (tb + lane < npair) {
             const int sa = seg[ea] + pa, sb = seg[eb] + pb;
             // c = u_a . u_b and s = sqrt((1 - c)(1 + c)) in double-single (c is
             // accurate to ~2^-44, so s is accurate even for nearly collinear triples)
@@ -376,7 +387,7 @@ __global__ void __launch_bounds__(128) k_desc_fwd(const DescArgs a, const tm_con
             tm_two_sum(ch, p, ch, t);
             cl += t + e + fmaf(w.uz[sa], w.vz[sb], w.vz[sa] * w.uz[sb]);
             tm_fast_two_sum(ch, cl, ch, cl);
-            float mh, ml, ph, pl, qh, ql, sh, sl;
+            float mh, ml, ph, pl, qh, ql;
             tm_two_sum(1.f, -ch, mh, ml);
             ml -= cl;
             tm_two_sum(1.f, ch, ph, pl);
@@ -384,44 +395,85 @@ __global__ void __launch_bounds__(128) k_desc_fwd(const DescArgs a, const tm_con
             tm_two_prod(mh, ph, qh, ql);
             ql += fmaf(mh, pl, ml * ph);
             tm_fast_two_sum(qh, ql, qh, ql);
-            tm_ds_sqrt(qh, ql, sh, sl);
-            float pw;
-            if (k.zeta_pow2) {
-              pw = pow8_ds(ch, cl, sh, sl, cth, cth_lo, sth, sth_lo);
-            } else {
-              float dp;
-              powz(fmaxf(0.f, 1.f + (ch * cth + sh * sth)), k, pw, dp);
-            }
-            AF[h] = k.two_1mz * pw * w.fc[sa] * w.fc[sb];
-            // (r_a + r_b) / 2 - Rs in double-single
-            float rh, rl2;
-            tm_two_sum(w.r[sa], w.r[sb], rh, rl2);
-            rl2 += w.fcd[sa] + w.fcd[sb];
-            const float u = __fadd_rn(__fsub_rn(0.5f * rh, rsq), __fsub_rn(0.5f * rl2, rsq_lo));
-            B[h] = expf(-k.eta * u * u);
-          } else if (!ACC && tb + 4 * h + grp < npair) {
-            const int sa = seg[ea] + pa, sb = seg[eb] + pb;
-            const float c = w.ux[sa] * w.ux[sb] + w.uy[sa] * w.uy[sb] + w.uz[sa] * w.uz[sb];
-            // sin(theta) = |u_a x u_b|: well conditioned for nearly collinear triples,
-            // where sqrt(1 - c^2) loses most of its digits in FP32
-            const float nx = w.uy[sa] * w.uz[sb] - w.uz[sa] * w.uy[sb];
-            const float ny = w.uz[sa] * w.ux[sb] - w.ux[sa] * w.uz[sb];
-            const float nz = w.ux[sa] * w.uy[sb] - w.uy[sa] * w.ux[sb];
-            const float sn = sqrtf(nx * nx + ny * ny + nz * nz);
-            const float T = c * cth + sn * sth;
-            float p, dp;
-            powz(fmaxf(0.f, 1.f + T), k, p, dp);
-            AF[h] = k.two_1mz * p * w.fc[sa] * w.fc[sb];
-            const float u = 0.5f * (w.r[sa] + w.r[sb]) - rsq;
-            B[h] = expf(-k.eta * u * u);
+            tm_ds_sqrt(qh, ql, tsh, tsl);
+            tch = ch;
+            tcl = cl;
+            tfa = w.fc[sa];
+            tfb = w.fc[sb];
+            // r_a + r_b in double-single
+            tm_two_sum(w.r[sa], w.r[sb], trh, trl);
+            trl += w.fcd[sa] + w.fcd[sb];
           }
-          pair_advance(pa, pb, na_, tri);
-        }
+          pair_advance_by(pa, pb, na_, tri, 32);
+          const int nt = min(32, npair - tb);
+          for (int j0 = 0; j0 < nt; j0 += 8) {
+            float AF[2], B[2];
 #pragma unroll
-        for (int n = 0; n < 8; ++n) {
-          const float B0 = __shfl_sync(TM_FULL, B[0], (lane & ~7) | n);
-          const float B1 = __shfl_sync(TM_FULL, B[1], (lane & ~7) | n);
-          acc[n] += AF[0] * B0 + AF[1] * B1;
+            for (int h = 0; h < 2; ++h) {
+              const int src = j0 + 4 * h + grp;
+              const float ch = __shfl_sync(TM_FULL, tch, src), cl = __shfl_sync(TM_FULL, tcl, src);
+              const float sh = __shfl_sync(TM_FULL, tsh, src), sl = __shfl_sync(TM_FULL, tsl, src);
+              const float fa = __shfl_sync(TM_FULL, tfa, src), fb = __shfl_sync(TM_FULL, tfb, src);
+              const float rh = __shfl_sync(TM_FULL, trh, src), rl2 = __shfl_sync(TM_FULL, trl, src);
+              AF[h] = 0.f;
+              B[h] = 0.f;
+              if (src < nt) {
+                float pw;
+                if (k.zeta_pow2) {
+                  pw = pow8_ds(ch, cl, sh, sl, cth, cth_lo, sth, sth_lo);
+                } else {
+                  float dp;
+                  powz(fmaxf(0.f, 1.f + (ch * cth + sh * sth)), k, pw, dp);
+                }
+                AF[h] = k.two_1mz * pw * fa * fb;
+                // (r_a + r_b) / 2 - Rs in double-single
+                const float u = __fadd_rn(__fsub_rn(0.5f * rh, rsq), __fsub_rn(0.5f * rl2, rsq_lo));
+                B[h] = expf(-k.eta * u * u);
+              }
+            }
+#pragma unroll
+            for (int n = 0; n < 8; ++n) {
+              const float B0 = __shfl_sync(TM_FULL, B[0], (lane & ~7) | n);
+              const float B1 = __shfl_sync(TM_FULL, B[1], (lane & ~7) | n);
+              acc[n] += AF[0] * B0 + AF[1] * B1;
+            }
+          }
+        }
+      } else {
+        int pa, pb;
+        pair_start(grp, pa, pb, na_, tri);
+        // FP32 form: two triples per group per iteration (independent chains
+        // for latency)
+        for (int tb = 0; tb < npair; tb += 8) {
+          float AF[2], B[2];
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            AF[h] = 0.f;
+            B[h] = 0.f;
+            if (tb + 4 * h + grp < npair) {
+              const int sa = seg[ea] + pa, sb = seg[eb] + pb;
+              const float c = w.ux[sa] * w.ux[sb] + w.uy[sa] * w.uy[sb] + w.uz[sa] * w.uz[sb];
+              // sin(theta) = |u_a x u_b|: well conditioned for nearly collinear triples,
+              // where sqrt(1 - c^2) loses most of its digits in FP32
+              const float nx = w.uy[sa] * w.uz[sb] - w.uz[sa] * w.uy[sb];
+              const float ny = w.uz[sa] * w.ux[sb] - w.ux[sa] * w.uz[sb];
+              const float nz = w.ux[sa] * w.uy[sb] - w.uy[sa] * w.ux[sb];
+              const float sn = sqrtf(nx * nx + ny * ny + nz * nz);
+              const float T = c * cth + sn * sth;
+              float p, dp;
+              powz(fmaxf(0.f, 1.f + T), k, p, dp);
+              AF[h] = k.two_1mz * p * w.fc[sa] * w.fc[sb];
+              const float u = 0.5f * (w.r[sa] + w.r[sb]) - rsq;
+              B[h] = expf(-k.eta * u * u);
+            }
+            pair_advance(pa, pb, na_, tri);
+          }
+#pragma unroll
+          for (int n = 0; n < 8; ++n) {
+            const float B0 = __shfl_sync(TM_FULL, B[0], (lane & ~7) | n);
+            const float B1 = __shfl_sync(TM_FULL, B[1], (lane & ~7) | n);
+            acc[n] += AF[0] * B0 + AF[1] * B1;
+          }
         }
       }
 #pragma unroll
