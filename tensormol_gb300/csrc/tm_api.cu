@@ -572,12 +572,12 @@ static int build_layout(tm_system* s, int N, int nmol, const int32_t* Z, const i
     for (int64_t i = off[q]; i < off[q + 1]; ++i) L.mol[i] = q;
   L.off32.resize(nmol + 1);
   for (int q = 0; q <= nmol; ++q) L.off32[q] = (int32_t)off[q];
-  // chunks of at most 1024 atoms of one molecule (two-level reductions)
+  // chunks of at most TM_CHUNK atoms of one molecule (two-level reductions)
   L.mol_chunk.assign(nmol + 1, 0);
   for (int q = 0; q < nmol; ++q) {
     L.mol_chunk[q] = (int32_t)L.chunks.size();
-    for (int64_t b = off[q]; b < off[q + 1]; b += 1024)
-      L.chunks.push_back(make_int2((int)b, (int)std::min<int64_t>(b + 1024, off[q + 1])));
+    for (int64_t b = off[q]; b < off[q + 1]; b += TM_CHUNK)
+      L.chunks.push_back(make_int2((int)b, (int)std::min<int64_t>(b + TM_CHUNK, off[q + 1])));
   }
   L.mol_chunk[nmol] = (int32_t)L.chunks.size();
   L.nchunk = (int)L.chunks.size();
@@ -926,7 +926,7 @@ int tm_system_create_capacity(tm_model* m, int N_cap, int nmol_cap, tm_system** 
   s->ctx = ctx;
   const int nele = m->k.nele;
   const int Mpad_cap = ((N_cap + TM_BM - 1) / TM_BM + nele) * TM_BM;
-  const int nchunk_cap = N_cap / 1024 + nmol_cap;
+  const int nchunk_cap = N_cap / TM_CHUNK + nmol_cap;
   const int rc = system_alloc(s, N_cap, nmol_cap, Mpad_cap, nchunk_cap, 2 * N_cap + 64 * nmol_cap,
                               N_cap / 8 + 8 * nmol_cap);
   if (rc) {

@@ -33,7 +33,7 @@ namespace {
 constexpr float kBand = 1e-5f;
 
 // Per-molecule sums in two fixed-order levels: one block per chunk of at most
-// 1024 atoms of one molecule, then one warp per molecule over its chunks.
+// TM_CHUNK atoms of one molecule, then one warp per molecule over its chunks.
 template <int NV>
 __device__ __forceinline__ void block_sum_store(double (&v)[NV], double* __restrict__ dst) {
   __shared__ double sh[NV][256];

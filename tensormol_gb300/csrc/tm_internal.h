@@ -15,6 +15,7 @@
 #define TM_MAX_HIDDEN 4
 #define TM_BN 256          // padding of the hidden width H and descriptor width Dp
 #define TM_KINK_LAYERS 8   // entry counters of the relu refinement (one per forward layer)
+#define TM_CHUNK 256      // atoms per reduction chunk (one block, one atom per thread)
 #define TM_BM 128          // GEMM M tile (rows per element are padded to this)
 #define TM_EE_SPLIT 25     // warps sharing one centre block's half stencil (one
                            // (x, y) column each at a 3-cell reach)
@@ -241,7 +242,7 @@ struct tm_system {
   double* d_F = nullptr;               // [N][3] force (J/mol/A)
   double* d_mol_E = nullptr;           // [nmol][4]
   double* d_mol_aux = nullptr;         // [nmol][8]: sum q, sum dEdq~, dipole xyz
-  // chunks of at most 1024 atoms of one molecule (two-level reductions)
+  // chunks of at most TM_CHUNK atoms of one molecule (two-level reductions)
   int nchunk = 0;
   int2* d_chunk = nullptr;             // [nchunk] (begin, end)
   int32_t* d_mol_chunk = nullptr;      // [nmol+1] first chunk of each molecule

@@ -139,7 +139,7 @@ __device__ tm_grid grid_from_bbox(double* mn, double* mx, int a0, int a1, double
   }
 }
 
-// Partial bounding boxes of chunks (<= 1024 atoms of one molecule) from the
+// Partial bounding boxes of chunks (<= TM_CHUNK atoms of one molecule) from the
 // FP32 hi parts: the grid origin only has to be close to the minimum, since an
 // atom a rounding error outside the box is clamped into the edge cell, which
 // keeps every pair within the cutoff in adjacent cells.

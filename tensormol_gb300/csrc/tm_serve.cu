@@ -121,7 +121,7 @@ __global__ void k_fire_gather(const int32_t* __restrict__ msrc, int nmol, const 
   np2[q] = o >= 0 ? np[o] : 0;
 }
 
-// per chunk (<= 1024 atoms of one molecule): F.v, F.F, v.v, max |F|^2
+// per chunk (<= TM_CHUNK atoms of one molecule): F.v, F.F, v.v, max |F|^2
 __global__ void k_fire_chunk(const int2* __restrict__ chunk, const int32_t* __restrict__ mol,
                              const int32_t* __restrict__ mode, const double* __restrict__ F,
                              const double* __restrict__ v, double* __restrict__ part) {
