@@ -41,7 +41,14 @@ METRIC = "atom-steps/s E+F, fused adjoint vs plain autograd, 1 GB300; serve p50/
 UNIT = "atom-steps/s"
 # DRAM bytes of the six k_gemm launches of one evaluation (one ncu capture; the
 # k_gemm summary under profiles/ gives the command and the per-launch figures)
-GEMM_DRAM_BYTES_PER_STEP = 2_278_800_000
+GEMM_DRAM_BYTES_PER_STEP = 2_275_904_000
+# Warp instructions per evaluation of the instruction-issue-bound kernels on
+# this workload (smsp__inst_executed.sum, one ncu capture; the
+# instruction-count summary under profiles/ gives the command). Their
+# roofline is the issue rate: 4 warp instructions per clock per SM.
+ISSUE_INST_PER_STEP = {"descriptors": {"k_desc_fwd": 114_775_011},
+                       "adjoint_gather": {"k_desc_adj": 135_380_912, "k_force_gather": 11_101_129},
+                       "pair_terms": {"k_coulomb": 213_111_838}}
 WORKLOAD = ("water cube: 8,000 H2O = 24,000 atoms, open boundary, O on a 3.1 A lattice "
             "+-0.2 A jitter, single energy+force")
 
@@ -725,6 +732,18 @@ def main():
         stage_roof[k_] = {"bound": "hbm", "algorithmic_bytes": int(b_), "achieved_gbs": gbs,
                           "peak_gbs": hbm, "frac": gbs / hbm}
     stage_roof["pair_terms"]["pair_evaluations_per_s"] = 2 * Pee / (stages["pair_terms"] * 1e-3)
+    # the same stages against the instruction issue rate (their bound)
+    nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    issue_peak = 4.0 * nsm * mhz * 1e6   # warp instructions per second
+    issue_roof = {}
+    for k_, kern in ISSUE_INST_PER_STEP.items():
+        inst = float(sum(kern.values()))
+        if inst <= 0:
+            continue
+        ach = inst / (stages[k_] * 1e-3)
+        issue_roof[k_] = {"bound": "issue", "warp_instructions": kern, "achieved": ach,
+                          "peak": issue_peak, "unit": "warp inst/s", "frac": ach / issue_peak}
     stage_roof["counts"] = {"atoms": N, "pairs": P, "triples": T, "ee_pairs_i_lt_j": Pee}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -737,7 +756,7 @@ def main():
             "e2e": {"value": ws * natoms / (e2e_ms / 1000.0), "unit": UNIT, "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches), "clocks": clocks, "stages_ms": stages, "roofline": roof,
-            "stage_rooflines": stage_roof,
+            "stage_rooflines": stage_roof, "issue_rooflines": issue_roof,
             "bf16": {"value": natoms / (ms16 / 1000.0), "ms_per_step": ms16},
             "plain_autograd": plain,
             "serve": serving,
@@ -745,11 +764,6 @@ def main():
             "chno512": chno,
             "published_reference": {"value": 274.0, "unit": UNIT, "hardware": "2015 Core i7, 1 core",
                                     "source": "24,000 atoms / ~87.5 s read off doc/images/Timings.png"}}
-    if rank == 0:
-        try:
-            c = s  # noqa: F841
-        except Exception:
-            pass
     if not args.no_cpu and rank == 0:
         ref, t_cpu = oracle_eval(w, eles, W)
         line["cpu_baseline"] = {"value": natoms / t_cpu, "unit": UNIT, "cores": os.cpu_count(),

@@ -268,9 +268,10 @@ int tm_serve_read(tm_serve *sv, int mol, double *x, double *v, double *F);
  * zeros. Returns TM_E_ARG for natoms > 32768, TM_E_CAPACITY when a row
  * overflowed (then retry with KR/KA >= needed). Runs on `stream` and
  * synchronises it before returning.
- * The first call on a device looks up the scratch's device address, so make
- * it before any stream capture. Every call reuses the same scratch (it clears
- * what must start at zero); calls that overlap on the GPU race.
+ * Every call copies counts to the host and synchronises `stream`, so it is
+ * never made on a capturing stream (TM_E_ARG). Every call reuses the same
+ * scratch (it clears what must start at zero); calls that overlap on the GPU
+ * race.
  */
 int tm_nlist_build_static(const double *x, const int32_t *elem, int natoms, double r_rc,
                           double a_rc, int32_t *cnt_r, uint32_t *nbr_r, int KR, int32_t *cnt_a,

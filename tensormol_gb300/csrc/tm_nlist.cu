@@ -1467,6 +1467,11 @@ extern "C" int tm_nlist_build_static(const double* x, const int32_t* elem, int n
   }
   StaticScratch* S = g_static_ptr[dev];
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // the call copies counts to the host and synchronises the stream: neither
+  // may happen inside a stream capture
+  cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap_status) != cudaSuccess) return TM_E_CUDA;
+  if (cap_status != cudaStreamCaptureStatusNone) return TM_E_ARG;
   const int N = natoms;
   const int cap = 2 * N + 64;
   k_static_init<<<tm_div_up(N, 256), 256, 0, st>>>(S, N);

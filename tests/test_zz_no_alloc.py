@@ -87,3 +87,41 @@ def test_static_nlist_matches_regular_twice_in_a_row():
     tc, _ = orc.nlist_entries(big.x, PARAMS["AN1_a_Rc"])
     assert need == (np.bincount(ref[:, 0]).max(), np.bincount(tc).max())
     model.close()
+
+
+def test_static_nlist_refuses_a_capturing_stream():
+    """The entry point copies counts to the host and synchronises its stream,
+    which a stream capture forbids: on a capturing stream it returns TM_E_ARG
+    before it enqueues anything, and the capture stays valid."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from tensormol_gb300 import _lib
+    from tensormol_gb300.model import BPEEModel
+    eles = [1, 8]
+    W = systems.random_weights(eles, descriptor_width(2), seed=7)
+    model = BPEEModel(eles, W, precision="fp32")
+    small = systems.water_cluster_60(seed=0)
+    elem = (small.Z == 8).astype(np.int32)
+    _static_lists(model.lib, small.x, elem)     # first call outside any capture
+    n, KR, KA = small.x.shape[0], 64, 48
+    xd = torch.tensor(small.x, dtype=torch.float64, device="cuda")
+    ed = torch.tensor(elem, dtype=torch.int32, device="cuda")
+    out = [torch.zeros(k, dtype=torch.int32, device="cuda") for k in (n, n * KR, n, n * KA)]
+    y = torch.zeros(4, device="cuda")
+    need = (ctypes.c_int32 * 2)()
+    g = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(g, stream=s):
+        rc = model.lib.tm_nlist_build_static(
+            ctypes.c_void_p(xd.data_ptr()), ctypes.c_void_p(ed.data_ptr()), n, PARAMS["AN1_r_Rc"],
+            PARAMS["AN1_a_Rc"], ctypes.c_void_p(out[0].data_ptr()), ctypes.c_void_p(out[1].data_ptr()),
+            KR, ctypes.c_void_p(out[2].data_ptr()), ctypes.c_void_p(out[3].data_ptr()), KA, need,
+            ctypes.c_void_p(s.cuda_stream))
+        y += 1.0
+    assert rc == _lib.ERROR_CODES["TM_E_ARG"], rc
+    g.replay()
+    torch.cuda.synchronize()
+    assert float(y.sum()) == 4.0
+    model.close()
