@@ -760,6 +760,7 @@ static int system_alloc(tm_system* s, int N_cap, int nmol_cap, int Mpad_cap, int
     A.get(&s->G3[h], 2 * Mp * H * es);
   }
   A.get(&s->dEdG, sizeof(float) * 2 * Mp * Dp);
+  if (m->k.act == TM_ACT_RELU) A.get(&s->relu_mask, sizeof(uint32_t) * TM_MAX_HIDDEN * 2 * Mp * (H / 32));
   A.get(&s->epart, sizeof(float) * 2 * Mp * tm_gemm_row_parts(m->desc.precision, H));
   if (m->kink) {
     const size_t parts = tm_gemm_row_parts(m->desc.precision, H);
@@ -958,7 +959,8 @@ static void system_free(tm_system* s) {
                   s->d_cnt_a, s->d_nbr_r, s->d_nbr_a, s->d_rev_r, s->d_rev_a, s->d_sr, s->d_va,
                   s->dEdG, s->epart, s->d_Eatom, s->d_qraw, s->d_q, s->d_dEdq, s->d_fself,
                   s->d_fcv, s->d_ecv, s->d_F, s->d_mol_E, s->d_mol_aux, s->d_xuser, s->kink_g2, s->kink_h2[0],
-                  s->kink_h2[1], s->kink_mask, s->kink_count, s->kink_rows, s->kink_nrows};
+                  s->kink_h2[1], s->kink_mask, s->kink_count, s->kink_rows, s->kink_nrows,
+                  s->relu_mask};
   for (void* p : ptrs)
     if (p) cudaFreeAsync(p, ctx->stream);
   for (int h = 0; h < 2; ++h) {

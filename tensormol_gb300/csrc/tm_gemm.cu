@@ -59,6 +59,11 @@ struct GemmArgs {
   void* out0;
   void* out1;
   int ldo;
+  // relu: the backward pass takes act'(z) = [z > 0] from one bit per unit that
+  // the forward pass of the layer wrote (and the refinement corrected), not
+  // from the stored activation
+  uint32_t* rmask_out;      // [2][Mpad][N/32] (forward, hidden layers), or null
+  const uint32_t* rmask_in; // [2][Mpad][N/32] (backward), or null
   const void* hprev0;
   const void* hprev1;
   tm_dev_status* st;
@@ -276,12 +281,16 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* b) {
 
 // Epilogue warps of one instantiation: eight (two per tensor-memory lane
 // quarter, each with half of the tile's columns), except for the FP32 backward
-// pass, whose four warps bring the previous activation's hi and lo parts in
-// with one bulk tensor load into an 8 KB box each (the same shared memory).
-template <int PREC, int EPI>
+// pass of a smooth activation, whose four warps bring the previous
+// activation's hi and lo parts in with one bulk tensor load into an 8 KB box
+// each (the same shared memory).
+template <int PREC, int EPI, int ACT>
 struct EpiShape {
-  static constexpr int WARPS =
-      (PREC == TM_PREC_FP32 && EPI == EPI_BWD && Cfg<PREC>::EPI_BYTES < 8 * 8192) ? 4 : 8;
+  // the FP32 backward pass loads the previous activation into the staging
+  // boxes (hi and lo side by side, 8 KB per warp), except with relu, whose
+  // derivative comes from the forward pass's bits
+  static constexpr bool BOXLOAD = PREC == TM_PREC_FP32 && EPI == EPI_BWD && ACT != TM_ACT_RELU;
+  static constexpr int WARPS = (BOXLOAD && Cfg<PREC>::EPI_BYTES < 8 * 8192) ? 4 : 8;
   static constexpr int WB = Cfg<PREC>::EPI_BYTES / WARPS;   // staging bytes per warp
   static constexpr int THREADS = 32 * (WARPS + 2);
   // FP32: hi and lo boxes side by side (8 KB per warp), else one 4 KB box
@@ -296,7 +305,7 @@ struct EpiShape {
 // tile boundaries; the MMA issuer alternates between two 256-column TMEM
 // tile buffers, so the epilogue of tile t overlaps the MMAs of tile t + 1.
 template <int PREC, int EPI, int ACT>
-__global__ void __launch_bounds__(EpiShape<PREC, EPI>::THREADS, 1) k_gemm(const __grid_constant__ GemmArgs g) {
+__global__ void __launch_bounds__(EpiShape<PREC, EPI, ACT>::THREADS, 1) k_gemm(const __grid_constant__ GemmArgs g) {
   using C = Cfg<PREC>;
   constexpr int BN = C::BN;
   constexpr bool KINK = PREC == TM_PREC_FP32 && ACT == TM_ACT_RELU && (EPI == EPI_FWD || EPI == EPI_FWD_LAST);
@@ -313,9 +322,10 @@ __global__ void __launch_bounds__(EpiShape<PREC, EPI>::THREADS, 1) k_gemm(const 
   uint64_t* ebar = acce + 2;            // [8] previous-activation loads (FP32 backward),
                                         // one per epilogue warp
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(ebar + 8);
-  constexpr int EW = EpiShape<PREC, EPI>::WARPS;
-  constexpr bool BOXLOAD = PREC == TM_PREC_FP32 && EPI == EPI_BWD;
-  constexpr bool PAIRBOX = EpiShape<PREC, EPI>::PAIRBOX;
+  constexpr int EW = EpiShape<PREC, EPI, ACT>::WARPS;
+  constexpr bool BOXLOAD = EpiShape<PREC, EPI, ACT>::BOXLOAD;
+  constexpr bool RMASK = ACT == TM_ACT_RELU && (EPI == EPI_FWD || EPI == EPI_BWD);
+  constexpr bool PAIRBOX = EpiShape<PREC, EPI, ACT>::PAIRBOX;
   static_assert(!BOXLOAD || PAIRBOX, "the FP32 backward pass loads hi and lo boxes together");
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
@@ -439,7 +449,7 @@ __global__ void __launch_bounds__(EpiShape<PREC, EPI>::THREADS, 1) k_gemm(const 
     // activation of its rows with vector loads.
     const int quad = warp & 3, half = EW == 8 ? warp >> 2 : 0;
     constexpr int HALF = EW == 8 ? BN / 2 : BN;   // columns per warp
-    float* ebox = reinterpret_cast<float*>(smem + C::NSTAGE * C::STAGE + warp * EpiShape<PREC, EPI>::WB);
+    float* ebox = reinterpret_cast<float*>(smem + C::NSTAGE * C::STAGE + warp * EpiShape<PREC, EPI, ACT>::WB);
     float* ebl = ebox + 1024;   // FP32 with 8 KB per warp: the lo box
     int eph = 0;                // uses of this warp's load barrier
     bool eok = true;
@@ -495,7 +505,9 @@ __global__ void __launch_bounds__(EpiShape<PREC, EPI>::THREADS, 1) k_gemm(const 
         // and output weights (same for every row): loads issued before the
         // tensor-memory reads
         float h[32];
-        if constexpr (EPI == EPI_BWD && !BOXLOAD) {
+        uint32_t rbits = 0;   // relu backward: this row's bits of these 32 columns
+        if constexpr (EPI == EPI_BWD && RMASK) rbits = g.rmask_in[orow * (g.N >> 5) + (col >> 5)];
+        if constexpr (EPI == EPI_BWD && !BOXLOAD && !RMASK) {
           if constexpr (PREC == TM_PREC_FP32) {
             const float4* ph = reinterpret_cast<const float4*>(
                 static_cast<const float*>(g.hprev0) + orow * g.ldo + col);
@@ -550,7 +562,7 @@ __global__ void __launch_bounds__(EpiShape<PREC, EPI>::THREADS, 1) k_gemm(const 
         }
         float v[32];
         if (EPI == EPI_FWD || EPI == EPI_FWD_LAST) {
-          uint32_t km = 0;
+          uint32_t km = 0, rm = 0;
 #pragma unroll
           for (int q = 0; q < 32; ++q) {
             const float z = __uint_as_float(r[q]) + __shfl_sync(TM_FULL, b_l, q);
@@ -561,12 +573,16 @@ __global__ void __launch_bounds__(EpiShape<PREC, EPI>::THREADS, 1) k_gemm(const 
             act_fwd<ACT>(z, g.alpha, hz, dz);
             if (EPI == EPI_FWD) {
               v[q] = hz;
+              if constexpr (RMASK) rm |= (hz > 0.f ? 1u : 0u) << q;
               if constexpr (KINK) hss = fmaf(v[q], v[q], hss);
             } else {
               const float wq = __shfl_sync(TM_FULL, w_l, q);
               esum += hz * wq;
               v[q] = wq * dz;
             }
+          }
+          if constexpr (RMASK && EPI == EPI_FWD) {
+            if (g.rmask_out) g.rmask_out[orow * (g.N >> 5) + (col >> 5)] = rm;
           }
           if constexpr (KINK) {
             if (g.kmask) g.kmask[((size_t)net * g.Mpad + row) * (g.N >> 5) + (col >> 5)] = km;
@@ -592,8 +608,13 @@ __global__ void __launch_bounds__(EpiShape<PREC, EPI>::THREADS, 1) k_gemm(const 
             }
             __syncwarp();   // every lane has read the boxes before they take the outputs
           }
+          if constexpr (RMASK) {
 #pragma unroll
-          for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]) * actd_h<ACT>(h[q], g.alpha);
+            for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]) * (((rbits >> q) & 1u) ? 1.f : 0.f);
+          } else {
+#pragma unroll
+            for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]) * actd_h<ACT>(h[q], g.alpha);
+          }
         } else {
 #pragma unroll
           for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]);
@@ -735,7 +756,7 @@ int launch_gemm(tm_ctx* ctx, const GemmArgs& g0, int mtiles) {
   g.ntiles = ntiles;
   const int total = 2 * mtiles * ntiles;
   const int grid = total < ctx->num_sms ? total : ctx->num_sms;
-  k_gemm<PREC, EPI, ACT><<<grid, EpiShape<PREC, EPI>::THREADS, C::SMEM, ctx->stream>>>(g);
+  k_gemm<PREC, EPI, ACT><<<grid, EpiShape<PREC, EPI, ACT>::THREADS, C::SMEM, ctx->stream>>>(g);
   ctx->launches++;
   return tm_cuda_check(ctx, cudaGetLastError(), "gemm");
 }
@@ -791,6 +812,7 @@ struct KinkArgs {
   const float* wout;      // [2][nele][N]
   const int32_t* tile_elem;
   const uint32_t* kmask;  // [2][Mpad][N/32]
+  uint32_t* rmask;        // hidden layers: the relu bits the backward pass reads (or null)
   const uint32_t* rows;   // entries orow * parts + part (appended by the layer kernel)
   const uint32_t* nrows;
   int parts, part_cols;   // column parts per row and their width
@@ -881,6 +903,12 @@ __global__ void __launch_bounds__(256) k_kink_refine(const KinkArgs a) {
           const size_t o = ((size_t)net * a.Mpad + r) * a.N + col;
           a.o_hi[o] = hi;
           a.o_lo[o] = lo;
+          if (!LAST && a.rmask) {
+            unsigned int* wd = a.rmask + (o >> 5);
+            const unsigned int bit = 1u << (col & 31);
+            if (z > 0.f) atomicOr(wd, bit);
+            else atomicAnd(wd, ~bit);
+          }
         }
         ++nref;
       }
@@ -1010,6 +1038,8 @@ static int mlp_layers(tm_system* s, bool forward, bool backward, cudaEvent_t* ev
     g.out1 = last ? s->G3[1] : bufH[l][1];
     g.o0 = last ? s->ts_G3[0] : *stH[l][0];
     g.o1 = last ? s->ts_G3[1] : *stH[l][1];
+    g.rmask_out = (m->k.act == TM_ACT_RELU && !last && s->relu_mask)
+                      ? s->relu_mask + (size_t)l * 2 * s->Mpad * (H / 32) : nullptr;
     if (kink) {
       g.kmask = s->kink_mask;
       g.wnorm = m->kwn[l];
@@ -1041,6 +1071,7 @@ static int mlp_layers(tm_system* s, bool forward, bool backward, cudaEvent_t* ev
       ka.Mpad = s->Mpad;
       ka.nele = m->k.nele;
       ka.count = s->kink_count;
+      ka.rmask = g.rmask_out;
       ka.rows = s->kink_rows;
       ka.nrows = s->kink_nrows + l;
       ka.parts = nparts;
@@ -1050,6 +1081,7 @@ static int mlp_layers(tm_system* s, bool forward, bool backward, cudaEvent_t* ev
   }
   g.kmask = nullptr;
   g.hn2_out = nullptr;
+  g.rmask_out = nullptr;
   if (!backward) return TM_OK;
   for (int l = L - 1; l >= 0; --l) {
     // A = g_{l+1} (level l+1 buffer), B = W_l as [Kin x Nout] rows
@@ -1067,6 +1099,8 @@ static int mlp_layers(tm_system* s, bool forward, bool backward, cudaEvent_t* ev
       g.ldo = H;
       g.hprev0 = bufH[l - 1][0];
       g.hprev1 = bufH[l - 1][1];
+      g.rmask_in = (m->k.act == TM_ACT_RELU && s->relu_mask)
+                       ? s->relu_mask + (size_t)(l - 1) * 2 * s->Mpad * (H / 32) : nullptr;
       g.out0 = bufH[l - 1][0];
       g.out1 = bufH[l - 1][1];
       g.o0 = *stH[l - 1][0];

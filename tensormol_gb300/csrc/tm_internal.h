@@ -223,6 +223,9 @@ struct tm_system {
                                        //   buffers alternating between layers
   uint32_t* kink_mask = nullptr;       // [2][Mpad][H/32]
   uint32_t* kink_rows = nullptr;       // [2][Mpad][row parts] (row, part) entries with flags
+  // relu networks: one bit per hidden unit, [z > 0], of each hidden layer
+  // (written by the forward pass, read by the backward pass)
+  uint32_t* relu_mask = nullptr;       // [TM_MAX_HIDDEN][2][Mpad][H/32]
   uint32_t* kink_nrows = nullptr;      // [TM_KINK_LAYERS] entries per forward layer
   unsigned long long* kink_count = nullptr;
   CUtensorMap tm_G[2], tm_H1[2], tm_H2[2], tm_G3[2];
