@@ -493,10 +493,84 @@ __global__ void __launch_bounds__(128) k_nbr_build(const NbrArgs a) {
   const int lc = a.cell_of[i] - g.cell_off;
   const int iz = lc % g.nz, iy = (lc / g.nz) % g.ny, ix = lc / (g.nz * g.ny);
   int nr = 0, na = 0;
+  if constexpr (!PERIODIC) {
+    // Open boundary: the three cells of each of the 9 (x, y) columns are one
+    // contiguous run of atoms (cell order). Lanes 0..8 load the 9 runs'
+    // bounds at once, the runs are laid end to end as one candidate index
+    // space, and each iteration takes two chunks of 32 candidates with their
+    // loads in flight together (the rows are sorted at the end, so the order
+    // in which candidates are met does not matter).
+    int ct0 = 0, clen = 0;
+    if (lane < 9) {
+      const int jx = ix + lane / 3 - 1, jy = iy + lane % 3 - 1;
+      if (jx >= 0 && jx < g.nx && jy >= 0 && jy < g.ny) {
+        const int cbase = g.cell_off + (jx * g.ny + jy) * g.nz;
+        ct0 = a.cell_start[cbase + max(iz - 1, 0)];
+        clen = a.cell_start[cbase + min(iz + 1, g.nz - 1) + 1] - ct0;
+      }
+    }
+    int incl = clen;
+#pragma unroll
+    for (int o = 1; o < 16; o <<= 1) {
+      const int v = __shfl_up_sync(TM_FULL, incl, o);
+      if (lane >= o) incl += v;
+    }
+    int pre[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) pre[q] = __shfl_sync(TM_FULL, incl, q);
+    const int total = pre[8];
+    const int excl = incl - clen;
+    // candidate f of the flattened runs: its run k and its atom slot t
+    auto slot = [&](int f) {
+      int k = 0;
+#pragma unroll
+      for (int q = 0; q < 9; ++q) k += f >= pre[q] ? 1 : 0;
+      k = min(k, 8);
+      return __shfl_sync(TM_FULL, ct0, k) + (f - __shfl_sync(TM_FULL, excl, k));
+    };
+    auto take = [&](bool valid, int j, float4 hj, float4 lj) {
+      bool in_r = false, in_a = false;
+      uint64_t key = 0;
+      if (valid && j != i) {
+        const float dx = ds_sub(hi.x, lo.x, hj.x, lj.x);
+        const float dy = ds_sub(hi.y, lo.y, hj.y, lj.y);
+        const float dz = ds_sub(hi.z, lo.z, hj.z, lj.z);
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        if (d2 <= a.rr2_hi) {
+          const double xj = a.x[3 * j], yj = a.x[3 * j + 1], zj = a.x[3 * j + 2];
+          in_r = d2 < a.rr2_lo ? true : tm_exact_within(xi, yi, zi, xj, yj, zj, a.rr);
+          if (in_r) in_a = d2 < a.ra2_lo ? true
+                           : (d2 <= a.ra2_hi ? tm_exact_within(xi, yi, zi, xj, yj, zj, a.ra) : false);
+          key = nbr_key(__float_as_int(hj.w), TM_IMG_SELF, j - g.atom_off);
+        }
+      }
+      const unsigned mr = __ballot_sync(TM_FULL, in_r);
+      const unsigned ma = __ballot_sync(TM_FULL, in_a);
+      if (in_r) {
+        const int p = nr + __popc(mr & lanemask_lt());
+        if (p < a.KR) kr[p] = key;
+      }
+      if (in_a) {
+        const int p = na + __popc(ma & lanemask_lt());
+        if (p < a.KA) ka[p] = key;
+      }
+      nr += __popc(mr);
+      na += __popc(ma);
+    };
+    for (int f0 = 0; f0 < total; f0 += 64) {
+      const int fa = f0 + lane, fb = f0 + 32 + lane;
+      const bool va = fa < total, vb = fb < total;
+      const int ta = slot(fa), tb = slot(fb);
+      const int ja = va ? a.cell_atoms[ta] : i, jb = vb ? a.cell_atoms[tb] : i;
+      const float4 ha = a.xhi[ja], la = a.xlo[ja], hb = a.xhi[jb], lb = a.xlo[jb];
+      take(va, ja, ha, la);
+      take(vb, jb, hb, lb);
+    }
+  }
   // the three cells of a z column without a periodic wrap are one contiguous
   // run of atoms (cell order); a wrapped column is taken cell by cell
   const bool zrun = !PERIODIC || (iz >= 1 && iz + 1 < g.nz);
-  for (int ox = -1; ox <= 1; ++ox) {
+  for (int ox = -1; ox <= 1 && PERIODIC; ++ox) {
     for (int oy = -1; oy <= 1; ++oy) {
       for (int oz = zrun ? 0 : -1; oz <= (zrun ? 0 : 1); ++oz) {
         int jx = ix + ox, jy = iy + oy, jz = iz + oz, sx = 0, sy = 0, sz = 0;
