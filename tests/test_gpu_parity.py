@@ -204,14 +204,18 @@ def test_energy_force_periodic(gpu):
     assert dFr < F_TOL, dFr
 
 
-def test_bf16_error_is_reported(gpu):
+@pytest.mark.parametrize("act", ["sigmoid_with_param", "relu"])
+def test_bf16_error_is_reported(gpu, act):
+    """BF16 networks (one pass, FP32 accumulate) against the FP64 oracle:
+    errors stated, not FP32-level. With relu the backward pass takes act'(z)
+    from the forward pass's bits instead of the stored activation."""
     w = systems.water_cluster_60(seed=0)
-    m, om = _model(gpu, [1, 8], "sigmoid_with_param", prec="bf16")
+    m, om = _model(gpu, [1, 8], act, prec="bf16")
     s = m.system(w.x, w.Z, w.offsets)
     out = s.energy_force(w.x, True)
     ref = orc.OpenSystemOracle(om, w.x, w.Z, w.offsets).terms(w.x)
     dE, dF = _errors(out, ref, w.natoms)
-    print(f"BF16 water60: dE/atom={dE:.2e} eV  max|dF|={dF:.2e} eV/A")
+    print(f"BF16 water60 ({act}): dE/atom={dE:.2e} eV  max|dF|={dF:.2e} eV/A")
     assert np.isfinite(dE) and np.isfinite(dF) and dE < 1e-2 and dF < 1.0
 
 
