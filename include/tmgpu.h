@@ -315,7 +315,8 @@ int tm_system_descriptors(tm_system *s, float *G_out);
  * the last evaluation, out[2][natoms][hidden[layer]] (net 0 = energy, 1 =
  * charge; atoms in input order): the activations h = act(z) of a hidden layer
  * before the last, and w_out * act'(z) (the backward pass's seed) for the last
- * one. Valid after an evaluation with TM_F_ENERGY_ONLY (the backward pass
+ * one; for relu networks in FP32 mode the last one is act'(z) in {0, 1} (the
+ * output weights are folded into the backward pass's first weights). Valid after an evaluation with TM_F_ENERGY_ONLY (the backward pass
  * reuses these buffers). No counterpart in the reference (TensorFlow keeps
  * its intermediate tensors internal).
  */

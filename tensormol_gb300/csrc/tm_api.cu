@@ -409,6 +409,25 @@ extern "C" int tm_model_finalize(tm_model* m) {
         for (int o = 0; o < Lh.fan_out; ++o) bias[blk * H + o] = (float)Lh.b[o];
       }
     if ((rc = upload_split(m, fwd, m->w_fwd[l])) || (rc = upload_split(m, bwd, m->w_bwd[l]))) return rc;
+    if (m->kink && l == L - 1) {
+      // the output weights folded into the last layer's backward weights
+      // (products in FP64, then split)
+      std::vector<float> bwdf(bwd.size(), 0.f);
+      for (int net = 0; net < 2; ++net)
+        for (int e = 0; e < nele; ++e) {
+          const tm_layer_host& Lh = layer(net, e, l);
+          const tm_layer_host& Lo = layer(net, e, L);
+          const size_t blk = (size_t)net * nele + e;
+          for (int i = 0; i < Lh.fan_in; ++i)
+            for (int o = 0; o < Lh.fan_out; ++o)
+              bwdf[(blk * Kin + i) * H + o] = (float)(Lh.W[(size_t)i * Lh.fan_out + o] * Lo.W[o]);
+        }
+      if (m->w_bwd_fold[0]) {   // finalized before: replace
+        tm_free(ctx, m->w_bwd_fold[0], bwdf.size() * 4);
+        tm_free(ctx, m->w_bwd_fold[1], bwdf.size() * 4);
+      }
+      if ((rc = upload_split(m, bwdf, m->w_bwd_fold))) return rc;
+    }
     if (m->kink) {
       // the weights and biases as given (FP64) and the norm of each unit's
       // weight vector, for the relu refinement (tm_gemm.cu)
@@ -457,6 +476,10 @@ extern "C" int tm_model_finalize(tm_model* m) {
         (rc = tm_make_tmap(ctx, &m->tm_wb[l][0], m->w_bwd[l][0], eb, (uint64_t)2 * nele * Kin, H, bn)) ||
         (rc = tm_make_tmap(ctx, &m->tm_wb[l][1], m->w_bwd[l][1], eb, (uint64_t)2 * nele * Kin, H, bn)))
       return rc;
+    if (m->w_bwd_fold[0] && l == L - 1 &&
+        ((rc = tm_make_tmap(ctx, &m->tm_wbf[0], m->w_bwd_fold[0], eb, (uint64_t)2 * nele * Kin, H, bn)) ||
+         (rc = tm_make_tmap(ctx, &m->tm_wbf[1], m->w_bwd_fold[1], eb, (uint64_t)2 * nele * Kin, H, bn))))
+      return rc;
   }
   std::vector<float> wout((size_t)2 * nele * H, 0.f);
   std::vector<double> bout((size_t)2 * nele, 0.0);
@@ -495,6 +518,11 @@ extern "C" int tm_model_destroy(tm_model* m) {
       tm_free(ctx, m->kb2[l], (size_t)2 * nele * H * 8);
       tm_free(ctx, m->kwn[l], (size_t)2 * nele * H * 4);
     }
+  }
+  if (m->w_bwd_fold[0]) {
+    const size_t nf = (size_t)2 * nele * (m->nlayer == 1 ? Dp : H) * H * 4;
+    tm_free(ctx, m->w_bwd_fold[0], nf);
+    tm_free(ctx, m->w_bwd_fold[1], nf);
   }
   tm_free(ctx, m->wout, (size_t)2 * nele * H * 4);
   tm_free(ctx, m->bout, (size_t)2 * nele * 8);
@@ -1280,6 +1308,8 @@ extern "C" int tm_system_layer_outputs(tm_system* s, int layer, float* out) {
   void* const* buf = layer == L - 1 ? s->G3 : (layer == 0 ? s->H1 : s->H2);
   const size_t n = (size_t)2 * s->Mpad * H;
   const bool split = m->desc.precision == TM_PREC_FP32;
+  // FP32 relu: the last layer holds act'(z) in {0, 1}, one plane
+  const bool one_plane = split && layer == L - 1 && m->w_bwd_fold[0];
   std::vector<float> hi(n), lo(split ? n : 0);
   std::vector<uint16_t> b16(split ? 0 : n);
   int rc;
@@ -1298,7 +1328,7 @@ extern "C" int tm_system_layer_outputs(tm_system* s, int layer, float* out) {
       float* dst = out + ((size_t)net * Nu + i) * width;
       for (int c = 0; c < width; ++c) {
         if (split) {
-          dst[c] = hi[src + c] + lo[src + c];
+          dst[c] = one_plane ? hi[src + c] : hi[src + c] + lo[src + c];
         } else {
           const uint32_t u = (uint32_t)b16[src + c] << 16;
           memcpy(&dst[c], &u, 4);

@@ -84,6 +84,9 @@ struct GemmArgs {
   // loads are withheld (-1: none), so that the MMA issuer's wait runs out
   long long wait_limit;
   int skip_it;
+  // A has no lo part (FP32: the relu seed act'(z) in {0, 1}, exact in TF32):
+  // its lo loads and the A_lo B_hi instruction are skipped
+  int a_single;
 };
 
 // ---- PTX wrappers ---------------------------------------------------------
@@ -325,6 +328,9 @@ __global__ void __launch_bounds__(EpiShape<PREC, EPI, ACT>::THREADS, 1) k_gemm(c
   constexpr int EW = EpiShape<PREC, EPI, ACT>::WARPS;
   constexpr bool BOXLOAD = EpiShape<PREC, EPI, ACT>::BOXLOAD;
   constexpr bool RMASK = ACT == TM_ACT_RELU && (EPI == EPI_FWD || EPI == EPI_BWD);
+  // FP32 relu, last layer: the backward seed is act'(z) in {0, 1} (the output
+  // weights are folded into the first backward launch's weights), one plane
+  constexpr bool FOLD = PREC == TM_PREC_FP32 && ACT == TM_ACT_RELU && EPI == EPI_FWD_LAST;
   constexpr bool PAIRBOX = EpiShape<PREC, EPI, ACT>::PAIRBOX;
   static_assert(!BOXLOAD || PAIRBOX, "the FP32 backward pass loads hi and lo boxes together");
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
@@ -378,12 +384,12 @@ __global__ void __launch_bounds__(EpiShape<PREC, EPI, ACT>::THREADS, 1) k_gemm(c
           }
           if (it == g.skip_it) continue;   // diagnostic: this stage never arrives
           uint8_t* st = smem + s * C::STAGE;
-          mbar_expect_tx(&full[s], C::STAGE);
+          mbar_expect_tx(&full[s], C::STAGE - (g.a_single ? C::A_TILE : 0));
           const int x = kb * C::BK;
           tma_load_2d(st, &g.a0, x, a_row, &full[s]);
           tma_load_2d(st + C::NSPLIT * C::A_TILE, &g.b0, x, b_row, &full[s]);
           if (C::NSPLIT == 2) {
-            tma_load_2d(st + C::A_TILE, &g.a1, x, a_row, &full[s]);
+            if (!g.a_single) tma_load_2d(st + C::A_TILE, &g.a1, x, a_row, &full[s]);
             tma_load_2d(st + 2 * C::A_TILE + C::B_TILE, &g.b1, x, b_row, &full[s]);
           }
         }
@@ -425,7 +431,7 @@ __global__ void __launch_bounds__(EpiShape<PREC, EPI, ACT>::THREADS, 1) k_gemm(c
               // A_hi B_hi -> main, A_hi B_lo -> correction (one instruction: A_hi is
               // read once), then A_lo B_hi -> correction
               umma_tf32(d, ad0, bd0, C::IDESC2, acc);
-              umma_tf32(d + BN, ad1, bd0, C::IDESC, 1u);
+              if (!g.a_single) umma_tf32(d + BN, ad1, bd0, C::IDESC, 1u);
             } else {
               umma_f16(d, ad0, bd0, C::IDESC, acc);
             }
@@ -578,7 +584,7 @@ __global__ void __launch_bounds__(EpiShape<PREC, EPI, ACT>::THREADS, 1) k_gemm(c
             } else {
               const float wq = __shfl_sync(TM_FULL, w_l, q);
               esum += hz * wq;
-              v[q] = wq * dz;
+              v[q] = FOLD ? dz : wq * dz;
             }
           }
           if constexpr (RMASK && EPI == EPI_FWD) {
@@ -655,7 +661,7 @@ __global__ void __launch_bounds__(EpiShape<PREC, EPI, ACT>::THREADS, 1) k_gemm(c
             if (PAIRBOX && EPI != EPI_OUT) tma_store_2d(&g.o1, col, orow0, ebl);
             bulk_commit();
           }
-          if constexpr (EPI != EPI_OUT && !PAIRBOX) {
+          if constexpr (EPI != EPI_OUT && !PAIRBOX && !FOLD) {
             if (lane == 0) bulk_wait_read();
             __syncwarp();
 #pragma unroll
@@ -813,6 +819,7 @@ struct KinkArgs {
   const int32_t* tile_elem;
   const uint32_t* kmask;  // [2][Mpad][N/32]
   uint32_t* rmask;        // hidden layers: the relu bits the backward pass reads (or null)
+  int fold;               // last layer: write act'(z) (the output weights are folded), hi only
   const uint32_t* rows;   // entries orow * parts + part (appended by the layer kernel)
   const uint32_t* nrows;
   int parts, part_cols;   // column parts per row and their width
@@ -897,12 +904,13 @@ __global__ void __launch_bounds__(256) k_kink_refine(const KinkArgs a) {
           tm_two_sum(sh, bb.x, sh, t);
           sl += t + bb.y;
           const float z = sh + sl;
-          const float v = LAST ? (z > 0.f ? a.wout[blk * a.N + col] : 0.f) : (z > 0.f ? z : 0.f);
+          const float v = LAST ? (z > 0.f ? (a.fold ? 1.f : a.wout[blk * a.N + col]) : 0.f)
+                               : (z > 0.f ? z : 0.f);
           float hi, lo;
           tm_tf32_split(v, hi, lo);
           const size_t o = ((size_t)net * a.Mpad + r) * a.N + col;
           a.o_hi[o] = hi;
-          a.o_lo[o] = lo;
+          if (!(LAST && a.fold)) a.o_lo[o] = lo;
           if (!LAST && a.rmask) {
             unsigned int* wd = a.rmask + (o >> 5);
             const unsigned int bit = 1u << (col & 31);
@@ -1072,6 +1080,7 @@ static int mlp_layers(tm_system* s, bool forward, bool backward, cudaEvent_t* ev
       ka.nele = m->k.nele;
       ka.count = s->kink_count;
       ka.rmask = g.rmask_out;
+      ka.fold = last && m->w_bwd_fold[0] ? 1 : 0;
       ka.rows = s->kink_rows;
       ka.nrows = s->kink_nrows + l;
       ka.parts = nparts;
@@ -1092,6 +1101,12 @@ static int mlp_layers(tm_system* s, bool forward, bool backward, cudaEvent_t* ev
     g.a1 = *gA[1];
     g.b0 = m->tm_wb[l][0];
     g.b1 = m->tm_wb[l][1];
+    g.a_single = 0;
+    if (l == L - 1 && m->w_bwd_fold[0]) {   // FP32 relu: seed act'(z), w_out folded into W
+      g.b0 = m->tm_wbf[0];
+      g.b1 = m->tm_wbf[1];
+      g.a_single = 1;
+    }
     g.K = H;
     g.a_net_rows = s->Mpad;
     if (l > 0) {

@@ -101,6 +101,11 @@ struct tm_model {
   double* bout = nullptr;              // [2][nele]
   CUtensorMap tm_wf[TM_MAX_HIDDEN][2];
   CUtensorMap tm_wb[TM_MAX_HIDDEN][2];
+  // FP32 relu networks: the last hidden layer's backward weights with the
+  // output weights folded in, W'[i][o] = W[i][o] w_out[o] (hi, lo); the
+  // backward pass then starts from act'(z) in {0, 1}, one exact plane
+  void* w_bwd_fold[2] = {};
+  CUtensorMap tm_wbf[2];
   size_t elem_size = 4;                // 4 (tf32 split) or 2 (bf16)
   // relu refinement (FP32 precision with relu only): hidden pre-activations
   // within the tensor-core error bound of zero are recomputed in FP64
