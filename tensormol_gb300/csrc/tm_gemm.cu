@@ -6,14 +6,16 @@
 // element of each 128-row tile taken from a table (rows of each element are
 // padded to 128, so no tile mixes elements).
 //
-// Persistent CTAs (one per SM, 192 threads) walk the tiles:
-//   warp 4       TMA producer: K-slices of A and B into a ring of 128-byte-
+// Persistent CTAs (one per SM) walk the tiles:
+//   warp EW      TMA producer: K-slices of A and B into a ring of 128-byte-
 //                swizzled shared-memory stages (cp.async.bulk.tensor, mbarriers)
-//   warp 5       MMA issuer: one elected thread issues tcgen05.mma into FP32
+//   warp EW + 1  MMA issuer: one elected thread issues tcgen05.mma into FP32
 //                accumulators in tensor memory (two tile buffers)
-//   warps 0..3   epilogue: tcgen05.ld 32 columns at a time, fused bias +
-//                activation (forward) or activation-derivative product
-//                (backward), stores to global.
+//   warps 0..EW-1  epilogue (EW = 8, two per tensor-memory lane quarter; 4 for
+//                the FP32 backward pass of a smooth activation): tcgen05.ld 32
+//                columns at a time, fused bias + activation (forward) or
+//                activation-derivative product (backward), staged in shared
+//                memory, bulk tensor stores.
 // Precision modes:
 //   TM_PREC_FP32  kind::tf32 with operands split as x = hi + lo (both rounded
 //                 to nearest TF32, tm_tf32_split); BN = 128. The large term
