@@ -41,7 +41,7 @@ METRIC = "atom-steps/s E+F, fused adjoint vs plain autograd, 1 GB300; serve p50/
 UNIT = "atom-steps/s"
 # DRAM bytes of the six k_gemm launches of one evaluation (one ncu capture; the
 # k_gemm summary under profiles/ gives the command and the per-launch figures)
-GEMM_DRAM_BYTES_PER_STEP = 1_890_944_000
+GEMM_DRAM_BYTES_PER_STEP = 1_706_279_000
 # Warp instructions per evaluation of the instruction-issue-bound kernels on
 # this workload (smsp__inst_executed.sum, one ncu capture; the
 # instruction-count summary under profiles/ gives the command). Their
