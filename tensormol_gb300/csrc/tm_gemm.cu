@@ -1025,6 +1025,10 @@ static int mlp_layers(tm_system* s, bool forward, bool backward, cudaEvent_t* ev
   g.st = ctx->d_status;
   g.skip_it = -1;
   const bool kink = m->kink && s->kink_mask;
+  // FP32 relu: the last forward layer writes act'(z) for the folded backward
+  // weights (a choice the kernel makes at compile time), so they must exist
+  if (prec == TM_PREC_FP32 && m->k.act == TM_ACT_RELU && !m->w_bwd_fold[0])
+    return tm_fail(ctx, TM_E_STATE, "relu model without its folded backward weights");
   const int nparts = tm_gemm_row_parts(prec, H);
   if (forward && kink && s->kink_count) {
     cudaMemsetAsync(s->kink_count, 0, sizeof(unsigned long long), ctx->stream);
